@@ -1,0 +1,70 @@
+// Argument blocks shared by the host runtime and the solver kernels.
+#pragma once
+
+#include <cuda.h>
+#include <stdint.h>
+
+namespace asets {
+
+// Bits of IterControl::error.
+enum DeviceError : int {
+    DEV_ERR_TIMEOUT = 1,  // an mbarrier wait exceeded its budget
+};
+
+// Per-solve control block in device memory.  Every iteration launch reads
+// `done`/`iter` at entry; the last block of the iteration to finish (ticket)
+// records erriter, decides convergence and advances `iter`.
+struct IterControl {
+    int iter;           // index of the next iteration
+    int done;           // converged, maxIt reached, or error
+    int it_num;         // the reference's itNum
+    int last_iter;      // last executed iteration, -1 if none
+    unsigned int ticket;
+    int error;          // DeviceError bits
+    int max_it;
+    int break_lt;       // 1: stop on cvg < errBound (Ishikawa 2D), 0: on <=
+    float err_bound;
+    float denom;        // cvg = (float)erru / denom
+    int alpha_bad;      // set by the validation pass
+    int pad[5];
+};
+
+// Stage slots: which field each TMA box holds.
+enum Slot : int {
+    SL_BC = 0,   // flow on faces normal to the column axis (Matlab x in 3D)
+    SL_BR = 1,   // flow on faces normal to the row axis (Matlab y)
+    SL_BS = 2,   // flow on faces normal to the stream axis (z in 3D, x in 2D)
+    SL_S0 = 3,   // gk source terms: gk = div - ((s0 - s1) + s2/cc)
+    SL_S1 = 4,
+    SL_S2 = 5,
+    SL_ALPHA = 6,
+    NUM_SLOTS = 7
+};
+
+enum Epilogue : int {
+    EPI_BINARY = 0,  // binary model: ps/pt/u update + erriter
+    EPI_DIV = 1,     // multi-label models: write the new flow and its divergence
+};
+
+struct StencilArgs {
+    CUtensorMap map[2][NUM_SLOTS];  // [parity of the source buffers][slot]
+    float *dst_b[2][3];             // [source parity][SL_BC, SL_BR, SL_BS]
+    float *dst_s[2][3];             // binary: ps, pt, u; EPI_DIV: [.][0] = divergence
+    const float *cs;                // binary source/sink capacities (padded layout)
+    const float *ct;
+    IterControl *ctl;
+    double *partials;               // one per block
+    float *cvg;
+    long long pitch;                // padded row pitch (elements)
+    long long plane_stride;         // pitch * nc
+    long long label_stride;         // plane_stride * ns
+    long long total_work;           // labels * tiles * ns tile-planes
+    int nr, nc, ns;                 // rows, columns (1 in 2D), stream length
+    int nlab_items;                 // labels swept by this launch
+    int tiles_r, tiles_c;
+    int lab_mul[NUM_SLOTS];         // label coordinate of slot = k*mul + add
+    int lab_add[NUM_SLOTS];
+    float cc, inv_cc, steps;
+};
+
+}  // namespace asets

@@ -1,0 +1,972 @@
+// Host runtime of libasetscuda: contexts, device-resident solver objects,
+// TMA descriptors, the iteration driver and the C ABI of include/asets.h.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "asets.h"
+#include "internal.h"
+
+using namespace asets;
+
+// ---------------------------------------------------------------- errors
+static thread_local std::string g_last_error;
+
+static asets_status fail(asets_status s, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return s;
+}
+
+static asets_status cuda_fail(cudaError_t e, const char *what)
+{
+    asets_status s = (e == cudaErrorMemoryAllocation) ? ASETS_ERR_OUT_OF_MEMORY : ASETS_ERR_CUDA;
+    cudaGetLastError();  // clear a non-sticky error
+    return fail(s, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CU_TRY(call)                                 \
+    do {                                             \
+        cudaError_t e_ = (call);                     \
+        if (e_ != cudaSuccess)                       \
+            return cuda_fail(e_, #call);             \
+    } while (0)
+
+// RAII: make ctx->device current for the duration of an API call.
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = true;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess)
+            prev = -1;
+        ok = (prev == dev) || (cudaSetDevice(dev) == cudaSuccess);
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev)
+            cudaSetDevice(prev);
+    }
+};
+
+// ---------------------------------------------------------------- context
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+struct asets_context {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    PFN_encodeTiled encode = nullptr;
+    std::recursive_mutex mu;
+    asets_solver *cached = nullptr;  // solver reused by the one-shot calls
+    int *pinned_flags = nullptr;     // host-visible done flags of in-flight chunks
+};
+
+struct asets_solver {
+    asets_context *ctx = nullptr;
+    asets_model model = ASETS_BINARY;
+    int dim = 3, ny = 0, nx = 0, nz = 0, nlab = 1;
+    // kernel view: rows, columns (1 in 2D), stream axis
+    int nr = 0, nc = 0, ns = 0;
+    long long pitch = 0, plane = 0, cells = 0;  // cells = padded cells per label
+    int flow_labels = 1, alpha_labels = 1, ct_labels = 1, pt_labels = 1, u_labels = 1;
+    // device buffers (padded layout)
+    std::vector<void *> allocations;
+    float *cs = nullptr, *ct = nullptr, *alpha = nullptr;
+    float *b[2][3] = {};
+    float *ps[2] = {}, *pt[2] = {}, *u[2] = {};
+    float *dv = nullptr;
+    float *warm_u = nullptr, *warm_ps = nullptr, *warm_pt = nullptr;
+    bool warm = false;
+    bool inputs_set = false;
+    bool alpha_ok = true;
+    IterControl *ctl = nullptr;
+    double *partials = nullptr;
+    int partials_cap = 0;
+    float *cvg = nullptr;
+    int cvg_cap = 0;
+    // results of the last run
+    int last_max_it = 0;
+    int final_parity = 0;
+    float last_ms = 0.f;
+    int last_launches = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t flag_ev[2] = {nullptr, nullptr};
+    // kernel setup cache
+    const StencilVariant *variant = nullptr;
+    int grid = 0;
+    StencilArgs args;
+};
+
+static asets_status get_encoder(asets_context *ctx)
+{
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                     cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+        return fail(ASETS_ERR_CUDA, "cuTensorMapEncodeTiled unavailable from the driver");
+    ctx->encode = reinterpret_cast<PFN_encodeTiled>(fn);
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API int asets_abi_version(void) { return ASETS_ABI_VERSION; }
+
+extern "C" ASETS_API const char *asets_status_string(asets_status s)
+{
+    switch (s) {
+    case ASETS_OK: return "ok";
+    case ASETS_ERR_INVALID_ARG: return "invalid argument";
+    case ASETS_ERR_ALPHA: return "alpha(x) must be positive. Exiting...";
+    case ASETS_ERR_CUDA: return "CUDA error";
+    case ASETS_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case ASETS_ERR_TIMEOUT: return "device wait timed out";
+    case ASETS_ERR_NO_DEVICE: return "no usable sm_103 GPU";
+    case ASETS_ERR_UNSUPPORTED: return "unsupported";
+    }
+    return "unknown status";
+}
+
+extern "C" ASETS_API const char *asets_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" ASETS_API asets_status asets_context_create(int device, asets_context **out)
+{
+    if (!out)
+        return fail(ASETS_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(ASETS_ERR_NO_DEVICE, "no CUDA device (%s)", cudaGetErrorString(e));
+    }
+    if (device < 0 || device >= n)
+        return fail(ASETS_ERR_INVALID_ARG, "device %d out of range (0..%d)", device, n - 1);
+    cudaDeviceProp prop;
+    CU_TRY(cudaGetDeviceProperties(&prop, device));
+    if (!(prop.major == 10 && prop.minor == 3))
+        return fail(ASETS_ERR_NO_DEVICE, "device %d is sm_%d%d; libasetscuda is built for sm_103a",
+                    device, prop.major, prop.minor);
+    DeviceGuard guard(device);
+    if (!guard.ok)
+        return fail(ASETS_ERR_CUDA, "cudaSetDevice(%d) failed", device);
+    std::unique_ptr<asets_context> ctx(new asets_context);
+    ctx->device = device;
+    ctx->num_sms = prop.multiProcessorCount;
+    asets_status s = get_encoder(ctx.get());
+    if (s != ASETS_OK)
+        return s;
+    CU_TRY(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+    ctx->stream = ctx->own_stream;
+    CU_TRY(cudaMallocHost(&ctx->pinned_flags, 64 * sizeof(int)));
+    *out = ctx.release();
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API void asets_solver_destroy(asets_solver *s);
+
+extern "C" ASETS_API void asets_context_destroy(asets_context *ctx)
+{
+    if (!ctx)
+        return;
+    {
+        DeviceGuard guard(ctx->device);
+        if (ctx->cached)
+            asets_solver_destroy(ctx->cached);
+        if (ctx->own_stream) {
+            cudaStreamSynchronize(ctx->own_stream);
+            cudaStreamDestroy(ctx->own_stream);
+        }
+        if (ctx->pinned_flags)
+            cudaFreeHost(ctx->pinned_flags);
+    }
+    delete ctx;
+}
+
+extern "C" ASETS_API asets_status asets_default_context(asets_context **out)
+{
+    static std::mutex mu;
+    static asets_context *ctx = nullptr;
+    static asets_status status = ASETS_OK;
+    static bool tried = false;
+    if (!out)
+        return fail(ASETS_ERR_INVALID_ARG, "out is NULL");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!tried || (!ctx && status != ASETS_ERR_NO_DEVICE)) {
+        tried = true;
+        const char *env = getenv("ASETS_DEVICE");
+        int dev = env ? atoi(env) : 0;
+        status = asets_context_create(dev, &ctx);
+    }
+    *out = ctx;
+    if (!ctx)
+        return status != ASETS_OK ? status : fail(ASETS_ERR_NO_DEVICE, "no default context");
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_context_set_stream(asets_context *ctx, void *stream)
+{
+    if (!ctx)
+        return fail(ASETS_ERR_INVALID_ARG, "ctx is NULL");
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+    return ASETS_OK;
+}
+
+// ---------------------------------------------------------------- solver
+static asets_status dalloc(asets_solver *s, float **p, size_t floats)
+{
+    void *ptr = nullptr;
+    cudaError_t e = cudaMalloc(&ptr, std::max<size_t>(floats, 1) * sizeof(float));
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaMalloc");
+    s->allocations.push_back(ptr);
+    *p = static_cast<float *>(ptr);
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API void asets_solver_destroy(asets_solver *s)
+{
+    if (!s)
+        return;
+    DeviceGuard guard(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    for (void *p : s->allocations)
+        cudaFree(p);
+    if (s->ev0)
+        cudaEventDestroy(s->ev0);
+    if (s->ev1)
+        cudaEventDestroy(s->ev1);
+    for (int i = 0; i < 2; ++i)
+        if (s->flag_ev[i])
+            cudaEventDestroy(s->flag_ev[i]);
+    if (s->ctx->cached == s)
+        s->ctx->cached = nullptr;
+    delete s;
+}
+
+static long long round_pitch(int nr)
+{
+    if (nr >= 32)
+        return ((long long)nr + 31) / 32 * 32;
+    return ((long long)nr + 3) / 4 * 4;
+}
+
+static asets_status encode_map(asets_solver *s, CUtensorMap *map, float *base, int labels,
+                               int box_rows, int box_cols)
+{
+    cuuint64_t dims[4] = {(cuuint64_t)s->nr, (cuuint64_t)s->nc, (cuuint64_t)s->ns,
+                          (cuuint64_t)std::max(labels, 1)};
+    cuuint64_t strides[3] = {(cuuint64_t)(s->pitch * 4), (cuuint64_t)(s->plane * 4),
+                             (cuuint64_t)(s->cells * 4)};
+    cuuint32_t box[4] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols, 1, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = s->ctx->encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box,
+                                estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return fail(ASETS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d) rows=%d cols=%d", (int)r,
+                    box_rows, box_cols);
+    return ASETS_OK;
+}
+
+static const StencilVariant *pick_variant(const asets_solver *s, int exact, int tile_config)
+{
+    int n = 0;
+    const StencilVariant *tab;
+    const bool binary = (s->model == ASETS_BINARY);
+    if (s->dim == 3)
+        tab = binary ? binary3d_variants(&n) : flow3d_variants(&n);
+    else
+        tab = binary ? binary2d_variants(&n) : flow2d_variants(&n);
+    std::vector<const StencilVariant *> match;
+    for (int i = 0; i < n; ++i)
+        if (tab[i].exact == exact)
+            match.push_back(&tab[i]);
+    if (match.empty())
+        return nullptr;
+    if (tile_config > 0 && tile_config <= (int)match.size())
+        return match[tile_config - 1];
+    if (s->dim == 2 && s->nr <= 48) {
+        for (auto *v : match)
+            if (v->tr == 32)
+                return v;
+    }
+    return match[0];
+}
+
+// Build the kernel arguments (TMA maps for both parities, destinations).
+static asets_status setup_kernel(asets_solver *s, int exact, int tile_config)
+{
+    const StencilVariant *v = pick_variant(s, exact, tile_config);
+    if (!v)
+        return fail(ASETS_ERR_UNSUPPORTED, "no kernel variant for this configuration");
+    if (s->variant == v)
+        return ASETS_OK;
+    StencilArgs &A = s->args;
+    memset(&A, 0, sizeof A);
+    const bool binary = (s->model == ASETS_BINARY);
+    for (int par = 0; par < 2; ++par) {
+        float *srcs[NUM_SLOTS];
+        int labels[NUM_SLOTS];
+        srcs[SL_BC] = s->b[par][0];
+        srcs[SL_BR] = s->b[par][1];
+        srcs[SL_BS] = s->b[par][2];
+        for (int k = 0; k < 3; ++k)
+            labels[k] = s->flow_labels;
+        if (binary) {
+            srcs[SL_S0] = s->ps[par]; srcs[SL_S1] = s->pt[par]; srcs[SL_S2] = s->u[par];
+            labels[SL_S0] = labels[SL_S1] = labels[SL_S2] = 1;
+        } else if (s->model == ASETS_POTTS) {
+            srcs[SL_S0] = s->ps[0]; labels[SL_S0] = 1;
+            srcs[SL_S1] = s->pt[0]; labels[SL_S1] = s->nlab;
+            srcs[SL_S2] = s->u[0]; labels[SL_S2] = s->nlab;
+        } else {
+            srcs[SL_S0] = s->pt[0]; labels[SL_S0] = s->nlab;
+            srcs[SL_S1] = s->pt[0]; labels[SL_S1] = s->nlab;
+            srcs[SL_S2] = s->u[0]; labels[SL_S2] = s->nlab - 1;
+        }
+        srcs[SL_ALPHA] = s->alpha;
+        labels[SL_ALPHA] = s->alpha_labels;
+        for (int slot = 0; slot < NUM_SLOTS; ++slot) {
+            if (s->dim == 2 && slot == SL_BC)
+                continue;
+            int cols = (slot == SL_BC) ? v->box_cols_bc : v->box_cols;
+            asets_status st = encode_map(s, &A.map[par][slot], srcs[slot], labels[slot],
+                                         v->box_rows, cols);
+            if (st != ASETS_OK)
+                return st;
+        }
+        for (int k = 0; k < 3; ++k)
+            A.dst_b[par][k] = s->b[par ^ 1][k];
+        if (binary) {
+            A.dst_s[par][0] = s->ps[par ^ 1];
+            A.dst_s[par][1] = s->pt[par ^ 1];
+            A.dst_s[par][2] = s->u[par ^ 1];
+        } else {
+            A.dst_s[par][0] = s->dv;
+        }
+    }
+    for (int slot = 0; slot < NUM_SLOTS; ++slot) {
+        A.lab_mul[slot] = binary ? 0 : 1;
+        A.lab_add[slot] = 0;
+    }
+    if (s->model == ASETS_POTTS)
+        A.lab_mul[SL_S0] = 0;  // one shared source flow
+    if (s->model == ASETS_ISHIKAWA)
+        A.lab_add[SL_S1] = 1;  // pt_{k+1}
+    A.cs = s->cs;
+    A.ct = s->ct;
+    A.ctl = s->ctl;
+    A.pitch = s->pitch;
+    A.plane_stride = s->plane;
+    A.label_stride = s->cells;
+    A.nr = s->nr;
+    A.nc = s->nc;
+    A.ns = s->ns;
+    A.nlab_items = s->flow_labels;
+    A.tiles_r = (s->nr + v->tr - 1) / v->tr;
+    A.tiles_c = (s->dim == 3) ? (s->nc + v->tc - 1) / v->tc : 1;
+    A.total_work = (long long)s->flow_labels * A.tiles_r * A.tiles_c * s->ns;
+
+    CU_TRY(cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                v->smem_bytes));
+    int per_sm = 0;
+    CU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, v->nt, v->smem_bytes));
+    if (per_sm < 1)
+        return fail(ASETS_ERR_UNSUPPORTED, "stencil kernel does not fit on an SM");
+    long long grid = (long long)s->ctx->num_sms * per_sm;
+    // keep at least a few planes per block: the 2-plane lag costs 4 steps
+    const long long min_planes = 4;
+    grid = std::min(grid, (A.total_work + min_planes - 1) / min_planes);
+    s->grid = (int)std::max<long long>(grid, 1);
+    // one erriter partial per block of the stencil or label kernel
+    const int need = std::max({s->grid, s->ctx->num_sms * 8, 1024});
+    if (need > s->partials_cap) {
+        void *p = nullptr;
+        CU_TRY(cudaMalloc(&p, sizeof(double) * need));
+        s->allocations.push_back(p);
+        s->partials = static_cast<double *>(p);
+        s->partials_cap = need;
+    }
+    A.partials = s->partials;
+    s->variant = v;
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_solver_create(asets_context *ctx, asets_model model,
+                                                      int dim, int Ny, int Nx, int Nz, int nLab,
+                                                      asets_solver **out)
+{
+    if (!ctx || !out)
+        return fail(ASETS_ERR_INVALID_ARG, "ctx/out is NULL");
+    *out = nullptr;
+    if (dim != 2 && dim != 3)
+        return fail(ASETS_ERR_INVALID_ARG, "dim must be 2 or 3");
+    if (Ny < 1 || Nx < 1 || Nz < 1 || (dim == 2 && Nz != 1))
+        return fail(ASETS_ERR_INVALID_ARG, "bad grid size %d x %d x %d", Ny, Nx, Nz);
+    if (model == ASETS_BINARY) {
+        nLab = 1;
+    } else if (model == ASETS_POTTS) {
+        if (nLab < 1)
+            return fail(ASETS_ERR_INVALID_ARG, "Potts needs nLab >= 1");
+    } else if (model == ASETS_ISHIKAWA) {
+        if (nLab < 2)
+            return fail(ASETS_ERR_INVALID_ARG, "Ishikawa needs nLab >= 2");
+    } else {
+        return fail(ASETS_ERR_INVALID_ARG, "unknown model %d", (int)model);
+    }
+    if ((long long)Ny * Nx * Nz * nLab > (1LL << 31) - 1)
+        return fail(ASETS_ERR_INVALID_ARG, "problem too large for 32-bit Matlab indexing");
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    DeviceGuard guard(ctx->device);
+    std::unique_ptr<asets_solver> s(new asets_solver);
+    s->ctx = ctx;
+    s->model = model;
+    s->dim = dim;
+    s->ny = Ny;
+    s->nx = Nx;
+    s->nz = Nz;
+    s->nlab = nLab;
+    s->nr = Ny;
+    s->nc = (dim == 3) ? Nx : 1;
+    s->ns = (dim == 3) ? Nz : Nx;
+    s->pitch = round_pitch(Ny);
+    s->plane = s->pitch * s->nc;
+    s->cells = s->plane * s->ns;
+    switch (model) {
+    case ASETS_BINARY:
+        s->flow_labels = s->alpha_labels = s->ct_labels = s->pt_labels = s->u_labels = 1;
+        break;
+    case ASETS_POTTS:
+        s->flow_labels = s->alpha_labels = s->ct_labels = s->pt_labels = s->u_labels = nLab;
+        break;
+    case ASETS_ISHIKAWA:
+        s->flow_labels = s->alpha_labels = s->u_labels = nLab - 1;
+        s->ct_labels = s->pt_labels = nLab;
+        break;
+    }
+    const size_t n = (size_t)s->cells;
+    asets_status st = ASETS_OK;
+#define ALLOC(ptr, cnt)                      \
+    do {                                     \
+        st = dalloc(s.get(), &(ptr), (cnt)); \
+        if (st != ASETS_OK)                  \
+            goto cleanup;                    \
+    } while (0)
+    if (model == ASETS_BINARY)
+        ALLOC(s->cs, n);
+    ALLOC(s->ct, n * s->ct_labels);
+    ALLOC(s->alpha, n * s->alpha_labels);
+    for (int par = 0; par < 2; ++par)
+        for (int k = 0; k < 3; ++k) {
+            if (dim == 2 && k == 0)
+                continue;
+            ALLOC(s->b[par][k], n * s->flow_labels);
+        }
+    if (dim == 2) {
+        // column faces do not exist in 2D; keep a valid pointer for the maps
+        s->b[0][0] = s->b[0][1];
+        s->b[1][0] = s->b[1][1];
+    }
+    if (model == ASETS_BINARY) {
+        for (int par = 0; par < 2; ++par) {
+            ALLOC(s->ps[par], n);
+            ALLOC(s->pt[par], n);
+            ALLOC(s->u[par], n);
+        }
+    } else {
+        if (model == ASETS_POTTS)
+            ALLOC(s->ps[0], n);
+        ALLOC(s->pt[0], n * s->pt_labels);
+        ALLOC(s->u[0], n * s->u_labels);
+        ALLOC(s->dv, n * s->flow_labels);
+        s->ps[1] = s->ps[0];
+        s->pt[1] = s->pt[0];
+        s->u[1] = s->u[0];
+    }
+    {
+        void *p = nullptr;
+        cudaError_t e = cudaMalloc(&p, sizeof(IterControl));
+        if (e != cudaSuccess) {
+            st = cuda_fail(e, "cudaMalloc");
+            goto cleanup;
+        }
+        s->allocations.push_back(p);
+        s->ctl = static_cast<IterControl *>(p);
+    }
+    if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->flag_ev[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->flag_ev[1], cudaEventDisableTiming) != cudaSuccess) {
+        st = fail(ASETS_ERR_CUDA, "cudaEventCreate failed");
+        goto cleanup;
+    }
+#undef ALLOC
+    *out = s.release();
+    return ASETS_OK;
+cleanup:
+    asets_solver_destroy(s.release());
+    return st;
+}
+
+// Copy a Matlab-layout array (rows of nr floats) into / out of the padded
+// layout (rows of pitch floats).
+static cudaError_t copy_in(asets_solver *s, float *dst, const float *src, int labels,
+                           asets_memory where)
+{
+    const size_t rows = (size_t)s->nc * s->ns * labels;
+    return cudaMemcpy2DAsync(dst, s->pitch * sizeof(float), src, s->nr * sizeof(float),
+                             s->nr * sizeof(float), rows,
+                             where == ASETS_DEVICE ? cudaMemcpyDeviceToDevice
+                                                   : cudaMemcpyHostToDevice,
+                             s->ctx->stream);
+}
+
+static cudaError_t copy_out(asets_solver *s, float *dst, const float *src, int labels,
+                            asets_memory where)
+{
+    const size_t rows = (size_t)s->nc * s->ns * labels;
+    return cudaMemcpy2DAsync(dst, s->nr * sizeof(float), src, s->pitch * sizeof(float),
+                             s->nr * sizeof(float), rows,
+                             where == ASETS_DEVICE ? cudaMemcpyDeviceToDevice
+                                                   : cudaMemcpyDeviceToHost,
+                             s->ctx->stream);
+}
+
+static InitArgs init_args(asets_solver *s)
+{
+    InitArgs a;
+    memset(&a, 0, sizeof a);
+    a.cs = s->cs;
+    a.ct = s->ct;
+    a.alpha = s->alpha;
+    a.u = s->u[0];
+    a.ps = s->ps[0];
+    a.pt = s->pt[0];
+    a.ctl = s->ctl;
+    a.cells = s->cells;
+    a.label_stride = s->cells;
+    a.pitch = (int)s->pitch;
+    a.nr = s->nr;
+    a.nlab = s->nlab;
+    a.alpha_labels = s->alpha_labels;
+    return a;
+}
+
+extern "C" ASETS_API asets_status asets_solver_set_inputs(asets_solver *s, asets_memory where,
+                                                          const float *Cs, const float *Ct,
+                                                          const float *alpha)
+{
+    if (!s)
+        return fail(ASETS_ERR_INVALID_ARG, "solver is NULL");
+    if (!Ct || !alpha || (s->model == ASETS_BINARY && !Cs))
+        return fail(ASETS_ERR_INVALID_ARG, "missing input array");
+    std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
+    DeviceGuard guard(s->ctx->device);
+    if (s->model == ASETS_BINARY)
+        CU_TRY(copy_in(s, s->cs, Cs, 1, where));
+    CU_TRY(copy_in(s, s->ct, Ct, s->ct_labels, where));
+    CU_TRY(copy_in(s, s->alpha, alpha, s->alpha_labels, where));
+    // alpha(x) > 0 is checked once per input set; run() reports it when it
+    // iterates, as projStep does on the first iteration.
+    IterControl zero;
+    memset(&zero, 0, sizeof zero);
+    CU_TRY(cudaMemcpyAsync(s->ctl, &zero, sizeof zero, cudaMemcpyHostToDevice, s->ctx->stream));
+    InitArgs a = init_args(s);
+    CU_TRY(launch_validate_alpha(a, s->ctx->num_sms, s->ctx->stream));
+    int bad = 0;
+    CU_TRY(cudaMemcpyAsync(&bad, &s->ctl->alpha_bad, sizeof(int), cudaMemcpyDeviceToHost,
+                           s->ctx->stream));
+    CU_TRY(cudaStreamSynchronize(s->ctx->stream));
+    s->alpha_ok = (bad == 0);
+    s->inputs_set = true;
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_solver_set_initial(asets_solver *s, asets_memory where,
+                                                           const float *u0, const float *ps0,
+                                                           const float *pt0)
+{
+    if (!s)
+        return fail(ASETS_ERR_INVALID_ARG, "solver is NULL");
+    std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
+    DeviceGuard guard(s->ctx->device);
+    if (!u0 && !ps0 && !pt0) {
+        s->warm = false;
+        return ASETS_OK;
+    }
+    const bool need_ps = (s->model != ASETS_ISHIKAWA);
+    if (!u0 || !pt0 || (need_ps && !ps0))
+        return fail(ASETS_ERR_INVALID_ARG, "warm start needs u0, pt0%s", need_ps ? " and ps0" : "");
+    const size_t n = (size_t)s->cells;
+    asets_status st;
+    if (!s->warm_u) {
+        if ((st = dalloc(s, &s->warm_u, n * s->u_labels)) != ASETS_OK)
+            return st;
+        if ((st = dalloc(s, &s->warm_pt, n * s->pt_labels)) != ASETS_OK)
+            return st;
+        if (need_ps && (st = dalloc(s, &s->warm_ps, n)) != ASETS_OK)
+            return st;
+    }
+    CU_TRY(copy_in(s, s->warm_u, u0, s->u_labels, where));
+    CU_TRY(copy_in(s, s->warm_pt, pt0, s->pt_labels, where));
+    if (need_ps)
+        CU_TRY(copy_in(s, s->warm_ps, ps0, 1, where));
+    s->warm = true;
+    return ASETS_OK;
+}
+
+static cudaError_t launch_stencil(asets_solver *s)
+{
+    const StencilVariant *v = s->variant;
+    void *params[] = {&s->args};
+    return cudaLaunchKernel(v->fn, dim3(s->grid), dim3(v->nt), params, v->smem_bytes,
+                            s->ctx->stream);
+}
+
+static LabelArgs label_args(asets_solver *s)
+{
+    LabelArgs a;
+    memset(&a, 0, sizeof a);
+    a.u = s->u[0];
+    a.pt = s->pt[0];
+    a.ps = s->ps[0];
+    a.dv = s->dv;
+    a.ct = s->ct;
+    a.ctl = s->ctl;
+    a.partials = s->partials;
+    a.cvg = s->cvg;
+    a.cells = s->cells;
+    a.label_stride = s->cells;
+    a.pitch = (int)s->pitch;
+    a.nr = s->nr;
+    a.nlab = s->nlab;
+    a.cc = s->args.cc;
+    a.inv_cc = s->args.inv_cc;
+    // `1/(cc*nLab)` of updatePSU: cc*nLab rounded to float, then divided
+    a.inv_cc_l = 1.0f / (s->args.cc * (float)s->nlab);
+    return a;
+}
+
+extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_options *opt,
+                                                   int maxIt, float errBound, float cc,
+                                                   float steps, int *itNum)
+{
+    if (!s)
+        return fail(ASETS_ERR_INVALID_ARG, "solver is NULL");
+    if (maxIt < 0)
+        return fail(ASETS_ERR_INVALID_ARG, "maxIt must be >= 0");
+    if (!s->inputs_set)
+        return fail(ASETS_ERR_INVALID_ARG, "inputs not set");
+    const int flags = opt ? opt->flags : 0;
+    const int exact = (flags & ASETS_FLAG_EXACT) ? 1 : 0;
+    std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
+    DeviceGuard guard(s->ctx->device);
+    cudaStream_t st = s->ctx->stream;
+    if (maxIt >= 1 && !s->alpha_ok && !(flags & ASETS_FLAG_NO_ALPHA_CHECK))
+        return fail(ASETS_ERR_ALPHA, "%s", s->alpha_labels > 1 && s->model != ASETS_BINARY
+                                               ? "alpha(x,l) must be positive. Exiting..."
+                                               : "alpha(x) must be positive. Exiting...");
+    asets_status ss = setup_kernel(s, exact, opt ? opt->tile_config : 0);
+    if (ss != ASETS_OK)
+        return ss;
+    if (maxIt > s->cvg_cap) {
+        float *p = nullptr;
+        ss = dalloc(s, &p, (size_t)maxIt);
+        if (ss != ASETS_OK)
+            return ss;
+        s->cvg = p;
+        s->cvg_cap = maxIt;
+    }
+    StencilArgs &A = s->args;
+    A.cvg = s->cvg;
+    A.cc = cc;
+    A.inv_cc = 1.0f / cc;  // `1/cc` of the reference, a float division
+    A.steps = steps;
+
+    // control block
+    IterControl c;
+    memset(&c, 0, sizeof c);
+    c.iter = 0;
+    c.done = (maxIt == 0) ? 1 : 0;
+    c.it_num = 0;
+    c.last_iter = -1;
+    c.max_it = maxIt;
+    c.err_bound = errBound;
+    c.break_lt = (s->model == ASETS_ISHIKAWA && s->dim == 2) ? 1 : 0;
+    {
+        long long denom = (long long)s->ny * s->nx * s->nz * s->u_labels;
+        c.denom = (float)(int)denom;  // (float)(Nx*Ny*Nz[*L]) in int arithmetic
+    }
+    CU_TRY(cudaMemcpyAsync(s->ctl, &c, sizeof c, cudaMemcpyHostToDevice, st));
+    if (maxIt > 0)
+        CU_TRY(cudaMemsetAsync(s->cvg, 0, sizeof(float) * maxIt, st));
+
+    // initial state: flows zero, (u, ps, pt) from init or the warm start
+    const size_t n = (size_t)s->cells;
+    for (int k = 0; k < 3; ++k) {
+        if (s->dim == 2 && k == 0)
+            continue;
+        CU_TRY(cudaMemsetAsync(s->b[0][k], 0, n * s->flow_labels * sizeof(float), st));
+    }
+    if (s->warm) {
+        CU_TRY(cudaMemcpyAsync(s->u[0], s->warm_u, n * s->u_labels * sizeof(float),
+                               cudaMemcpyDeviceToDevice, st));
+        CU_TRY(cudaMemcpyAsync(s->pt[0], s->warm_pt, n * s->pt_labels * sizeof(float),
+                               cudaMemcpyDeviceToDevice, st));
+        if (s->warm_ps)
+            CU_TRY(cudaMemcpyAsync(s->ps[0], s->warm_ps, n * sizeof(float),
+                                   cudaMemcpyDeviceToDevice, st));
+    } else {
+        InitArgs ia = init_args(s);
+        CU_TRY(launch_init((int)s->model, ia, s->ctx->num_sms, st));
+    }
+
+    // iterate: the kernels stop by themselves once `done` is set; the host
+    // stops launching when a chunk it has already checked reports done.
+    const bool binary = (s->model == ASETS_BINARY);
+    LabelArgs la;
+    int label_grid = 0;
+    if (!binary) {
+        la = label_args(s);
+        label_grid = label_kernel_grid(s->cells, s->ctx->num_sms);
+    }
+    CU_TRY(cudaEventRecord(s->ev0, st));
+    // Chunks of kChunk iterations; at most two chunks are queued.  Before
+    // queueing chunk c the host waits for chunk c-2's done flag, so a
+    // converged solve stops launching within two chunks.
+    const int kChunk = 16;
+    int launched = 0, launches = 0, chunk = 0;
+    int *flags_h = s->ctx->pinned_flags;
+    while (launched < maxIt) {
+        if (chunk >= 2) {
+            CU_TRY(cudaEventSynchronize(s->flag_ev[chunk % 2]));
+            if (flags_h[chunk % 2])
+                break;
+        }
+        const int nit = std::min(kChunk, maxIt - launched);
+        for (int i = 0; i < nit; ++i) {
+            CU_TRY(launch_stencil(s));
+            ++launches;
+            if (!binary) {
+                CU_TRY(s->model == ASETS_POTTS ? launch_potts_labels(la, label_grid, st)
+                                               : launch_ishikawa_labels(la, label_grid, st));
+                ++launches;
+            }
+        }
+        launched += nit;
+        CU_TRY(cudaMemcpyAsync(&flags_h[chunk % 2], &s->ctl->done, sizeof(int),
+                               cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaEventRecord(s->flag_ev[chunk % 2], st));
+        ++chunk;
+    }
+    CU_TRY(cudaEventRecord(s->ev1, st));
+    IterControl out;
+    CU_TRY(cudaMemcpyAsync(&out, s->ctl, sizeof out, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    CU_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    s->last_ms = ms;
+    s->last_launches = launches;
+    s->last_max_it = maxIt;
+    if (out.error & DEV_ERR_TIMEOUT)
+        return fail(ASETS_ERR_TIMEOUT, "a device-side wait for a TMA load timed out");
+    if (maxIt > 0 && !out.done)
+        return fail(ASETS_ERR_CUDA, "iteration loop ended without completion (iter=%d)", out.iter);
+    s->final_parity = binary ? ((out.last_iter + 1) & 1) : 0;
+    if (itNum)
+        *itNum = (maxIt == 0) ? 0 : out.it_num;
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_solver_get_u(asets_solver *s, asets_memory where, float *u)
+{
+    if (!s || !u)
+        return fail(ASETS_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
+    DeviceGuard guard(s->ctx->device);
+    CU_TRY(copy_out(s, u, s->u[s->final_parity], s->u_labels, where));
+    CU_TRY(cudaStreamSynchronize(s->ctx->stream));
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_solver_get_cvg(asets_solver *s, asets_memory where,
+                                                       float *cvg, int n)
+{
+    if (!s || (!cvg && n > 0))
+        return fail(ASETS_ERR_INVALID_ARG, "NULL argument");
+    if (n < 0 || n > s->last_max_it)
+        return fail(ASETS_ERR_INVALID_ARG, "n=%d exceeds maxIt of the last run (%d)", n,
+                    s->last_max_it);
+    if (n == 0)
+        return ASETS_OK;
+    std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
+    DeviceGuard guard(s->ctx->device);
+    CU_TRY(cudaMemcpyAsync(cvg, s->cvg, sizeof(float) * n,
+                           where == ASETS_DEVICE ? cudaMemcpyDeviceToDevice
+                                                 : cudaMemcpyDeviceToHost,
+                           s->ctx->stream));
+    CU_TRY(cudaStreamSynchronize(s->ctx->stream));
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_solver_get_flows(asets_solver *s, asets_memory where,
+                                                         float *ps, float *pt)
+{
+    if (!s)
+        return fail(ASETS_ERR_INVALID_ARG, "NULL solver");
+    std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
+    DeviceGuard guard(s->ctx->device);
+    if (ps) {
+        if (s->model == ASETS_ISHIKAWA)
+            return fail(ASETS_ERR_INVALID_ARG, "the Ishikawa model has no source flow");
+        CU_TRY(copy_out(s, ps, s->ps[s->final_parity], 1, where));
+    }
+    if (pt)
+        CU_TRY(copy_out(s, pt, s->pt[s->final_parity], s->pt_labels, where));
+    CU_TRY(cudaStreamSynchronize(s->ctx->stream));
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_solver_last_run_stats(asets_solver *s, float *ms,
+                                                              int *kernel_launches)
+{
+    if (!s)
+        return fail(ASETS_ERR_INVALID_ARG, "NULL solver");
+    if (ms)
+        *ms = s->last_ms;
+    if (kernel_launches)
+        *kernel_launches = s->last_launches;
+    return ASETS_OK;
+}
+
+// ---------------------------------------------------------------- one-shot
+static asets_status one_shot(asets_context *ctx, const asets_options *opt, asets_model model,
+                             int dim, int Ny, int Nx, int Nz, int nLab, const float *alpha,
+                             const float *Cs, const float *Ct, int maxIt, float errBound, float cc,
+                             float steps, float *u, float *cvg, int *itNum, float *seconds)
+{
+    const auto t0 = std::chrono::steady_clock::now();
+    if (!ctx) {
+        asets_status st = asets_default_context(&ctx);
+        if (st != ASETS_OK)
+            return st;
+    }
+    if (!alpha || !Ct || !u || (maxIt > 0 && !cvg) || (model == ASETS_BINARY && !Cs))
+        return fail(ASETS_ERR_INVALID_ARG, "NULL input or output pointer");
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    asets_solver *s = ctx->cached;
+    if (!s || s->model != model || s->dim != dim || s->ny != Ny || s->nx != Nx || s->nz != Nz ||
+        s->nlab != (model == ASETS_BINARY ? 1 : nLab)) {
+        if (s)
+            asets_solver_destroy(s);
+        ctx->cached = nullptr;
+        asets_status st = asets_solver_create(ctx, model, dim, Ny, Nx, Nz, nLab, &s);
+        if (st != ASETS_OK)
+            return st;
+        ctx->cached = s;
+    }
+    s->warm = false;
+    asets_status st = asets_solver_set_inputs(s, ASETS_HOST, Cs, Ct, alpha);
+    if (st != ASETS_OK)
+        return st;
+    int it = 0;
+    st = asets_solver_run(s, opt, maxIt, errBound, cc, steps, &it);
+    if (st != ASETS_OK)
+        return st;
+    st = asets_solver_get_u(s, ASETS_HOST, u);
+    if (st != ASETS_OK)
+        return st;
+    st = asets_solver_get_cvg(s, ASETS_HOST, cvg, maxIt);
+    if (st != ASETS_OK)
+        return st;
+    if (itNum)
+        *itNum = it;
+    if (seconds)
+        *seconds = std::chrono::duration<float>(std::chrono::steady_clock::now() - t0).count();
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_binary_mf2d(asets_context *ctx, const asets_options *opt,
+                                                    const float *alpha, const float *Cs,
+                                                    const float *Ct, int Nx, int Ny, int maxIt,
+                                                    float errBound, float cc, float steps,
+                                                    float *u, float *cvg, int *itNum,
+                                                    float *seconds)
+{
+    return one_shot(ctx, opt, ASETS_BINARY, 2, Ny, Nx, 1, 1, alpha, Cs, Ct, maxIt, errBound, cc,
+                    steps, u, cvg, itNum, seconds);
+}
+
+extern "C" ASETS_API asets_status asets_binary_mf3d(asets_context *ctx, const asets_options *opt,
+                                                    const float *alpha, const float *Cs,
+                                                    const float *Ct, int Nx, int Ny, int Nz,
+                                                    int maxIt, float errBound, float cc,
+                                                    float steps, float *u, float *cvg,
+                                                    int *itNum, float *seconds)
+{
+    return one_shot(ctx, opt, ASETS_BINARY, 3, Ny, Nx, Nz, 1, alpha, Cs, Ct, maxIt, errBound, cc,
+                    steps, u, cvg, itNum, seconds);
+}
+
+extern "C" ASETS_API asets_status asets_potts2d(asets_context *ctx, const asets_options *opt,
+                                                const float *alpha, const float *Ct, int Nx,
+                                                int Ny, int nLab, int maxIt, float errBound,
+                                                float cc, float steps, float *u, float *cvg,
+                                                int *itNum, float *seconds)
+{
+    return one_shot(ctx, opt, ASETS_POTTS, 2, Ny, Nx, 1, nLab, alpha, nullptr, Ct, maxIt,
+                    errBound, cc, steps, u, cvg, itNum, seconds);
+}
+
+extern "C" ASETS_API asets_status asets_potts3d(asets_context *ctx, const asets_options *opt,
+                                                const float *alpha, const float *Ct, int Nx,
+                                                int Ny, int Nz, int nLab, int maxIt,
+                                                float errBound, float cc, float steps, float *u,
+                                                float *cvg, int *itNum, float *seconds)
+{
+    return one_shot(ctx, opt, ASETS_POTTS, 3, Ny, Nx, Nz, nLab, alpha, nullptr, Ct, maxIt,
+                    errBound, cc, steps, u, cvg, itNum, seconds);
+}
+
+extern "C" ASETS_API asets_status asets_ishikawa2d(asets_context *ctx, const asets_options *opt,
+                                                   const float *alpha, const float *Ct, int Nx,
+                                                   int Ny, int nLab, int maxIt, float errBound,
+                                                   float cc, float steps, float *u, float *cvg,
+                                                   int *itNum, float *seconds)
+{
+    return one_shot(ctx, opt, ASETS_ISHIKAWA, 2, Ny, Nx, 1, nLab, alpha, nullptr, Ct, maxIt,
+                    errBound, cc, steps, u, cvg, itNum, seconds);
+}
+
+extern "C" ASETS_API asets_status asets_ishikawa3d(asets_context *ctx, const asets_options *opt,
+                                                   const float *alpha, const float *Ct, int Nx,
+                                                   int Ny, int Nz, int nLab, int maxIt,
+                                                   float errBound, float cc, float steps,
+                                                   float *u, float *cvg, int *itNum,
+                                                   float *seconds)
+{
+    return one_shot(ctx, opt, ASETS_ISHIKAWA, 3, Ny, Nx, Nz, nLab, alpha, nullptr, Ct, maxIt,
+                    errBound, cc, steps, u, cvg, itNum, seconds);
+}

@@ -1,0 +1,267 @@
+"""ctypes binding of libasetscuda (include/asets.h).
+
+The library must have been built in-tree (asetsmatlabmaxflow_gb300.build);
+there is no fallback: every solve runs the CUDA kernels or raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+ASETS_OK = 0
+ASETS_ERR_INVALID_ARG = 1
+ASETS_ERR_ALPHA = 2
+ASETS_ERR_CUDA = 3
+ASETS_ERR_OUT_OF_MEMORY = 4
+ASETS_ERR_TIMEOUT = 5
+ASETS_ERR_NO_DEVICE = 6
+ASETS_ERR_UNSUPPORTED = 7
+
+BINARY, POTTS, ISHIKAWA = 0, 1, 2
+MODELS = {"binary": BINARY, "potts": POTTS, "ishikawa": ISHIKAWA}
+HOST, DEVICE = 0, 1
+FLAG_EXACT = 0x1
+FLAG_NO_ALPHA_CHECK = 0x2
+
+_FP = ctypes.POINTER(ctypes.c_float)
+_VP = ctypes.c_void_p
+
+
+class AsetsError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[{status}] {message}")
+        self.status = status
+        self.message = message
+
+
+class AlphaError(AsetsError):
+    """alpha(x) <= 0, the reference's mexErrMsgTxt case."""
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("flags", ctypes.c_int), ("tile_config", ctypes.c_int),
+                ("reserved", ctypes.c_int * 6)]
+
+
+_lib = None
+
+LIB_PATH = _build.LIB / "libasetscuda.so"
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "asets_abi_version": (ctypes.c_int, []),
+    "asets_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "asets_last_error": (ctypes.c_char_p, []),
+    "asets_context_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_VP)]),
+    "asets_context_destroy": (None, [_VP]),
+    "asets_default_context": (ctypes.c_int, [ctypes.POINTER(_VP)]),
+    "asets_context_set_stream": (ctypes.c_int, [_VP, _VP]),
+    "asets_binary_mf2d": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                         ctypes.c_float, _VP, _VP, _VP, _VP]),
+    "asets_binary_mf3d": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                         ctypes.c_float, ctypes.c_float, _VP, _VP, _VP, _VP]),
+    "asets_potts2d": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                     ctypes.c_float, _VP, _VP, _VP, _VP]),
+    "asets_potts3d": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                     ctypes.c_float, ctypes.c_float, _VP, _VP, _VP, _VP]),
+    "asets_ishikawa2d": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                        ctypes.c_float, ctypes.c_float, _VP, _VP, _VP, _VP]),
+    "asets_ishikawa3d": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                        ctypes.c_float, ctypes.c_float, _VP, _VP, _VP, _VP]),
+    "asets_solver_create": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(_VP)]),
+    "asets_solver_destroy": (None, [_VP]),
+    "asets_solver_set_inputs": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
+    "asets_solver_set_initial": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
+    "asets_solver_run": (ctypes.c_int, [_VP, _VP, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                        ctypes.c_float, ctypes.POINTER(ctypes.c_int)]),
+    "asets_solver_get_u": (ctypes.c_int, [_VP, ctypes.c_int, _VP]),
+    "asets_solver_get_cvg": (ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.c_int]),
+    "asets_solver_get_flows": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP]),
+    "asets_solver_last_run_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_float),
+                                                   ctypes.POINTER(ctypes.c_int)]),
+}
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+def lib() -> ctypes.CDLL:
+    """Load libasetscuda.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} not found: build it with "
+                               "`python -m asetsmatlabmaxflow_gb300.build` (needs nvcc)")
+        l = ctypes.CDLL(str(LIB_PATH), mode=os.RTLD_GLOBAL | os.RTLD_NOW)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def check(status: int) -> None:
+    if status == ASETS_OK:
+        return
+    msg = lib().asets_last_error().decode(errors="replace")
+    if status == ASETS_ERR_ALPHA:
+        raise AlphaError(status, msg)
+    raise AsetsError(status, msg or lib().asets_status_string(status).decode())
+
+
+def _ptr(a) -> int | None:
+    """Address of a numpy array, a torch tensor, or anything exposing
+    __cuda_array_interface__ / an integer address."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    if hasattr(a, "__cuda_array_interface__"):
+        return a.__cuda_array_interface__["data"][0]
+    raise TypeError(f"cannot take the address of {type(a)}")
+
+
+def _host_f32(a) -> np.ndarray | None:
+    if a is None:
+        return None
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float32).ravel(order="F"))
+
+
+class Context:
+    def __init__(self, device: int = 0, handle: int | None = None):
+        if handle is not None:
+            self._h = handle
+            self._own = False
+        else:
+            h = _VP()
+            check(lib().asets_context_create(device, ctypes.byref(h)))
+            self._h = h.value
+            self._own = True
+
+    @staticmethod
+    def default() -> "Context":
+        h = _VP()
+        check(lib().asets_default_context(ctypes.byref(h)))
+        return Context(handle=h.value)
+
+    @property
+    def handle(self) -> int:
+        return self._h
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        check(lib().asets_context_set_stream(self._h, stream_ptr))
+
+    def close(self) -> None:
+        if self._own and self._h:
+            lib().asets_context_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Solver:
+    """A device-resident problem (asets_solver_*)."""
+
+    def __init__(self, ctx: Context, model: str, dims: tuple[int, ...], nlab: int = 1):
+        self.ctx = ctx
+        self.model = model
+        self.dim = len(dims)
+        self.ny, self.nx = dims[0], dims[1]
+        self.nz = dims[2] if self.dim == 3 else 1
+        self.nlab = nlab if model != "binary" else 1
+        h = _VP()
+        check(lib().asets_solver_create(ctx.handle, MODELS[model], self.dim, self.ny, self.nx,
+                                        self.nz, self.nlab, ctypes.byref(h)))
+        self._h = h.value
+        self._keep = []
+        self.last_max_it = 0
+
+    @property
+    def n(self) -> int:
+        return self.ny * self.nx * self.nz
+
+    @property
+    def u_labels(self) -> int:
+        return {"binary": 1, "potts": self.nlab, "ishikawa": self.nlab - 1}[self.model]
+
+    @property
+    def pt_labels(self) -> int:
+        return 1 if self.model == "binary" else self.nlab
+
+    def set_inputs(self, Ct, alpha, Cs=None, where: int = HOST) -> None:
+        if where == HOST:
+            Ct, alpha, Cs = _host_f32(Ct), _host_f32(alpha), _host_f32(Cs)
+            self._keep = [Ct, alpha, Cs]
+        check(lib().asets_solver_set_inputs(self._h, where, _ptr(Cs), _ptr(Ct), _ptr(alpha)))
+
+    def set_initial(self, u0=None, ps0=None, pt0=None, where: int = HOST) -> None:
+        if where == HOST:
+            u0, ps0, pt0 = _host_f32(u0), _host_f32(ps0), _host_f32(pt0)
+        check(lib().asets_solver_set_initial(self._h, where, _ptr(u0), _ptr(ps0), _ptr(pt0)))
+
+    def run(self, max_it: int, err_bound: float, cc: float, steps: float, *, exact: bool = False,
+            tile_config: int = 0, flags: int = 0) -> int:
+        opt = Options(flags=flags | (FLAG_EXACT if exact else 0), tile_config=tile_config)
+        it = ctypes.c_int(0)
+        check(lib().asets_solver_run(self._h, ctypes.byref(opt), max_it, err_bound, cc, steps,
+                                     ctypes.byref(it)))
+        self.last_max_it = max_it
+        return it.value
+
+    def get_u(self, out=None, where: int = HOST) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.n * self.u_labels, np.float32)
+        check(lib().asets_solver_get_u(self._h, where, _ptr(out)))
+        return out
+
+    def get_cvg(self, n: int | None = None) -> np.ndarray:
+        n = self.last_max_it if n is None else n
+        out = np.empty(max(n, 0), np.float32)
+        check(lib().asets_solver_get_cvg(self._h, HOST, _ptr(out) if n else None, n))
+        return out
+
+    def get_flows(self) -> tuple[np.ndarray | None, np.ndarray]:
+        ps = None if self.model == "ishikawa" else np.empty(self.n, np.float32)
+        pt = np.empty(self.n * self.pt_labels, np.float32)
+        check(lib().asets_solver_get_flows(self._h, HOST, _ptr(ps), _ptr(pt)))
+        return ps, pt
+
+    def last_run_stats(self) -> tuple[float, int]:
+        ms = ctypes.c_float(0)
+        n = ctypes.c_int(0)
+        check(lib().asets_solver_last_run_stats(self._h, ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
+    def close(self) -> None:
+        if self._h:
+            lib().asets_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

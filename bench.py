@@ -1,0 +1,332 @@
+"""Benchmark: binary continuous max-flow 3D, 256^3 float32, 200 fixed ALM
+iterations per step (the throughput run of the binary 3D workload).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+One JSON line on rank 0.  `value` is whole-job Gvoxel-iter/s with inputs
+resident in HBM; `e2e` the same through the C ABI one-shot call
+(asets_binary_mf3d) from pinned host buffers, host<->device copies included.
+`roofline` relates the fused iteration kernel's algorithmic bytes (60 B per
+voxel-iteration: 6 state arrays read+written, 3 inputs read) to the measured
+HBM copy bandwidth.  `--impl reference` times the CPU restatement of the
+reference C solver (bit-identical to it) on all host cores, one independent
+solve per core.  Under torchrun each rank solves its own volume (weak
+scaling, replicas only: the path has no exchange between problems).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gvoxel-iter/s (binary 3D 256^3); time-to-errBound, learned warm vs cold start"
+UNIT = "Gvoxel-iter/s"
+SHAPE = (256, 256, 256)
+ITERS = 200
+CC, STEPS = 0.35, 0.11
+BYTES_PER_VOXEL_ITER = 60  # 6 state arrays x (read + write) x 4 B + 3 inputs x 4 B
+WORKLOAD = "binary3d_256^3_200it"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def max_over_ranks(pg, x: float) -> float:
+    if pg is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch():
+    """DRAM bytes of one fused iteration launch on this workload, from the
+    committed ncu summary (profiles/), or None."""
+    p = ROOT / "profiles" / "binary3d_256_traffic.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["dram_bytes_per_launch"])
+        except (KeyError, ValueError):
+            return None
+    return None
+
+
+def cpu_baseline_sample(cs, ct, alpha, iters: int) -> dict:
+    """Single-core oracle solve of the same volume for `iters` iterations
+    (init included, as the reference's timet)."""
+    from oracle import oracle as O
+
+    t0 = time.perf_counter()
+    O.solve("binary", SHAPE, ct, alpha, cs=cs, max_it=iters, err_bound=0.0, cc=CC, steps=STEPS)
+    dt = time.perf_counter() - t0
+    return {"value": float(np.prod(SHAPE)) * iters / dt / 1e9, "unit": UNIT, "cores": 1,
+            "kind": "port", "seconds": dt,
+            "sample": f"256^3 binary 3D, {iters} iterations incl. init, 1 thread "
+                      "(C restatement, bit-identical to maxflow/asetsBinaryMF3D_mex.c)"}
+
+
+def run_reference(args, rank, pg):
+    """CPU arm: the reference C path on all host cores, one solve per core."""
+    if rank != 0:
+        return
+    from concurrent.futures import ThreadPoolExecutor
+
+    from asetsmatlabmaxflow_gb300 import synth
+    from oracle import oracle as O
+
+    cs, ct, alpha = synth.binary3d(seed=0, shape=SHAPE)
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    iters = 2  # per core per step: a bounded sample of the 200-iteration run
+
+    def one(_):
+        O.solve("binary", SHAPE, ct, alpha, cs=cs, max_it=iters, err_bound=0.0, cc=CC, steps=STEPS)
+
+    O.lib()
+    with ThreadPoolExecutor(max_workers=cores) as ex:
+        for _ in range(args.warmup):
+            list(ex.map(one, range(cores)))
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            list(ex.map(one, range(cores)))
+        dt = time.perf_counter() - t0
+    value = float(np.prod(SHAPE)) * iters * cores * args.steps / dt / 1e9
+    sample = (f"256^3 binary 3D, {iters} iterations incl. init per core per step, "
+              f"{cores} concurrent single-thread solves")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "shape": list(SHAPE), "cc": CC, "steps": STEPS},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local, pg = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank, pg)
+        return
+    import torch
+
+    from asetsmatlabmaxflow_gb300 import native as N
+    from asetsmatlabmaxflow_gb300 import synth
+
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    ctx = N.Context(local)
+    ctx.set_stream(stream.cuda_stream)
+    cs, ct, alpha = synth.binary3d(seed=rank, shape=SHAPE)
+    nvox = int(np.prod(SHAPE))
+
+    # ---- value: device-resident inputs, one step = one 200-iteration solve
+    s = N.Solver(ctx, "binary", SHAPE)
+    s.set_inputs(ct, alpha, cs)
+    for _ in range(args.warmup):
+        s.run(ITERS, 0.0, CC, STEPS)
+    kernel_ms = []
+    launches = 0
+    barrier(pg)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            it = s.run(ITERS, 0.0, CC, STEPS)
+            ms, nl = s.last_run_stats()
+            kernel_ms.append(ms / nl)
+            launches += nl + 1  # iteration launches + the init kernel
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier(pg)
+    t_ms = max_over_ranks(pg, ev0.elapsed_time(ev1))
+    value = world * nvox * ITERS * args.steps / (t_ms * 1e-3) / 1e9
+
+    # ---- roofline of the fused iteration kernel
+    peak, peak_kind = peaks()
+    per_launch_ms = statistics.median(kernel_ms)
+    achieved = BYTES_PER_VOXEL_ITER * nvox / (per_launch_ms * 1e-3) / 1e9
+    traffic = traffic_per_launch()
+
+    # ---- time to errBound 1e-4 (convergence run)
+    s.run(2000, 1e-4, CC, STEPS)
+    conv_ms, conv_launches = s.last_run_stats()
+    conv_it = s.run(2000, 1e-4, CC, STEPS)
+    conv_ms, _ = s.last_run_stats()
+    s.close()
+
+    # ---- e2e: the C ABI one-shot call from pinned host buffers
+    h_cs = torch.from_numpy(cs.ravel(order="F").copy()).pin_memory()
+    h_ct = torch.from_numpy(ct.ravel(order="F").copy()).pin_memory()
+    h_al = torch.from_numpy(alpha.ravel(order="F").copy()).pin_memory()
+    h_u = torch.empty(nvox, dtype=torch.float32).pin_memory()
+    h_cvg = torch.empty(ITERS, dtype=torch.float32).pin_memory()
+    lib = N.lib()
+    import ctypes
+
+    itn = ctypes.c_int(0)
+
+    def e2e_call():
+        st = lib.asets_binary_mf3d(ctx.handle, None, h_al.data_ptr(), h_cs.data_ptr(),
+                                   h_ct.data_ptr(), SHAPE[1], SHAPE[0], SHAPE[2], ITERS, 0.0, CC,
+                                   STEPS, h_u.data_ptr(), h_cvg.data_ptr(), ctypes.byref(itn), None)
+        N.check(st)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_call()
+    barrier(pg)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_call()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
+    e2e_value = world * nvox * ITERS * args.steps / e2e_s / 1e9
+    ok = bool(np.isfinite(h_u.numpy()).all())
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample(cs, ct, alpha, 8)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "model": "binary continuous max-flow 3D",
+                       "shape": list(SHAPE), "iterations_per_step": ITERS, "cc": CC,
+                       "steps": STEPS, "err_bound": 0.0, "parallelism": f"replicas{world}",
+                       "l2": "working set ~1 GB per iteration, larger than L2; no flush",
+                       "voronoi_cells": 40, "intensities": [0.25, 0.75], "noise": 0.2},
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": 3 * nvox * 4, "d2h_bytes_per_step": nvox * 4 + ITERS * 4},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_kind": peak_kind, "kernel": "stencil_iteration_kernel<3,32,16>",
+                         "bytes_per_voxel_iter": BYTES_PER_VOXEL_ITER,
+                         "launch_ms": per_launch_ms},
+            "time_to_errbound": {"err_bound": 1e-4, "iterations": conv_it, "ms": conv_ms},
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+            "finite": ok,
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,176 @@
+/*
+ * libasetscuda -- GB300 (sm_103a) continuous max-flow solvers.
+ *
+ * C ABI: plain pointers and sizes, no CUDA or torch types.  Arrays are
+ * float32 in Matlab column-major order (index g = z*Nx*Ny + x*Ny + y, the
+ * label index slowest), exactly as the reference mex files receive them
+ * through mxGetData.
+ *
+ * Every function returns an asets_status.  On failure nothing is written to
+ * the outputs; asets_last_error() gives a message for the calling thread.
+ */
+#ifndef ASETS_H
+#define ASETS_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ASETS_ABI_VERSION 1
+
+#if defined(_WIN32)
+#define ASETS_API __declspec(dllexport)
+#else
+#define ASETS_API __attribute__((visibility("default")))
+#endif
+
+typedef enum asets_status {
+    ASETS_OK = 0,
+    ASETS_ERR_INVALID_ARG = 1,  /* bad sizes/pars/pointers */
+    ASETS_ERR_ALPHA = 2,        /* "alpha(x) must be positive. Exiting..." */
+    ASETS_ERR_CUDA = 3,         /* a CUDA runtime call failed */
+    ASETS_ERR_OUT_OF_MEMORY = 4,
+    ASETS_ERR_TIMEOUT = 5,      /* a bounded device-side wait ran out */
+    ASETS_ERR_NO_DEVICE = 6,    /* no usable sm_103 GPU */
+    ASETS_ERR_UNSUPPORTED = 7
+} asets_status;
+
+typedef enum asets_model {
+    ASETS_BINARY = 0,
+    ASETS_POTTS = 1,
+    ASETS_ISHIKAWA = 2
+} asets_model;
+
+/* Where a pointer lives. */
+typedef enum asets_memory { ASETS_HOST = 0, ASETS_DEVICE = 1 } asets_memory;
+
+/* Solve options; pass NULL for the defaults. */
+typedef struct asets_options {
+    int flags;       /* ASETS_FLAG_* */
+    int tile_config; /* 0 = autotuned/default, else an index from asets_tile_configs */
+    int reserved[6];
+} asets_options;
+
+/* Form |p(x)| in double precision exactly as projStep does
+ * (maxflow/asetsBinaryMF3D_mex.c:321-324), making u bit-identical to the
+ * reference C.  Without it |p(x)| is formed in float (default, faster). */
+#define ASETS_FLAG_EXACT 0x1
+/* Skip the alpha(x) > 0 validation pass. */
+#define ASETS_FLAG_NO_ALPHA_CHECK 0x2
+
+ASETS_API int asets_abi_version(void);
+ASETS_API const char *asets_status_string(asets_status s);
+/* Message of the last failure on the calling thread ("" if none). */
+ASETS_API const char *asets_last_error(void);
+
+/* ------------------------------------------------------------------------
+ * Contexts.  A context owns a CUDA stream on one device, the device buffers
+ * of the last problem shape (reused across calls of the same shape) and a
+ * pinned staging area.  Calls on one context are serialised internally;
+ * different contexts may be used from different threads.
+ * ---------------------------------------------------------------------- */
+typedef struct asets_context asets_context;
+
+ASETS_API asets_status asets_context_create(int device, asets_context **out);
+ASETS_API void asets_context_destroy(asets_context *ctx);
+/* The process-wide context used by the mex entry points (device from
+ * $ASETS_DEVICE, default 0), created on first use. */
+ASETS_API asets_status asets_default_context(asets_context **out);
+/* Launch on this CUDA stream (a cudaStream_t passed as void*, or NULL for the
+ * context's own stream). */
+ASETS_API asets_status asets_context_set_stream(asets_context *ctx, void *stream);
+
+/* ------------------------------------------------------------------------
+ * One-shot solvers with host pointers: the runMaxFlow() of each mex file,
+ * same argument meaning and order (alpha, costs, sizes, maxIt, errBound, cc,
+ * steps, outputs).  u/cvg/itNum follow the reference exactly:
+ *   u      final labelling (binary N, Potts N*L, Ishikawa N*(L-1))
+ *   cvg    maxIt entries, erriter per iteration, zero after the break
+ *   itNum  index of the iteration that met errBound, or maxIt
+ * seconds (optional, may be NULL) receives the wall time of the call.
+ * ---------------------------------------------------------------------- */
+
+/* replaces runMaxFlow, maxflow/asetsBinaryMF2D_mex.c:132-194 */
+ASETS_API asets_status asets_binary_mf2d(asets_context *ctx, const asets_options *opt,
+                                         const float *alpha, const float *Cs, const float *Ct,
+                                         int Nx, int Ny, int maxIt, float errBound, float cc,
+                                         float steps, float *u, float *cvg, int *itNum,
+                                         float *seconds);
+/* replaces runMaxFlow, maxflow/asetsBinaryMF3D_mex.c:137-203 */
+ASETS_API asets_status asets_binary_mf3d(asets_context *ctx, const asets_options *opt,
+                                         const float *alpha, const float *Cs, const float *Ct,
+                                         int Nx, int Ny, int Nz, int maxIt, float errBound,
+                                         float cc, float steps, float *u, float *cvg, int *itNum,
+                                         float *seconds);
+/* replaces runMaxFlow, maxflow/asetsPotts2D_mex.c:138-210 */
+ASETS_API asets_status asets_potts2d(asets_context *ctx, const asets_options *opt,
+                                     const float *alpha, const float *Ct, int Nx, int Ny,
+                                     int nLab, int maxIt, float errBound, float cc, float steps,
+                                     float *u, float *cvg, int *itNum, float *seconds);
+/* replaces runMaxFlow, maxflow/asetsPotts3D_mex.c:144-217 */
+ASETS_API asets_status asets_potts3d(asets_context *ctx, const asets_options *opt,
+                                     const float *alpha, const float *Ct, int Nx, int Ny, int Nz,
+                                     int nLab, int maxIt, float errBound, float cc, float steps,
+                                     float *u, float *cvg, int *itNum, float *seconds);
+/* replaces runMaxFlow, maxflow/asetsIshikawa2D_mex.c:136-219 */
+ASETS_API asets_status asets_ishikawa2d(asets_context *ctx, const asets_options *opt,
+                                        const float *alpha, const float *Ct, int Nx, int Ny,
+                                        int nLab, int maxIt, float errBound, float cc,
+                                        float steps, float *u, float *cvg, int *itNum,
+                                        float *seconds);
+/* replaces runMaxFlow, maxflow/asetsIshikawa3D_mex.c:141-228 */
+ASETS_API asets_status asets_ishikawa3d(asets_context *ctx, const asets_options *opt,
+                                        const float *alpha, const float *Ct, int Nx, int Ny,
+                                        int Nz, int nLab, int maxIt, float errBound, float cc,
+                                        float steps, float *u, float *cvg, int *itNum,
+                                        float *seconds);
+
+/* ------------------------------------------------------------------------
+ * Solver objects: device-resident problems.  Inputs are uploaded once
+ * (host or device pointers, Matlab layout); run() iterates on the device;
+ * results are read back on demand.  This is the path for repeated solves,
+ * for device-resident pipelines, and for warm starts.
+ * ---------------------------------------------------------------------- */
+typedef struct asets_solver asets_solver;
+
+/* dims: Ny (rows), Nx (cols), Nz (slices, 1 for 2D); dim is 2 or 3;
+ * nLab is 1 for binary. */
+ASETS_API asets_status asets_solver_create(asets_context *ctx, asets_model model, int dim,
+                                           int Ny, int Nx, int Nz, int nLab,
+                                           asets_solver **out);
+ASETS_API void asets_solver_destroy(asets_solver *s);
+/* Cs is used by the binary model only (NULL otherwise).  alpha has 1 (binary),
+ * L (Potts) or L-1 (Ishikawa) slices. */
+ASETS_API asets_status asets_solver_set_inputs(asets_solver *s, asets_memory where,
+                                               const float *Cs, const float *Ct,
+                                               const float *alpha);
+/* Warm start: initial u/ps/pt instead of the reference's init (the flows
+ * still start at zero, as calloc'd in runMaxFlow).  Shapes: binary u,ps,pt N;
+ * Potts u N*L, ps N, pt N*L; Ishikawa u N*(L-1), pt N*L (ps NULL).  Pass all
+ * NULL to return to the cold start. */
+ASETS_API asets_status asets_solver_set_initial(asets_solver *s, asets_memory where,
+                                                const float *u0, const float *ps0,
+                                                const float *pt0);
+/* Run up to maxIt iterations; itNum as in the one-shot calls. */
+ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_options *opt, int maxIt,
+                                        float errBound, float cc, float steps, int *itNum);
+ASETS_API asets_status asets_solver_get_u(asets_solver *s, asets_memory where, float *u);
+/* n = number of entries to copy (<= maxIt of the last run). */
+ASETS_API asets_status asets_solver_get_cvg(asets_solver *s, asets_memory where, float *cvg,
+                                            int n);
+/* Final source/sink flows (ps: binary/Potts N, NULL allowed; pt: binary N,
+ * Potts/Ishikawa N*L). */
+ASETS_API asets_status asets_solver_get_flows(asets_solver *s, asets_memory where, float *ps,
+                                              float *pt);
+/* Device time (ms) of the last run's iteration loop, from CUDA events on the
+ * launch stream, and the number of kernel launches it made. */
+ASETS_API asets_status asets_solver_last_run_stats(asets_solver *s, float *ms,
+                                                   int *kernel_launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ASETS_H */
