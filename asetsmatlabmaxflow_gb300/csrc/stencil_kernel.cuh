@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(NT, (DIM == 3 ? 2 : 4))
             for (int i = tid; i < G::FRR * G::FRC; i += NT) {
                 const int gr = 1 + i % G::FRR;
                 const int gc = (DIM == 3) ? 1 + i / G::FRR : 0;
-                const int r = r0 - 2 + gr, c = c0 - 2 + gc;
+                const int r = r0 - 2 + gr, c = (DIM == 3) ? c0 - 2 + gc : 0;
                 const int gi = gr + gc * G::GR;
                 float v = 0.f;
                 if (r >= 1 && r < nr && c >= 0 && c < nc && s_in)
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(NT, (DIM == 3 ? 2 : 4))
             if constexpr (DIM == 3) {
                 for (int i = tid; i < G::FCR * G::FCC; i += NT) {
                     const int gr = 1 + i % G::FCR, gc = 1 + i / G::FCR;
-                    const int r = r0 - 2 + gr, c = c0 - 2 + gc;
+                    const int r = r0 - 2 + gr, c = (DIM == 3) ? c0 - 2 + gc : 0;
                     const int gi = gr + gc * G::GR;
                     float v = 0.f;
                     if (r >= 0 && r < nr && c >= 1 && c < nc && s_in)
@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(NT, (DIM == 3 ? 2 : 4))
                 if (i < G::R1) {
                     const int gr = 1 + i % G::R1R;
                     const int gc = (DIM == 3) ? 1 + i / G::R1R : 0;
-                    const int r = r0 - 2 + gr, c = c0 - 2 + gc;
+                    const int r = r0 - 2 + gr, c = (DIM == 3) ? c0 - 2 + gc : 0;
                     const int gi = gr + gc * G::GR, si = gr + 2 + gc * G::LR;
                     const bool inplane = (r >= 0 && r < nr && c >= 0 && c < nc);
                     const float gk_now = GK[gi];
@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(NT, (DIM == 3 ? 2 : 4))
             for (int i = tid; i < G::HRR * G::HRC; i += NT) {
                 const int gr = 2 + i % G::HRR;
                 const int gc = (DIM == 3) ? 2 + i / G::HRR : 0;
-                const int r = r0 - 2 + gr, c = c0 - 2 + gc;
+                const int r = r0 - 2 + gr, c = (DIM == 3) ? c0 - 2 + gc : 0;
                 const int gi = gr + gc * G::GR;
                 float v = 0.f;
                 if (r >= 1 && r < nr && c >= 0 && c < nc && sp_in)
@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(NT, (DIM == 3 ? 2 : 4))
             if constexpr (DIM == 3) {
                 for (int i = tid; i < G::HCR * G::HCC; i += NT) {
                     const int gr = 2 + i % G::HCR, gc = 2 + i / G::HCR;
-                    const int r = r0 - 2 + gr, c = c0 - 2 + gc;
+                    const int r = r0 - 2 + gr, c = (DIM == 3) ? c0 - 2 + gc : 0;
                     const int gi = gr + gc * G::GR;
                     float v = 0.f;
                     if (r >= 0 && r < nr && c >= 1 && c < nc && sp_in)
@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(NT, (DIM == 3 ? 2 : 4))
                     const bool tile_cell = (gr >= 2 && gr < TR + 2 &&
                                             gc >= (DIM == 3 ? 2 : 0) && gc < (DIM == 3 ? TC + 2 : 1));
                     if (tile_cell) {
-                        const int r = r0 - 2 + gr, c = c0 - 2 + gc;
+                        const int r = r0 - 2 + gr, c = (DIM == 3) ? c0 - 2 + gc : 0;
                         const int gi = gr + gc * G::GR, si = gr + 2 + gc * G::LR;
                         const bool inplane = (r < nr && c < nc);
                         float dn = BRR[gi + 1] - BRR[gi];
