@@ -46,7 +46,24 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-iters", type=int, default=0,
+                    help="run one solve of N iterations of the workload and exit (for ncu)")
+    ap.add_argument("--shape", default="256,256,256", help="volume for --profile-iters")
     return ap.parse_args()
+
+
+def profile_run(args):
+    """One solve of the benchmark problem (or a smaller volume) for profilers."""
+    from asetsmatlabmaxflow_gb300 import native as N
+    from asetsmatlabmaxflow_gb300 import synth
+
+    shape = tuple(int(x) for x in args.shape.split(","))
+    cs, ct, alpha = synth.binary3d(seed=0, shape=shape)
+    s = N.Solver(N.Context.default(), "binary", shape)
+    s.set_inputs(ct, alpha, cs)
+    it = s.run(args.profile_iters, 0.0, CC, STEPS)
+    ms, n = s.last_run_stats()
+    print(json.dumps({"profile_run": list(shape), "iterations": it, "ms_per_launch": ms / max(n, 1)}))
 
 
 def dist_setup():
@@ -213,6 +230,9 @@ def run_reference(args, rank, pg):
 
 def main():
     args = parse()
+    if args.profile_iters:
+        profile_run(args)
+        return
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":
         run_reference(args, rank, pg)
