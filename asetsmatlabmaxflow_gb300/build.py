@@ -41,6 +41,7 @@ CU_SOURCES = (
     "flow2d.cu",
     "label_kernels.cu",
     "batch.cu",
+    "noalloc.cu",
 )
 
 MEX_SOLVERS = (

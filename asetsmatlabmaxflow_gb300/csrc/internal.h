@@ -63,4 +63,7 @@ struct InitArgs {
 cudaError_t launch_init(int model, const InitArgs &a, int num_sms, cudaStream_t st);
 cudaError_t launch_validate_alpha(const InitArgs &a, int num_sms, cudaStream_t st);
 
+// Message returned by asets_last_error() on the calling thread.
+void set_last_error(const char *msg);
+
 }  // namespace asets

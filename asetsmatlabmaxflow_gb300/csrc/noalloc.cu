@@ -1,0 +1,311 @@
+// Allocation-free binary 3D solve.
+//
+// Some callers cannot allocate device memory at solve time: a host
+// application whose device memory is owned by another allocator (a framework
+// with a caching allocator that has reserved the GPU, or Matlab's gpuArray
+// memory manager around a mex file), or a long-running pipeline that sizes
+// and reserves everything at start-up and forbids allocation afterwards.
+// For them asets_binary_mf3d_noalloc() runs the same fused iteration kernel as
+// asets_binary_mf3d() but takes every input and output as a device pointer and
+// keeps all of its scratch -- padded inputs, the ping-pong flow and
+// ps/pt/u state, the iteration control block and the erriter partials -- in
+// one file-scope device array of fixed size.  It calls no cudaMalloc,
+// cudaFree or other allocating routine.
+//
+// That array is reserved on every GPU that loads the library, for the life
+// of the process: kNoallocScratchBytes (about 15 MiB).  Problems whose padded
+// volume exceeds kNoallocMaxCells voxels are rejected.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "asets.h"
+#include "internal.h"
+
+using namespace asets;
+
+namespace {
+
+constexpr long long kNoallocMaxCells = 262144;  // padded voxels (row pitch x Nx x Nz)
+constexpr size_t kAlign = 256;
+constexpr size_t kFieldBytes = (size_t)kNoallocMaxCells * sizeof(float);
+// 3 inputs + 2 parities x (3 flow components + ps + pt + u)
+constexpr size_t kNumFields = 3 + 2 * 6;
+constexpr size_t kControlBytes = 256;
+constexpr int kMaxBlocks = 1024;
+constexpr size_t kPartialBytes = kMaxBlocks * sizeof(double);
+constexpr size_t kNoallocScratchBytes = kNumFields * kFieldBytes + kControlBytes + kPartialBytes;
+
+}  // namespace
+
+// The scratch of every call on this device.  In host code this name is only
+// a host-side stand-in; its device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+namespace {
+
+typedef CUresult (*PFN_encodeTiled_na)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                      const cuuint64_t *, const cuuint64_t *,
+                                      const cuuint32_t *, const cuuint32_t *,
+                                      CUtensorMapInterleave, CUtensorMapSwizzle,
+                                      CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+struct DeviceSetup {
+    bool ready = false;
+    unsigned char *scratch = nullptr;  // device address of g_noalloc_scratch
+    int num_sms = 0;
+    PFN_encodeTiled_na encode = nullptr;
+    std::mutex call_mu;                // serialises calls on this device
+};
+
+constexpr int kMaxDevices = 64;
+DeviceSetup g_setup[kMaxDevices];
+std::mutex g_setup_mu;
+
+// Reset of the control block for a new solve, on the solve's stream.
+__global__ void noalloc_reset_kernel(IterControl *ctl, int max_it, float err_bound, float denom)
+{
+    IterControl c;
+    memset(&c, 0, sizeof c);
+    c.done = (max_it == 0) ? 1 : 0;
+    c.last_iter = -1;
+    c.max_it = max_it;
+    c.err_bound = err_bound;
+    c.break_lt = 0;
+    c.denom = denom;
+    *ctl = c;
+}
+
+asets_status na_fail(asets_status s, const char *fmt, ...)
+{
+    static thread_local char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    set_last_error(buf);
+    return s;
+}
+
+// Set-up once per device, with that device current: look up the scratch
+// array's device address and the driver's tensor-map encoder.
+asets_status setup_device(int dev, DeviceSetup **out)
+{
+    if (dev < 0 || dev >= kMaxDevices)
+        return na_fail(ASETS_ERR_UNSUPPORTED, "device index %d not supported", dev);
+    std::lock_guard<std::mutex> lock(g_setup_mu);
+    DeviceSetup &d = g_setup[dev];
+    if (!d.ready) {
+        void *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return na_fail(ASETS_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        }
+        int sms = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess)
+            return na_fail(ASETS_ERR_CUDA, "cudaDeviceGetAttribute: %s", cudaGetErrorString(e));
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                             cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+            return na_fail(ASETS_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+        d.scratch = static_cast<unsigned char *>(ptr);
+        d.num_sms = sms;
+        d.encode = reinterpret_cast<PFN_encodeTiled_na>(fn);
+        d.ready = true;
+    }
+    *out = &d;
+    return ASETS_OK;
+}
+
+}  // namespace
+
+extern "C" ASETS_API asets_status asets_binary_mf3d_noalloc(
+    const asets_options *opt, const float *alpha, const float *Cs, const float *Ct, int Nx,
+    int Ny, int Nz, int maxIt, float errBound, float cc, float steps, float *u, float *cvg,
+    int *itNum, void *stream)
+{
+    if (!alpha || !Cs || !Ct || !u || !itNum || (maxIt > 0 && !cvg))
+        return na_fail(ASETS_ERR_INVALID_ARG, "NULL pointer argument");
+    if (Nx < 1 || Ny < 1 || Nz < 1 || maxIt < 0)
+        return na_fail(ASETS_ERR_INVALID_ARG, "bad sizes %d x %d x %d or maxIt %d", Ny, Nx, Nz,
+                       maxIt);
+    const long long pitch = (Ny >= 32) ? ((long long)Ny + 31) / 32 * 32 : ((long long)Ny + 3) / 4 * 4;
+    const long long cells = pitch * Nx * Nz;
+    if (cells > kNoallocMaxCells)
+        return na_fail(ASETS_ERR_INVALID_ARG,
+                       "problem needs %lld padded voxels; the allocation-free entry point is "
+                       "limited to %lld",
+                       cells, kNoallocMaxCells);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return na_fail(ASETS_ERR_NO_DEVICE, "no current CUDA device");
+    }
+    DeviceSetup *d = nullptr;
+    asets_status st = setup_device(dev, &d);
+    if (st != ASETS_OK)
+        return st;
+    std::lock_guard<std::mutex> call_lock(d->call_mu);
+    cudaStream_t sm = static_cast<cudaStream_t>(stream);
+
+    // carve the scratch
+    unsigned char *base = d->scratch;
+    auto field = [&](int i) { return reinterpret_cast<float *>(base + (size_t)i * kFieldBytes); };
+    float *cs = field(0), *ct = field(1), *al = field(2);
+    float *b[2][3], *ps[2], *pt[2], *uu[2];
+    for (int par = 0; par < 2; ++par) {
+        for (int k = 0; k < 3; ++k)
+            b[par][k] = field(3 + par * 6 + k);
+        ps[par] = field(3 + par * 6 + 3);
+        pt[par] = field(3 + par * 6 + 4);
+        uu[par] = field(3 + par * 6 + 5);
+    }
+    IterControl *ctl = reinterpret_cast<IterControl *>(base + kNumFields * kFieldBytes);
+    double *partials = reinterpret_cast<double *>(base + kNumFields * kFieldBytes + kControlBytes);
+
+#define NA_TRY(call)                                                                     \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            cudaGetLastError();                                                          \
+            return na_fail(ASETS_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));      \
+        }                                                                                \
+    } while (0)
+
+    // inputs into the padded layout (device to device)
+    const size_t rows = (size_t)Nx * Nz;
+    NA_TRY(cudaMemcpy2DAsync(cs, pitch * 4, Cs, (size_t)Ny * 4, (size_t)Ny * 4, rows,
+                             cudaMemcpyDeviceToDevice, sm));
+    NA_TRY(cudaMemcpy2DAsync(ct, pitch * 4, Ct, (size_t)Ny * 4, (size_t)Ny * 4, rows,
+                             cudaMemcpyDeviceToDevice, sm));
+    NA_TRY(cudaMemcpy2DAsync(al, pitch * 4, alpha, (size_t)Ny * 4, (size_t)Ny * 4, rows,
+                             cudaMemcpyDeviceToDevice, sm));
+    // state that must start at zero: the previous call left its own in place
+    const float denom = (float)(int)((long long)Nx * Ny * Nz);
+    noalloc_reset_kernel<<<1, 1, 0, sm>>>(ctl, maxIt, errBound, denom);
+    NA_TRY(cudaGetLastError());
+    for (int k = 0; k < 3; ++k)
+        NA_TRY(cudaMemsetAsync(b[0][k], 0, (size_t)cells * 4, sm));
+    if (maxIt > 0)
+        NA_TRY(cudaMemsetAsync(cvg, 0, (size_t)maxIt * 4, sm));
+
+    InitArgs ia;
+    memset(&ia, 0, sizeof ia);
+    ia.cs = cs;
+    ia.ct = ct;
+    ia.alpha = al;
+    ia.u = uu[0];
+    ia.ps = ps[0];
+    ia.pt = pt[0];
+    ia.ctl = ctl;
+    ia.cells = cells;
+    ia.label_stride = cells;
+    ia.pitch = (int)pitch;
+    ia.nr = Ny;
+    ia.nlab = 1;
+    ia.alpha_labels = 1;
+    const int flags = opt ? opt->flags : 0;
+    if (maxIt >= 1 && !(flags & ASETS_FLAG_NO_ALPHA_CHECK)) {
+        NA_TRY(launch_validate_alpha(ia, d->num_sms, sm));
+        int bad = 0;
+        NA_TRY(cudaMemcpyAsync(&bad, &ctl->alpha_bad, sizeof bad, cudaMemcpyDeviceToHost, sm));
+        NA_TRY(cudaStreamSynchronize(sm));
+        if (bad)
+            return na_fail(ASETS_ERR_ALPHA, "alpha(x) must be positive. Exiting...");
+    }
+    NA_TRY(launch_init(0, ia, d->num_sms, sm));
+
+    // kernel variant and arguments (the same fused kernel as the other entry points)
+    const int exact = (flags & ASETS_FLAG_EXACT) ? 1 : 0;
+    int nv = 0;
+    const StencilVariant *tab = binary3d_variants(&nv);
+    const StencilVariant *v = nullptr;
+    for (int i = 0; i < nv && !v; ++i)
+        if (tab[i].exact == exact)
+            v = &tab[i];
+    if (!v)
+        return na_fail(ASETS_ERR_UNSUPPORTED, "no kernel variant");
+    StencilArgs A;
+    memset(&A, 0, sizeof A);
+    const int box_cols[NUM_SLOTS] = {v->box_cols_bc, v->box_cols, v->box_cols, v->box_cols,
+                                     v->box_cols, v->box_cols, v->box_cols};
+    for (int par = 0; par < 2; ++par) {
+        float *src[NUM_SLOTS] = {b[par][0], b[par][1], b[par][2], ps[par], pt[par], uu[par], al};
+        for (int slot = 0; slot < NUM_SLOTS; ++slot) {
+            cuuint64_t dims[4] = {(cuuint64_t)Ny, (cuuint64_t)Nx, (cuuint64_t)Nz, 1};
+            cuuint64_t strides[3] = {(cuuint64_t)(pitch * 4), (cuuint64_t)(pitch * Nx * 4),
+                                     (cuuint64_t)(cells * 4)};
+            cuuint32_t box[4] = {(cuuint32_t)v->box_rows, (cuuint32_t)box_cols[slot], 1, 1};
+            cuuint32_t estr[4] = {1, 1, 1, 1};
+            CUresult r = d->encode(&A.map[par][slot], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
+                                   src[slot], dims, strides, box, estr,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS)
+                return na_fail(ASETS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+        }
+        for (int k = 0; k < 3; ++k)
+            A.dst_b[par][k] = b[par ^ 1][k];
+        A.dst_s[par][0] = ps[par ^ 1];
+        A.dst_s[par][1] = pt[par ^ 1];
+        A.dst_s[par][2] = uu[par ^ 1];
+    }
+    A.cs = cs;
+    A.ct = ct;
+    A.ctl = ctl;
+    A.partials = partials;
+    A.cvg = cvg;
+    A.pitch = pitch;
+    A.plane_stride = pitch * Nx;
+    A.label_stride = cells;
+    A.nr = Ny;
+    A.nc = Nx;
+    A.ns = Nz;
+    A.nlab_items = 1;
+    A.tiles_r = (Ny + v->tr - 1) / v->tr;
+    A.tiles_c = (Nx + v->tc - 1) / v->tc;
+    A.total_work = (long long)A.tiles_r * A.tiles_c * Nz;
+    A.cc = cc;
+    A.inv_cc = 1.0f / cc;
+    A.steps = steps;
+    NA_TRY(cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                v->smem_bytes));
+    int per_sm = 0;
+    NA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, v->nt, v->smem_bytes));
+    long long grid = (long long)d->num_sms * (per_sm > 0 ? per_sm : 1);
+    if (grid > (A.total_work + 3) / 4)
+        grid = (A.total_work + 3) / 4;
+    if (grid > kMaxBlocks)
+        grid = kMaxBlocks;
+    if (grid < 1)
+        grid = 1;
+
+    // All maxIt iterations are queued; once erriter meets errBound the
+    // remaining launches return at entry.
+    void *params[] = {&A};
+    for (int i = 0; i < maxIt; ++i)
+        NA_TRY(cudaLaunchKernel(v->fn, dim3((unsigned)grid), dim3(v->nt), params, v->smem_bytes,
+                                sm));
+    IterControl out;
+    NA_TRY(cudaMemcpyAsync(&out, ctl, sizeof out, cudaMemcpyDeviceToHost, sm));
+    NA_TRY(cudaStreamSynchronize(sm));
+    if (out.error & DEV_ERR_TIMEOUT)
+        return na_fail(ASETS_ERR_TIMEOUT, "a device-side wait timed out");
+    const int final_par = (maxIt == 0) ? 0 : ((out.last_iter + 1) & 1);
+    NA_TRY(cudaMemcpy2DAsync(u, (size_t)Ny * 4, uu[final_par], pitch * 4, (size_t)Ny * 4, rows,
+                             cudaMemcpyDeviceToDevice, sm));
+    NA_TRY(cudaStreamSynchronize(sm));
+    *itNum = (maxIt == 0) ? 0 : out.it_num;
+    return ASETS_OK;
+#undef NA_TRY
+}

@@ -33,6 +33,10 @@ static asets_status fail(asets_status s, const char *fmt, ...)
     return s;
 }
 
+namespace asets {
+void set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
+}  // namespace asets
+
 static asets_status cuda_fail(cudaError_t e, const char *what)
 {
     asets_status s = (e == cudaErrorMemoryAllocation) ? ASETS_ERR_OUT_OF_MEMORY : ASETS_ERR_CUDA;

@@ -92,6 +92,10 @@ _SIGS = {
     "asets_solver_get_flows": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP]),
     "asets_solver_last_run_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_float),
                                                    ctypes.POINTER(ctypes.c_int)]),
+    "asets_binary_mf3d_noalloc": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                                 ctypes.c_float, ctypes.c_float, _VP, _VP,
+                                                 ctypes.POINTER(ctypes.c_int), _VP]),
 }
 
 

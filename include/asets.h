@@ -169,6 +169,35 @@ ASETS_API asets_status asets_solver_get_flows(asets_solver *s, asets_memory wher
 ASETS_API asets_status asets_solver_last_run_stats(asets_solver *s, float *ms,
                                                    int *kernel_launches);
 
+/* ------------------------------------------------------------------------
+ * Allocation-free binary 3D solve.  No counterpart in the reference: it
+ * exists for callers that cannot allocate device memory while they run -- a
+ * host whose GPU memory is owned by another allocator (a framework's caching
+ * allocator that has reserved the device, Matlab's gpuArray memory manager
+ * around a mex file) or a pipeline that reserves everything at start-up and
+ * forbids allocation afterwards.
+ *
+ * Same solve as asets_binary_mf3d(), but alpha/Cs/Ct/u/cvg are DEVICE
+ * pointers (Matlab layout; cvg has maxIt entries), itNum is a host pointer,
+ * and stream is a cudaStream_t (NULL: the default stream) on the current
+ * device.  It calls no cudaMalloc/cudaFree or other allocating routine: its
+ * scratch lives in one fixed device array of about 15 MiB that every GPU
+ * loading the library reserves until the process exits.  Problems whose
+ * padded volume (row pitch x Nx x Nz, the pitch being Ny rounded up to a
+ * multiple of 32, or of 4 below 32 rows) exceeds 262144 voxels are rejected
+ * with ASETS_ERR_INVALID_ARG.  The first call on a device looks up that
+ * array's address; make it before any stream capture.  All calls on a device
+ * share the array and keep the previous call's contents (the solve clears
+ * what must start at zero); calls are serialised inside the library and each
+ * waits for its GPU work before returning -- two calls whose GPU work
+ * overlapped would race on the shared scratch.
+ * ---------------------------------------------------------------------- */
+ASETS_API asets_status asets_binary_mf3d_noalloc(const asets_options *opt, const float *alpha,
+                                                 const float *Cs, const float *Ct, int Nx,
+                                                 int Ny, int Nz, int maxIt, float errBound,
+                                                 float cc, float steps, float *u, float *cvg,
+                                                 int *itNum, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
