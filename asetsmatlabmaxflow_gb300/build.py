@@ -34,6 +34,7 @@ NVCC_FLAGS = [
 
 CU_SOURCES = (
     "runtime.cu",
+    "stencil_setup.cu",
     "init_kernels.cu",
     "binary3d.cu",
     "binary2d.cu",

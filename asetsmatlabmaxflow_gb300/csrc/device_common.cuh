@@ -161,12 +161,31 @@ struct Proj<false> {
     }
     __device__ __forceinline__ static float finish(float s, float alpha)
     {
-        float fpt = __fsqrt_rn(s * 0.5f);
-        // alpha/|p| when the projection is active; the reference's
-        // 1/(|p|/alpha) differs from this by at most one rounding.
-        return (fpt > alpha) ? __fdiv_rn(alpha, fpt) : 1.0f;
+        // alpha/|p| when |p| > alpha, from the hardware reciprocal square
+        // root; the reference's 1/(|p|/alpha) differs by a few roundings.
+        const float n2 = s * 0.5f;
+        return (n2 > alpha * alpha) ? alpha * rsqrtf(n2) : 1.0f;
     }
 };
+
+// x / d rounded to nearest for a fixed divisor, given rd = RN(1/d).
+// Markstein's correction (Markstein, "Computation of elementary functions on
+// the IBM RISC System/6000", 1990): with q = RN(x*rd) within one ulp of x/d,
+// the residual x - q*d is exact under FMA and q + residual*rd rounds to
+// RN(x/d).  It needs every intermediate in the normal range, so x outside
+// [2^-100, 2^100] in magnitude (zero, tiny, huge, non-finite) takes the IEEE
+// division.  tests/test_gpu_kernels.py compares it with __fdiv_rn over all
+// 2^32 inputs for several divisors.
+__device__ __forceinline__ float div_by(float x, float d, float rd)
+{
+    const float ax = fabsf(x);
+    if (ax >= 0x1p-100f && ax <= 0x1p100f) {
+        const float q = __fmul_rn(x, rd);
+        const float r = __fmaf_rn(-q, d, x);
+        return __fmaf_rn(r, rd, q);
+    }
+    return __fdiv_rn(x, d);
+}
 
 // MIN of the reference macros: `a < b ? a : b` (NaN picks b).
 __device__ __forceinline__ float min_ref(float a, float b) { return (a < b) ? a : b; }

@@ -13,13 +13,41 @@ namespace asets {
 // One compiled instance of stencil_iteration_kernel.
 struct StencilVariant {
     int dim, epi, exact;
-    int tr, tc, nt, nstage;
-    int smem_bytes;   // dynamic shared memory per block
-    int box_rows;     // TMA box rows (tr + 8)
-    int box_cols;     // TMA box columns for slots other than SL_BC
-    int box_cols_bc;  // TMA box columns of the SL_BC slot
+    int tr, tc, nt, nstage;  // tile rows/cols, threads, TMA ring depth
+    int smem_bytes;          // dynamic shared memory per block
+    int box_rows;            // halo box rows (tr + 8)
+    int box_cols;            // halo box columns for slots other than SL_BC
+    int box_cols_bc;         // halo box columns of the SL_BC slot
     const void *fn;
 };
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// Device buffers of one problem in the padded layout, as the iteration
+// kernel sees them.
+struct StencilProblem {
+    int nr, nc, ns;              // rows, columns (1 in 2D), stream length
+    long long pitch, plane, cells;
+    int flow_labels;             // labels swept per launch
+    float *b[2][3];              // flows [parity][SL_BC, SL_BR, SL_BS]
+    float *src[2][3];            // gk sources s0, s1, s2 per parity
+    int src_labels[3];           // label extent of each source array
+    int lab_mul[NUM_SLOTS], lab_add[NUM_SLOTS];
+    float *alpha;
+    int alpha_labels;
+    const float *cs, *ct;        // binary capacities
+    float *dst_s[2][3];          // binary: new ps/pt/u; labelled: [.][0] = divergence
+};
+
+// Fill the TMA descriptors and destinations of `A` for variant `v`.
+// Returns 0, or the CUresult of a failed encode.
+int build_stencil_args(EncodeTiledFn encode, const StencilVariant &v, const StencilProblem &p,
+                       StencilArgs2 *A);
+// Work split: stream-axis chunks per tile for `slots` resident blocks.
+int choose_zchunks(const StencilProblem &p, const StencilVariant &v, long long slots);
 
 // Variant tables, one per translation unit.
 const StencilVariant *binary3d_variants(int *count);

@@ -67,4 +67,29 @@ struct StencilArgs {
     float cc, inv_cc, steps;
 };
 
+// Arguments of the column-per-thread iteration kernel (stencil2_kernel.cuh).
+// Halo slots are SL_BC..SL_ALPHA at the step's plane; tile slots carry the
+// old ps/pt/u and the capacities of the plane two steps behind (binary).
+enum TileSlot : int { TS_S0 = 0, TS_S1 = 1, TS_S2 = 2, TS_CS = 3, TS_CT = 4, NUM_TILE_SLOTS = 5 };
+
+struct StencilArgs2 {
+    CUtensorMap halo[2][NUM_SLOTS];        // [source parity][slot]
+    CUtensorMap tile[2][NUM_TILE_SLOTS];   // binary only
+    float *dst_b[2][3];                    // [source parity][SL_BC, SL_BR, SL_BS]
+    float *dst_s[2][3];                    // binary: ps, pt, u; EPI_DIV: [.][0] = divergence
+    IterControl *ctl;
+    double *partials;
+    float *cvg;
+    long long pitch;
+    long long plane_stride;
+    long long label_stride;
+    int nr, nc, ns;
+    int nlab_items;
+    int tiles_r, tiles_c;
+    int zchunks;                           // stream-axis chunks per tile
+    int lab_mul[NUM_SLOTS];
+    int lab_add[NUM_SLOTS];
+    float cc, inv_cc, steps;
+};
+
 }  // namespace asets

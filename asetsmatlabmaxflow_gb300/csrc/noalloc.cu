@@ -234,47 +234,37 @@ extern "C" ASETS_API asets_status asets_binary_mf3d_noalloc(
             v = &tab[i];
     if (!v)
         return na_fail(ASETS_ERR_UNSUPPORTED, "no kernel variant");
-    StencilArgs A;
-    memset(&A, 0, sizeof A);
-    const int box_cols[NUM_SLOTS] = {v->box_cols_bc, v->box_cols, v->box_cols, v->box_cols,
-                                     v->box_cols, v->box_cols, v->box_cols};
+    StencilProblem p;
+    memset(&p, 0, sizeof p);
+    p.nr = Ny;
+    p.nc = Nx;
+    p.ns = Nz;
+    p.pitch = pitch;
+    p.plane = pitch * Nx;
+    p.cells = cells;
+    p.flow_labels = 1;
     for (int par = 0; par < 2; ++par) {
-        float *src[NUM_SLOTS] = {b[par][0], b[par][1], b[par][2], ps[par], pt[par], uu[par], al};
-        for (int slot = 0; slot < NUM_SLOTS; ++slot) {
-            cuuint64_t dims[4] = {(cuuint64_t)Ny, (cuuint64_t)Nx, (cuuint64_t)Nz, 1};
-            cuuint64_t strides[3] = {(cuuint64_t)(pitch * 4), (cuuint64_t)(pitch * Nx * 4),
-                                     (cuuint64_t)(cells * 4)};
-            cuuint32_t box[4] = {(cuuint32_t)v->box_rows, (cuuint32_t)box_cols[slot], 1, 1};
-            cuuint32_t estr[4] = {1, 1, 1, 1};
-            CUresult r = d->encode(&A.map[par][slot], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4,
-                                   src[slot], dims, strides, box, estr,
-                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-            if (r != CUDA_SUCCESS)
-                return na_fail(ASETS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
-        }
         for (int k = 0; k < 3; ++k)
-            A.dst_b[par][k] = b[par ^ 1][k];
-        A.dst_s[par][0] = ps[par ^ 1];
-        A.dst_s[par][1] = pt[par ^ 1];
-        A.dst_s[par][2] = uu[par ^ 1];
+            p.b[par][k] = b[par][k];
+        p.src[par][0] = ps[par];
+        p.src[par][1] = pt[par];
+        p.src[par][2] = uu[par];
+        p.dst_s[par][0] = ps[par ^ 1];
+        p.dst_s[par][1] = pt[par ^ 1];
+        p.dst_s[par][2] = uu[par ^ 1];
     }
-    A.cs = cs;
-    A.ct = ct;
+    p.src_labels[0] = p.src_labels[1] = p.src_labels[2] = 1;
+    p.alpha = al;
+    p.alpha_labels = 1;
+    p.cs = cs;
+    p.ct = ct;
+    StencilArgs2 A;
+    const int r = build_stencil_args(reinterpret_cast<EncodeTiledFn>(d->encode), *v, p, &A);
+    if (r)
+        return na_fail(ASETS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", r);
     A.ctl = ctl;
     A.partials = partials;
     A.cvg = cvg;
-    A.pitch = pitch;
-    A.plane_stride = pitch * Nx;
-    A.label_stride = cells;
-    A.nr = Ny;
-    A.nc = Nx;
-    A.ns = Nz;
-    A.nlab_items = 1;
-    A.tiles_r = (Ny + v->tr - 1) / v->tr;
-    A.tiles_c = (Nx + v->tc - 1) / v->tc;
-    A.total_work = (long long)A.tiles_r * A.tiles_c * Nz;
     A.cc = cc;
     A.inv_cc = 1.0f / cc;
     A.steps = steps;
@@ -282,9 +272,11 @@ extern "C" ASETS_API asets_status asets_binary_mf3d_noalloc(
                                 v->smem_bytes));
     int per_sm = 0;
     NA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, v->nt, v->smem_bytes));
-    long long grid = (long long)d->num_sms * (per_sm > 0 ? per_sm : 1);
-    if (grid > (A.total_work + 3) / 4)
-        grid = (A.total_work + 3) / 4;
+    const long long slots = (long long)d->num_sms * (per_sm > 0 ? per_sm : 1);
+    A.zchunks = choose_zchunks(p, *v, slots);
+    long long grid = (long long)A.tiles_r * A.tiles_c * A.zchunks;
+    if (grid > slots)
+        grid = slots;
     if (grid > kMaxBlocks)
         grid = kMaxBlocks;
     if (grid < 1)

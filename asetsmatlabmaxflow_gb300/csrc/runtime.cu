@@ -70,17 +70,13 @@ struct DeviceGuard {
 };
 
 // ---------------------------------------------------------------- context
-typedef CUresult (*PFN_encodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
-                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
-                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 struct asets_context {
     int device = 0;
     int num_sms = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
-    PFN_encodeTiled encode = nullptr;
+    EncodeTiledFn encode = nullptr;
     std::recursive_mutex mu;
     asets_solver *cached = nullptr;  // solver reused by the one-shot calls
     int *pinned_flags = nullptr;     // host-visible done flags of in-flight chunks
@@ -119,7 +115,7 @@ struct asets_solver {
     // kernel setup cache
     const StencilVariant *variant = nullptr;
     int grid = 0;
-    StencilArgs args;
+    StencilArgs2 args;
 };
 
 static asets_status get_encoder(asets_context *ctx)
@@ -130,7 +126,7 @@ static asets_status get_encoder(asets_context *ctx)
                                                      cudaEnableDefault, &q);
     if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
         return fail(ASETS_ERR_CUDA, "cuTensorMapEncodeTiled unavailable from the driver");
-    ctx->encode = reinterpret_cast<PFN_encodeTiled>(fn);
+    ctx->encode = reinterpret_cast<EncodeTiledFn>(fn);
     return ASETS_OK;
 }
 
@@ -276,25 +272,6 @@ static long long round_pitch(int nr)
     return ((long long)nr + 3) / 4 * 4;
 }
 
-static asets_status encode_map(asets_solver *s, CUtensorMap *map, float *base, int labels,
-                               int box_rows, int box_cols)
-{
-    cuuint64_t dims[4] = {(cuuint64_t)s->nr, (cuuint64_t)s->nc, (cuuint64_t)s->ns,
-                          (cuuint64_t)std::max(labels, 1)};
-    cuuint64_t strides[3] = {(cuuint64_t)(s->pitch * 4), (cuuint64_t)(s->plane * 4),
-                             (cuuint64_t)(s->cells * 4)};
-    cuuint32_t box[4] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols, 1, 1};
-    cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUresult r = s->ctx->encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box,
-                                estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS)
-        return fail(ASETS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d) rows=%d cols=%d", (int)r,
-                    box_rows, box_cols);
-    return ASETS_OK;
-}
-
 static const StencilVariant *pick_variant(const asets_solver *s, int exact, int tile_config)
 {
     int n = 0;
@@ -312,9 +289,10 @@ static const StencilVariant *pick_variant(const asets_solver *s, int exact, int 
         return nullptr;
     if (tile_config > 0 && tile_config <= (int)match.size())
         return match[tile_config - 1];
-    if (s->dim == 2 && s->nr <= 48) {
+    if (s->dim == 2 && s->nr <= 112) {
+        // short columns: the narrow 2D variant wastes fewer rows
         for (auto *v : match)
-            if (v->tr == 32)
+            if (v->tr < 112)
                 return v;
     }
     return match[0];
@@ -328,71 +306,64 @@ static asets_status setup_kernel(asets_solver *s, int exact, int tile_config)
         return fail(ASETS_ERR_UNSUPPORTED, "no kernel variant for this configuration");
     if (s->variant == v)
         return ASETS_OK;
-    StencilArgs &A = s->args;
-    memset(&A, 0, sizeof A);
     const bool binary = (s->model == ASETS_BINARY);
+    StencilProblem p;
+    memset(&p, 0, sizeof p);
+    p.nr = s->nr;
+    p.nc = s->nc;
+    p.ns = s->ns;
+    p.pitch = s->pitch;
+    p.plane = s->plane;
+    p.cells = s->cells;
+    p.flow_labels = s->flow_labels;
     for (int par = 0; par < 2; ++par) {
-        float *srcs[NUM_SLOTS];
-        int labels[NUM_SLOTS];
-        srcs[SL_BC] = s->b[par][0];
-        srcs[SL_BR] = s->b[par][1];
-        srcs[SL_BS] = s->b[par][2];
         for (int k = 0; k < 3; ++k)
-            labels[k] = s->flow_labels;
+            p.b[par][k] = s->b[par][k];
         if (binary) {
-            srcs[SL_S0] = s->ps[par]; srcs[SL_S1] = s->pt[par]; srcs[SL_S2] = s->u[par];
-            labels[SL_S0] = labels[SL_S1] = labels[SL_S2] = 1;
+            p.src[par][0] = s->ps[par];
+            p.src[par][1] = s->pt[par];
+            p.src[par][2] = s->u[par];
+            p.dst_s[par][0] = s->ps[par ^ 1];
+            p.dst_s[par][1] = s->pt[par ^ 1];
+            p.dst_s[par][2] = s->u[par ^ 1];
         } else if (s->model == ASETS_POTTS) {
-            srcs[SL_S0] = s->ps[0]; labels[SL_S0] = 1;
-            srcs[SL_S1] = s->pt[0]; labels[SL_S1] = s->nlab;
-            srcs[SL_S2] = s->u[0]; labels[SL_S2] = s->nlab;
+            p.src[par][0] = s->ps[0];
+            p.src[par][1] = s->pt[0];
+            p.src[par][2] = s->u[0];
+            p.dst_s[par][0] = s->dv;
         } else {
-            srcs[SL_S0] = s->pt[0]; labels[SL_S0] = s->nlab;
-            srcs[SL_S1] = s->pt[0]; labels[SL_S1] = s->nlab;
-            srcs[SL_S2] = s->u[0]; labels[SL_S2] = s->nlab - 1;
+            p.src[par][0] = s->pt[0];
+            p.src[par][1] = s->pt[0];
+            p.src[par][2] = s->u[0];
+            p.dst_s[par][0] = s->dv;
         }
-        srcs[SL_ALPHA] = s->alpha;
-        labels[SL_ALPHA] = s->alpha_labels;
-        for (int slot = 0; slot < NUM_SLOTS; ++slot) {
-            if (s->dim == 2 && slot == SL_BC)
-                continue;
-            int cols = (slot == SL_BC) ? v->box_cols_bc : v->box_cols;
-            asets_status st = encode_map(s, &A.map[par][slot], srcs[slot], labels[slot],
-                                         v->box_rows, cols);
-            if (st != ASETS_OK)
-                return st;
-        }
-        for (int k = 0; k < 3; ++k)
-            A.dst_b[par][k] = s->b[par ^ 1][k];
-        if (binary) {
-            A.dst_s[par][0] = s->ps[par ^ 1];
-            A.dst_s[par][1] = s->pt[par ^ 1];
-            A.dst_s[par][2] = s->u[par ^ 1];
-        } else {
-            A.dst_s[par][0] = s->dv;
-        }
+    }
+    if (binary) {
+        p.src_labels[0] = p.src_labels[1] = p.src_labels[2] = 1;
+    } else if (s->model == ASETS_POTTS) {
+        p.src_labels[0] = 1;
+        p.src_labels[1] = p.src_labels[2] = s->nlab;
+    } else {
+        p.src_labels[0] = p.src_labels[1] = s->nlab;
+        p.src_labels[2] = s->nlab - 1;
     }
     for (int slot = 0; slot < NUM_SLOTS; ++slot) {
-        A.lab_mul[slot] = binary ? 0 : 1;
-        A.lab_add[slot] = 0;
+        p.lab_mul[slot] = binary ? 0 : 1;
+        p.lab_add[slot] = 0;
     }
     if (s->model == ASETS_POTTS)
-        A.lab_mul[SL_S0] = 0;  // one shared source flow
+        p.lab_mul[SL_S0] = 0;  // one shared source flow
     if (s->model == ASETS_ISHIKAWA)
-        A.lab_add[SL_S1] = 1;  // pt_{k+1}
-    A.cs = s->cs;
-    A.ct = s->ct;
+        p.lab_add[SL_S1] = 1;  // pt_{k+1}
+    p.alpha = s->alpha;
+    p.alpha_labels = s->alpha_labels;
+    p.cs = s->cs;
+    p.ct = s->ct;
+    StencilArgs2 &A = s->args;
+    int r = build_stencil_args(s->ctx->encode, *v, p, &A);
+    if (r)
+        return fail(ASETS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", r);
     A.ctl = s->ctl;
-    A.pitch = s->pitch;
-    A.plane_stride = s->plane;
-    A.label_stride = s->cells;
-    A.nr = s->nr;
-    A.nc = s->nc;
-    A.ns = s->ns;
-    A.nlab_items = s->flow_labels;
-    A.tiles_r = (s->nr + v->tr - 1) / v->tr;
-    A.tiles_c = (s->dim == 3) ? (s->nc + v->tc - 1) / v->tc : 1;
-    A.total_work = (long long)s->flow_labels * A.tiles_r * A.tiles_c * s->ns;
 
     CU_TRY(cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 v->smem_bytes));
@@ -400,18 +371,17 @@ static asets_status setup_kernel(asets_solver *s, int exact, int tile_config)
     CU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, v->nt, v->smem_bytes));
     if (per_sm < 1)
         return fail(ASETS_ERR_UNSUPPORTED, "stencil kernel does not fit on an SM");
-    long long grid = (long long)s->ctx->num_sms * per_sm;
-    // keep at least a few planes per block: the 2-plane lag costs 4 steps
-    const long long min_planes = 4;
-    grid = std::min(grid, (A.total_work + min_planes - 1) / min_planes);
-    s->grid = (int)std::max<long long>(grid, 1);
+    const long long slots = (long long)s->ctx->num_sms * per_sm;
+    A.zchunks = choose_zchunks(p, *v, slots);
+    const long long items = (long long)s->flow_labels * A.tiles_r * A.tiles_c * A.zchunks;
+    s->grid = (int)std::max<long long>(1, std::min(items, slots));
     // one erriter partial per block of the stencil or label kernel
     const int need = std::max({s->grid, s->ctx->num_sms * 8, 1024});
     if (need > s->partials_cap) {
-        void *p = nullptr;
-        CU_TRY(cudaMalloc(&p, sizeof(double) * need));
-        s->allocations.push_back(p);
-        s->partials = static_cast<double *>(p);
+        void *ptr = nullptr;
+        CU_TRY(cudaMalloc(&ptr, sizeof(double) * need));
+        s->allocations.push_back(ptr);
+        s->partials = static_cast<double *>(ptr);
         s->partials_cap = need;
     }
     A.partials = s->partials;
@@ -703,7 +673,7 @@ extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_
         s->cvg = p;
         s->cvg_cap = maxIt;
     }
-    StencilArgs &A = s->args;
+    StencilArgs2 &A = s->args;
     A.cvg = s->cvg;
     A.cc = cc;
     A.inv_cc = 1.0f / cc;  // `1/cc` of the reference, a float division

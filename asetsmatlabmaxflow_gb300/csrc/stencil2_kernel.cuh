@@ -1,0 +1,370 @@
+// Fused ALM iteration kernel, column-per-thread form: one launch = one
+// iteration of the continuous max-flow solver (all labels of a labelled
+// model).
+//
+// It fuses, per label, the reference's updateP1, updatePX/PY/PZ, projStep,
+// updateBX/BY/BZ and divergence sweeps (maxflow/asetsBinaryMF3D_mex.c:166-180)
+// and, for the binary model, updateDIVPSPTU and the erriter sum (:398-437).
+//
+// Geometry.  Rows r (Matlab y, contiguous), columns c (Matlab x in 3D) and a
+// stream axis s (z in 3D, x in 2D).  Each warp owns 32 consecutive rows: 28
+// tile rows plus two halo rows on each side.  In 3D warp w is column
+// c0 - 2 + w of a 28 x (NW-4) tile; in 2D the NW warps are consecutive
+// 28-row sub-tiles.  Every thread owns one (r, c) column for the whole sweep
+// along s, so its indices, border flags and carried values stay in registers;
+// row neighbours come through warp shuffles, column neighbours through three
+// small shared planes.  One iteration has a stencil radius of two cells, so
+// step s computes
+//   X: gk(s) = div b(s) - ((s0 - s1) + s2/cc)               all threads
+//   Y: gradient step b'(s); projection g2(s-1); b''_s(s-1)   tile + 1
+//   Z: b''_r, b''_c of plane s-1; ps/pt/u (or div) of s-2    tile
+// with two block barriers per step.  Old-state planes come through a ring of
+// 4D TMA tiled loads; a stage holds the halo boxes of its plane and, for the
+// binary model, tile boxes of ps/pt/u/Cs/Ct two planes behind, which is the
+// plane the step writes.  Out-of-grid elements load as 0: the zero-flux
+// border of the reference.
+//
+// Work split: (label, tile, stream chunk) items ordered chunk-major so that
+// the blocks running at the same time hold neighbouring tiles at the same
+// planes and share their halos through L2.
+//
+// Arithmetic follows the reference's float expressions (build flags:
+// --fmad=false, IEEE div/sqrt).  EXACT forms |p| in double as projStep does;
+// the fast path uses a float sum and the hardware reciprocal square root.
+#pragma once
+
+#include "device_common.cuh"
+#include "iteration_end.cuh"
+#include "kernel_args.h"
+
+namespace asets {
+
+template <int DIM, int NW>
+struct ColGeom {
+    static_assert(DIM == 2 || DIM == 3, "2D or 3D");
+    static constexpr int NT = 32 * NW;
+    static constexpr int TRW = 28;                            // tile rows per warp
+    static constexpr int TR = (DIM == 3) ? TRW : TRW * NW;    // tile rows
+    static constexpr int TC = (DIM == 3) ? NW - 4 : 1;        // tile columns
+    static_assert(DIM == 2 || NW >= 5, "3D needs at least one tile column");
+    static constexpr int LR = TR + 8;                         // halo box rows (origin r0-4)
+    static_assert(LR <= 256, "TMA box dimension limit");
+    static constexpr int LC = (DIM == 3) ? TC + 4 : 1;        // halo box columns (origin c0-2)
+    static constexpr int LC_BC = (DIM == 3) ? TC + 5 : 1;     // column-face box (+forward face)
+
+    static constexpr int align128(int b) { return (b + 127) & ~127; }
+    static constexpr int halo_floats(int slot) { return slot == SL_BC ? LR * LC_BC : LR * LC; }
+    static constexpr int tile_floats() { return TR * TC; }
+    static constexpr bool has_slot(int slot) { return !(DIM == 2 && slot == SL_BC); }
+    template <int EPI>
+    static constexpr int stage_bytes()
+    {
+        int b = 0;
+        for (int s = 0; s < NUM_SLOTS; ++s)
+            if (has_slot(s))
+                b += align128(halo_floats(s) * 4);
+        if (EPI == EPI_BINARY)
+            b += NUM_TILE_SLOTS * align128(tile_floats() * 4);
+        return b;
+    }
+    template <int EPI>
+    static constexpr int tx_bytes()
+    {
+        int b = 0;
+        for (int s = 0; s < NUM_SLOTS; ++s)
+            if (has_slot(s))
+                b += halo_floats(s) * 4;
+        if (EPI == EPI_BINARY)
+            b += NUM_TILE_SLOTS * tile_floats() * 4;
+        return b;
+    }
+    static constexpr int plane_bytes() { return (DIM == 3) ? align128(NT * 4) : 0; }
+    template <int NSTAGE, int EPI>
+    static constexpr int smem_bytes()
+    {
+        // stages | GK | BC x2 | G2 | mbarriers | alignment slack
+        return NSTAGE * stage_bytes<EPI>() + 4 * plane_bytes() + NSTAGE * 8 + 128;
+    }
+};
+
+template <int DIM, int NW, int NSTAGE, int EPI, bool EXACT>
+__global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
+    stencil_col_kernel(const __grid_constant__ StencilArgs2 A)
+{
+    using G = ColGeom<DIM, NW>;
+    constexpr int NT = G::NT;
+    static_assert(NSTAGE >= 4, "stage of plane s stays resident until step s ends");
+
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ int s_abort;
+    __shared__ double s_red[NT / 32];
+    __shared__ int s_is_last;
+
+    IterControl *ctl = A.ctl;
+    if (*(volatile int *)&ctl->done)
+        return;
+    const int it = *(volatile int *)&ctl->iter;
+    const int par = it & 1;
+    const CUtensorMap *hmaps = A.halo[par];
+    const CUtensorMap *tmaps = A.tile[par];
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
+    constexpr int SB = G::template stage_bytes<EPI>();
+    auto halo_slot = [&](int st, int slot) -> float * {
+        int off = st * SB;
+        for (int s = 0; s < slot; ++s)
+            if (G::has_slot(s))
+                off += G::align128(G::halo_floats(s) * 4);
+        return reinterpret_cast<float *>(smem + off);
+    };
+    auto tile_slot = [&](int st, int ts) -> float * {
+        int off = st * SB;
+        for (int s = 0; s < NUM_SLOTS; ++s)
+            if (G::has_slot(s))
+                off += G::align128(G::halo_floats(s) * 4);
+        off += ts * G::align128(G::tile_floats() * 4);
+        return reinterpret_cast<float *>(smem + off);
+    };
+    float *planes = reinterpret_cast<float *>(smem + NSTAGE * SB);
+    constexpr int PF = G::plane_bytes() / 4;
+    float *GK = planes;
+    float *BCb0 = planes + PF, *BCb1 = planes + 2 * PF;
+    float *G2p = planes + 3 * PF;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NSTAGE * SB + 4 * G::plane_bytes());
+
+    if (tid == 0) {
+        s_abort = 0;
+        for (int i = 0; i < NSTAGE; ++i)
+            mbar_init(&bars[i], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+
+    const int nr = A.nr, nc = A.nc, ns = A.ns;
+    const float cc = A.cc, inv_cc = A.inv_cc, steps = A.steps;
+    const int tiles = A.tiles_r * A.tiles_c;
+    const long long items = (long long)A.nlab_items * tiles * A.zchunks;
+
+    // per-thread constants
+    const int row_in_tile = (DIM == 3) ? lane : G::TRW * w + lane;   // G-row index + 0
+    const int si = row_in_tile + 2 + ((DIM == 3) ? w * G::LR : 0);   // halo box index
+    const int gi = lane + 32 * w;                                     // shared plane index (3D)
+    const bool tile_row = (lane >= 2 && lane < 30);
+    const bool tile_col = (DIM == 3) ? (w >= 2 && w < G::TC + 2) : true;
+    const bool r1_row = (lane >= 1 && lane < 31);
+    const bool r1_col = (DIM == 3) ? (w >= 1 && w < G::TC + 3) : true;
+    const int ti = (DIM == 3) ? (lane - 2) + (w - 2) * G::TRW : (row_in_tile - 2);
+
+    float erru = 0.0f;
+    unsigned int q0 = 0;
+    bool aborted = false;
+
+    for (long long item = blockIdx.x; item < items && !aborted; item += gridDim.x) {
+        // chunk-major order: neighbouring tiles of one chunk run together
+        const int tile = (int)(item % tiles);
+        const long long rest = item / tiles;
+        const int chunk = (int)(rest % A.zchunks);
+        const int k = (int)(rest / A.zchunks);
+        const int s_begin = (int)((long long)ns * chunk / A.zchunks);
+        const int s_end = (int)((long long)ns * (chunk + 1) / A.zchunks);
+        if (s_end <= s_begin)
+            continue;
+        const int r0 = (tile % A.tiles_r) * G::TR;
+        const int c0 = (DIM == 3) ? (tile / A.tiles_r) * G::TC : 0;
+        const int n_steps = s_end - s_begin + 4;
+        const int n_loads = n_steps + 1;
+        const int p_first = s_begin - 2;
+        const long long lab_off = (long long)k * A.label_stride;
+
+        int lab_coord[NUM_SLOTS];
+#pragma unroll
+        for (int s = 0; s < NUM_SLOTS; ++s)
+            lab_coord[s] = k * A.lab_mul[s] + A.lab_add[s];
+
+        auto issue_load = [&](int j) {
+            const unsigned int q = q0 + j;
+            const int st = q % NSTAGE;
+            const int plane = p_first + j;
+            mbar_arrive_expect_tx(&bars[st], G::template tx_bytes<EPI>());
+#pragma unroll
+            for (int s = 0; s < NUM_SLOTS; ++s) {
+                if (!G::has_slot(s))
+                    continue;
+                tma_load_4d(halo_slot(st, s), &hmaps[s], r0 - 4, (DIM == 3) ? c0 - 2 : 0, plane,
+                            lab_coord[s], &bars[st]);
+            }
+            if constexpr (EPI == EPI_BINARY) {
+#pragma unroll
+                for (int ts = 0; ts < NUM_TILE_SLOTS; ++ts)
+                    tma_load_4d(tile_slot(st, ts), &tmaps[ts], r0, c0, plane - 2, 0, &bars[st]);
+            }
+        };
+        if (tid == 0)
+            for (int j = 0; j < NSTAGE && j < n_loads; ++j)
+                issue_load(j);
+
+        // this thread's column
+        const int r = r0 - 2 + row_in_tile;
+        const int c = (DIM == 3) ? c0 - 2 + w : 0;
+        const bool in_r = (r >= 0 && r < nr), in_c = (c >= 0 && c < nc);
+        const bool inplane = in_r && in_c;
+        const bool is_tile = tile_row && tile_col && inplane;
+        const bool fr_ok = (r >= 1 && r < nr && in_c);          // row face r
+        const bool fr1_ok = (r + 1 >= 1 && r + 1 < nr && in_c); // row face r+1
+        const bool fc_ok = (in_r && c >= 1 && c < nc);
+        const bool fc1_ok = (in_r && c + 1 >= 1 && c + 1 < nc);
+        const long long col_off = lab_off + (long long)c * A.pitch + r;
+
+        float gkprev = 0.f, bsprev = 0.f, g2prev = 1.f, alpha_prev = 1.f;
+        float br_prev = 0.f, bc_prev = 0.f, bss_cur = 0.f, bss_old = 0.f, dvp = 0.f;
+
+        for (int t = 0; t < n_steps; ++t) {
+            const int s = p_first + t;
+            const int st_cur = (q0 + t) % NSTAGE, st_nxt = (q0 + t + 1) % NSTAGE;
+            bool ok = mbar_wait_bounded(&bars[st_cur], ((q0 + t) / NSTAGE) & 1, &s_abort);
+            ok = ok && mbar_wait_bounded(&bars[st_nxt], ((q0 + t + 1) / NSTAGE) & 1, &s_abort);
+            if (__syncthreads_or(!ok)) {
+                aborted = true;
+                if (tid == 0) {
+                    s_abort = 0;
+                    // loads issued so far: the prologue, then one per step from t = 1
+                    const int issued = min(n_loads, (t >= 1) ? t + NSTAGE - 1 : NSTAGE);
+                    for (int j = t; j < issued; ++j) {
+                        const unsigned int q = q0 + j;
+                        mbar_wait_bounded(&bars[q % NSTAGE], (q / NSTAGE) & 1, &s_abort);
+                    }
+                    atomicOr(&ctl->error, DEV_ERR_TIMEOUT);
+                }
+                __syncthreads();
+                break;
+            }
+            const bool s_in = (s >= 0 && s < ns);
+
+            // ---- X: gk(s) from the old state
+            float gk, by_own, bx_own = 0.f, bs_own, alpha_cur;
+            {
+                const float *S_br = halo_slot(st_cur, SL_BR);
+                const float *S_bs = halo_slot(st_cur, SL_BS);
+                by_own = S_br[si];
+                float d = S_br[si + 1] - by_own;
+                if constexpr (DIM == 3) {
+                    const float *S_bc = halo_slot(st_cur, SL_BC);
+                    bx_own = S_bc[si];
+                    d = d + S_bc[si + G::LR];
+                    d = d - bx_own;
+                }
+                bs_own = S_bs[si];
+                d = d + halo_slot(st_nxt, SL_BS)[si];
+                d = d - bs_own;
+                const float s0 = halo_slot(st_cur, SL_S0)[si];
+                const float s1 = halo_slot(st_cur, SL_S1)[si];
+                const float s2 = halo_slot(st_cur, SL_S2)[si];
+                gk = d - ((s0 - s1) + div_by(s2, cc, inv_cc));
+                alpha_cur = halo_slot(st_cur, SL_ALPHA)[si];
+                if constexpr (DIM == 3)
+                    GK[gi] = gk;
+            }
+            __syncthreads();
+
+            // refill the slot of plane s-1 (its last readers finished before the barrier)
+            if (tid == 0 && t >= 1 && t + NSTAGE - 1 < n_loads)
+                issue_load(t + NSTAGE - 1);
+
+            // ---- Y: gradient step b'(s), projection g2(s-1), stream faces b''(s-1)
+            const float gk_up = __shfl_up_sync(0xffffffffu, gk, 1);
+            const float brn = (fr_ok && s_in) ? steps * (gk - gk_up) + by_own : 0.f;
+            float bcn = 0.f, bc_rt = 0.f;
+            float *BCc = (t & 1) ? BCb1 : BCb0;
+            const float *BCp = (t & 1) ? BCb0 : BCb1;
+            if constexpr (DIM == 3) {
+                const float gk_left = (w >= 1) ? GK[gi - 32] : 0.f;
+                bcn = (fc_ok && s_in) ? steps * (gk - gk_left) + bx_own : 0.f;
+                BCc[gi] = bcn;
+                bc_rt = (w + 1 < NW) ? BCp[gi + 32] : 0.f;  // b'_c(s-1) at c+1
+            }
+            const float bsn = (inplane && s >= 1 && s < ns) ? steps * (gk - gkprev) + bs_own : 0.f;
+            gkprev = gk;
+            const float br_dn = __shfl_down_sync(0xffffffffu, br_prev, 1);  // b'_r(s-1) at r+1
+            float g2;
+            if constexpr (DIM == 3)
+                g2 = Proj<EXACT>::gk(bc_rt, bc_prev, br_dn, br_prev, bsn, bsprev, alpha_prev);
+            else
+                g2 = Proj<EXACT>::gk(bsn, bsprev, br_dn, br_prev, alpha_prev);
+            if constexpr (DIM == 3)
+                G2p[gi] = g2;
+            const int sp = s - 1;
+            const float bssn = (inplane && sp >= 1 && sp < ns) ? ((g2 + g2prev) * 0.5f) * bsprev : 0.f;
+            if (is_tile && sp >= s_begin && sp < s_end)
+                A.dst_b[par][SL_BS][col_off + (long long)sp * A.plane_stride] = bssn;
+            bss_old = bss_cur;
+            bss_cur = bssn;
+            g2prev = g2;
+            bsprev = bsn;
+            alpha_prev = alpha_cur;
+            __syncthreads();
+
+            // ---- Z: row/column faces of plane s-1 and the output of plane s-2
+            {
+                const float g2_up = __shfl_up_sync(0xffffffffu, g2, 1);
+                const float g2_dn = __shfl_down_sync(0xffffffffu, g2, 1);
+                const bool sp_in = (sp >= 0 && sp < ns);
+                const float brr = (fr_ok && sp_in) ? ((g2 + g2_up) * 0.5f) * br_prev : 0.f;
+                const float brr1 = (fr1_ok && sp_in) ? ((g2_dn + g2) * 0.5f) * br_dn : 0.f;
+                float dn = brr1 - brr;
+                float bcc = 0.f;
+                if constexpr (DIM == 3) {
+                    const float g2_l = (w >= 1) ? G2p[gi - 32] : 1.f;
+                    const float g2_r = (w + 1 < NW) ? G2p[gi + 32] : 1.f;
+                    bcc = (fc_ok && sp_in) ? ((g2 + g2_l) * 0.5f) * bc_prev : 0.f;
+                    const float bcc1 = (fc1_ok && sp_in) ? ((g2_r + g2) * 0.5f) * bc_rt : 0.f;
+                    dn = dn + bcc1;
+                    dn = dn - bcc;
+                }
+                if (is_tile) {
+                    if (sp >= s_begin && sp < s_end) {
+                        const long long o = col_off + (long long)sp * A.plane_stride;
+                        A.dst_b[par][SL_BR][o] = brr;
+                        if constexpr (DIM == 3)
+                            A.dst_b[par][SL_BC][o] = bcc;
+                    }
+                    const int so = s - 2;
+                    if (so >= s_begin && so < s_end) {
+                        float dv = dvp + bss_cur;
+                        dv = dv - bss_old;
+                        const long long o = col_off + (long long)so * A.plane_stride;
+                        if constexpr (EPI == EPI_BINARY) {
+                            const float pt = tile_slot(st_cur, TS_S1)[ti];
+                            const float u = tile_slot(st_cur, TS_S2)[ti];
+                            const float csv = tile_slot(st_cur, TS_CS)[ti];
+                            const float ctv = tile_slot(st_cur, TS_CT)[ti];
+                            const float ucc = div_by(u, cc, inv_cc);
+                            float ps_n = ((pt - ucc) + dv) + inv_cc;
+                            ps_n = min_ref(ps_n, csv);
+                            float pt_n = (ps_n + ucc) - dv;
+                            pt_n = min_ref(pt_n, ctv);
+                            const float e = cc * ((pt_n + dv) - ps_n);
+                            erru += abs_ref(e);
+                            A.dst_s[par][0][o] = ps_n;
+                            A.dst_s[par][1][o] = pt_n;
+                            A.dst_s[par][2][o] = u - e;
+                        } else {
+                            A.dst_s[par][0][o] = dv;
+                        }
+                    }
+                }
+                dvp = dn;
+                br_prev = brn;
+                bc_prev = bcn;
+            }
+        }
+        q0 += n_loads;
+        __syncthreads();  // stage slots and shared planes are reused by the next item
+    }
+
+    if constexpr (EPI == EPI_BINARY)
+        finish_iteration<NT>(erru, ctl, A.partials, A.cvg, it, s_red, &s_is_last);
+}
+
+}  // namespace asets

@@ -1,0 +1,87 @@
+// Host-side set-up of the fused iteration kernel: TMA descriptors for the
+// halo and tile boxes of both ping-pong parities, destinations, work split.
+#include <cstring>
+
+#include "internal.h"
+
+namespace asets {
+
+static int encode(EncodeTiledFn fn, CUtensorMap *map, float *base, const StencilProblem &p,
+                  int labels, int box_rows, int box_cols)
+{
+    cuuint64_t dims[4] = {(cuuint64_t)p.nr, (cuuint64_t)p.nc, (cuuint64_t)p.ns,
+                          (cuuint64_t)(labels < 1 ? 1 : labels)};
+    cuuint64_t strides[3] = {(cuuint64_t)(p.pitch * 4), (cuuint64_t)(p.plane * 4),
+                             (cuuint64_t)(p.cells * 4)};
+    cuuint32_t box[4] = {(cuuint32_t)box_rows, (cuuint32_t)box_cols, 1, 1};
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return (int)r;
+}
+
+int build_stencil_args(EncodeTiledFn fn, const StencilVariant &v, const StencilProblem &p,
+                       StencilArgs2 *A)
+{
+    memset(A, 0, sizeof *A);
+    const bool binary = (v.epi == EPI_BINARY);
+    for (int par = 0; par < 2; ++par) {
+        float *srcs[NUM_SLOTS] = {p.b[par][0], p.b[par][1], p.b[par][2], p.src[par][0],
+                                  p.src[par][1], p.src[par][2], p.alpha};
+        int labels[NUM_SLOTS] = {p.flow_labels, p.flow_labels, p.flow_labels, p.src_labels[0],
+                                 p.src_labels[1], p.src_labels[2], p.alpha_labels};
+        for (int slot = 0; slot < NUM_SLOTS; ++slot) {
+            if (v.dim == 2 && slot == SL_BC)
+                continue;
+            const int cols = (slot == SL_BC) ? v.box_cols_bc : v.box_cols;
+            int r = encode(fn, &A->halo[par][slot], srcs[slot], p, labels[slot], v.box_rows, cols);
+            if (r)
+                return r;
+        }
+        if (binary) {
+            float *tsrc[NUM_TILE_SLOTS] = {p.src[par][0], p.src[par][1], p.src[par][2],
+                                           const_cast<float *>(p.cs), const_cast<float *>(p.ct)};
+            for (int ts = 0; ts < NUM_TILE_SLOTS; ++ts) {
+                int r = encode(fn, &A->tile[par][ts], tsrc[ts], p, 1, v.tr, v.tc);
+                if (r)
+                    return r;
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            A->dst_b[par][k] = p.b[par ^ 1][k];
+            A->dst_s[par][k] = p.dst_s[par][k];
+        }
+    }
+    for (int s = 0; s < NUM_SLOTS; ++s) {
+        A->lab_mul[s] = p.lab_mul[s];
+        A->lab_add[s] = p.lab_add[s];
+    }
+    A->pitch = p.pitch;
+    A->plane_stride = p.plane;
+    A->label_stride = p.cells;
+    A->nr = p.nr;
+    A->nc = p.nc;
+    A->ns = p.ns;
+    A->nlab_items = p.flow_labels;
+    A->tiles_r = (p.nr + v.tr - 1) / v.tr;
+    A->tiles_c = (v.dim == 3) ? (p.nc + v.tc - 1) / v.tc : 1;
+    A->zchunks = 1;
+    return 0;
+}
+
+int choose_zchunks(const StencilProblem &p, const StencilVariant &v, long long slots)
+{
+    const long long tiles = (long long)((p.nr + v.tr - 1) / v.tr) *
+                            ((v.dim == 3) ? (p.nc + v.tc - 1) / v.tc : 1) * p.flow_labels;
+    // as many chunks as fit the resident blocks, each at least 8 planes long
+    long long k = slots / (tiles > 0 ? tiles : 1);
+    const long long max_k = p.ns / 8;
+    if (k > max_k)
+        k = max_k;
+    if (k < 1)
+        k = 1;
+    return (int)k;
+}
+
+}  // namespace asets

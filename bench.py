@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="run one solve of N iterations of the workload and exit (for ncu)")
     ap.add_argument("--shape", default="256,256,256", help="volume for --profile-iters")
+    ap.add_argument("--tile-config", type=int, default=0, help="kernel variant for --profile-iters")
     return ap.parse_args()
 
 
@@ -61,9 +62,10 @@ def profile_run(args):
     cs, ct, alpha = synth.binary3d(seed=0, shape=shape)
     s = N.Solver(N.Context.default(), "binary", shape)
     s.set_inputs(ct, alpha, cs)
-    it = s.run(args.profile_iters, 0.0, CC, STEPS)
+    it = s.run(args.profile_iters, 0.0, CC, STEPS, tile_config=args.tile_config)
     ms, n = s.last_run_stats()
-    print(json.dumps({"profile_run": list(shape), "iterations": it, "ms_per_launch": ms / max(n, 1)}))
+    print(json.dumps({"profile_run": list(shape), "tile_config": args.tile_config,
+                      "iterations": it, "ms_per_launch": ms / max(n, 1)}))
 
 
 def dist_setup():
