@@ -47,12 +47,13 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase)
 {
     uint32_t ok;
+    // the thread may sleep in try_wait for up to the hint (ns) before retrying
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(phase)
+        : "r"(smem_addr(bar)), "r"(phase), "r"(20000u)
         : "memory");
     return ok != 0;
 }
@@ -161,10 +162,10 @@ struct Proj<false> {
     }
     __device__ __forceinline__ static float finish(float s, float alpha)
     {
-        // alpha/|p| when |p| > alpha, from the hardware reciprocal square
-        // root; the reference's 1/(|p|/alpha) differs by a few roundings.
-        const float n2 = s * 0.5f;
-        return (n2 > alpha * alpha) ? alpha * rsqrtf(n2) : 1.0f;
+        // min(1, alpha/|p|) from the hardware reciprocal square root: equal
+        // to the reference's (|p| > alpha ? 1/(|p|/alpha) : 1) up to a few
+        // roundings (|p| = 0 gives alpha*inf = inf, so 1).
+        return fminf(1.0f, alpha * rsqrtf(s * 0.5f));
     }
 };
 
@@ -179,7 +180,8 @@ struct Proj<false> {
 __device__ __forceinline__ float div_by(float x, float d, float rd)
 {
     const float ax = fabsf(x);
-    if (ax >= 0x1p-100f && ax <= 0x1p100f) {
+    if ((ax >= 0x1p-100f && ax <= 0x1p100f) || ax == 0.0f) {
+        // (+-0 * rd is +-0, the IEEE quotient of a zero dividend)
         const float q = __fmul_rn(x, rd);
         const float r = __fmaf_rn(-q, d, x);
         return __fmaf_rn(r, rd, q);
@@ -189,7 +191,28 @@ __device__ __forceinline__ float div_by(float x, float d, float rd)
 
 // MIN of the reference macros: `a < b ? a : b` (NaN picks b).
 __device__ __forceinline__ float min_ref(float a, float b) { return (a < b) ? a : b; }
-__device__ __forceinline__ float abs_ref(float x) { return (x > 0.0f) ? x : -x; }
+// ABS of the reference macros; identical to fabsf except for the sign of a NaN.
+__device__ __forceinline__ float abs_ref(float x) { return fabsf(x); }
+
+// EXACT keeps the reference's select and MIN forms; the fast path zeroes a
+// border term by multiplying with a 0/1 mask (FMA pipe instead of the
+// half-rate ALU pipe) and takes the hardware min.
+template <bool EXACT>
+__device__ __forceinline__ float keep_if(float v, bool ok, float okf)
+{
+    if constexpr (EXACT)
+        return ok ? v : 0.0f;
+    else
+        return v * okf;
+}
+template <bool EXACT>
+__device__ __forceinline__ float min_sel(float a, float b)
+{
+    if constexpr (EXACT)
+        return min_ref(a, b);
+    else
+        return fminf(a, b);
+}
 
 // Warp + block sum of a per-thread float into one double (lane order fixed).
 template <int NT>

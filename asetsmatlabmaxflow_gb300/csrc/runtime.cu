@@ -429,6 +429,8 @@ extern "C" ASETS_API asets_status asets_solver_create(asets_context *ctx, asets_
     s->pitch = round_pitch(Ny);
     s->plane = s->pitch * s->nc;
     s->cells = s->plane * s->ns;
+    if (s->cells * std::max(nLab, 1) >= (1LL << 32))
+        return fail(ASETS_ERR_INVALID_ARG, "padded problem exceeds 2^32 voxel-labels");
     switch (model) {
     case ASETS_BINARY:
         s->flow_labels = s->alpha_labels = s->ct_labels = s->pt_labels = s->u_labels = 1;

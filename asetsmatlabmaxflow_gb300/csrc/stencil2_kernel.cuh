@@ -151,11 +151,16 @@ __global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
     const int row_in_tile = (DIM == 3) ? lane : G::TRW * w + lane;   // G-row index + 0
     const int si = row_in_tile + 2 + ((DIM == 3) ? w * G::LR : 0);   // halo box index
     const int gi = lane + 32 * w;                                     // shared plane index (3D)
+    const int gi_left = (w >= 1) ? gi - 32 : gi;                      // column c-1 (clamped)
+    const int gi_right = (w + 1 < NW) ? gi + 32 : gi;                 // column c+1 (clamped)
     const bool tile_row = (lane >= 2 && lane < 30);
     const bool tile_col = (DIM == 3) ? (w >= 2 && w < G::TC + 2) : true;
     const bool r1_row = (lane >= 1 && lane < 31);
     const bool r1_col = (DIM == 3) ? (w >= 1 && w < G::TC + 3) : true;
     const int ti = (DIM == 3) ? (lane - 2) + (w - 2) * G::TRW : (row_in_tile - 2);
+    // The thread that issues the TMA loads and waits on their barriers; the
+    // other threads block in the following CTA barrier instead of polling.
+    const bool producer = (tid == NT - 32);
 
     float erru = 0.0f;
     unsigned int q0 = 0;
@@ -201,7 +206,7 @@ __global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
                     tma_load_4d(tile_slot(st, ts), &tmaps[ts], r0, c0, plane - 2, 0, &bars[st]);
             }
         };
-        if (tid == 0)
+        if (producer)
             for (int j = 0; j < NSTAGE && j < n_loads; ++j)
                 issue_load(j);
 
@@ -215,7 +220,18 @@ __global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
         const bool fr1_ok = (r + 1 >= 1 && r + 1 < nr && in_c); // row face r+1
         const bool fc_ok = (in_r && c >= 1 && c < nc);
         const bool fc1_ok = (in_r && c + 1 >= 1 && c + 1 < nc);
-        const long long col_off = lab_off + (long long)c * A.pitch + r;
+        const float fr_f = fr_ok ? 1.f : 0.f, fr1_f = fr1_ok ? 1.f : 0.f;
+        const float fc_f = fc_ok ? 1.f : 0.f, fc1_f = fc1_ok ? 1.f : 0.f;
+        const float in_f = inplane ? 1.f : 0.f;
+        // element offsets fit 32 bits: solves are limited to 2^31 - 1 voxel-labels
+        const unsigned int col_off = (unsigned int)(lab_off + (long long)c * A.pitch + r);
+        const unsigned int plane_stride = (unsigned int)A.plane_stride;
+        float *__restrict__ d_bs = A.dst_b[par][SL_BS];
+        float *__restrict__ d_br = A.dst_b[par][SL_BR];
+        float *__restrict__ d_bc = A.dst_b[par][SL_BC];
+        float *__restrict__ d_s0 = A.dst_s[par][0];
+        float *__restrict__ d_s1 = A.dst_s[par][1];
+        float *__restrict__ d_s2 = A.dst_s[par][2];
 
         float gkprev = 0.f, bsprev = 0.f, g2prev = 1.f, alpha_prev = 1.f;
         float br_prev = 0.f, bc_prev = 0.f, bss_cur = 0.f, bss_old = 0.f, dvp = 0.f;
@@ -223,11 +239,15 @@ __global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
         for (int t = 0; t < n_steps; ++t) {
             const int s = p_first + t;
             const int st_cur = (q0 + t) % NSTAGE, st_nxt = (q0 + t + 1) % NSTAGE;
-            bool ok = mbar_wait_bounded(&bars[st_cur], ((q0 + t) / NSTAGE) & 1, &s_abort);
-            ok = ok && mbar_wait_bounded(&bars[st_nxt], ((q0 + t + 1) / NSTAGE) & 1, &s_abort);
+            bool ok = true;
+            if (producer) {
+                ok = mbar_wait_bounded(&bars[st_cur], ((q0 + t) / NSTAGE) & 1, &s_abort);
+                ok = ok && mbar_wait_bounded(&bars[st_nxt], ((q0 + t + 1) / NSTAGE) & 1, &s_abort);
+            }
+            // the barrier publishes the completed stages to every thread
             if (__syncthreads_or(!ok)) {
                 aborted = true;
-                if (tid == 0) {
+                if (producer) {
                     s_abort = 0;
                     // loads issued so far: the prologue, then one per step from t = 1
                     const int issued = min(n_loads, (t >= 1) ? t + NSTAGE - 1 : NSTAGE);
@@ -241,6 +261,11 @@ __global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
                 break;
             }
             const bool s_in = (s >= 0 && s < ns);
+            const bool sb_in = (s >= 1 && s < ns);          // stream face s is interior
+            const bool sp_in = (s - 1 >= 0 && s - 1 < ns);
+            const bool spb_in = (s - 1 >= 1 && s - 1 < ns);
+            const float s_f = s_in ? 1.f : 0.f, sb_f = sb_in ? 1.f : 0.f;
+            const float sp_f = sp_in ? 1.f : 0.f, spb_f = spb_in ? 1.f : 0.f;
 
             // ---- X: gk(s) from the old state
             float gk, by_own, bx_own = 0.f, bs_own, alpha_cur;
@@ -269,22 +294,22 @@ __global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
             __syncthreads();
 
             // refill the slot of plane s-1 (its last readers finished before the barrier)
-            if (tid == 0 && t >= 1 && t + NSTAGE - 1 < n_loads)
+            if (producer && t >= 1 && t + NSTAGE - 1 < n_loads)
                 issue_load(t + NSTAGE - 1);
 
             // ---- Y: gradient step b'(s), projection g2(s-1), stream faces b''(s-1)
             const float gk_up = __shfl_up_sync(0xffffffffu, gk, 1);
-            const float brn = (fr_ok && s_in) ? steps * (gk - gk_up) + by_own : 0.f;
+            const float brn = keep_if<EXACT>(steps * (gk - gk_up) + by_own, fr_ok && s_in, fr_f * s_f);
             float bcn = 0.f, bc_rt = 0.f;
             float *BCc = (t & 1) ? BCb1 : BCb0;
             const float *BCp = (t & 1) ? BCb0 : BCb1;
             if constexpr (DIM == 3) {
-                const float gk_left = (w >= 1) ? GK[gi - 32] : 0.f;
-                bcn = (fc_ok && s_in) ? steps * (gk - gk_left) + bx_own : 0.f;
+                const float gk_left = GK[gi_left];
+                bcn = keep_if<EXACT>(steps * (gk - gk_left) + bx_own, fc_ok && s_in, fc_f * s_f);
                 BCc[gi] = bcn;
-                bc_rt = (w + 1 < NW) ? BCp[gi + 32] : 0.f;  // b'_c(s-1) at c+1
+                bc_rt = BCp[gi_right];  // b'_c(s-1) at c+1
             }
-            const float bsn = (inplane && s >= 1 && s < ns) ? steps * (gk - gkprev) + bs_own : 0.f;
+            const float bsn = keep_if<EXACT>(steps * (gk - gkprev) + bs_own, inplane && sb_in, in_f * sb_f);
             gkprev = gk;
             const float br_dn = __shfl_down_sync(0xffffffffu, br_prev, 1);  // b'_r(s-1) at r+1
             float g2;
@@ -295,9 +320,9 @@ __global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
             if constexpr (DIM == 3)
                 G2p[gi] = g2;
             const int sp = s - 1;
-            const float bssn = (inplane && sp >= 1 && sp < ns) ? ((g2 + g2prev) * 0.5f) * bsprev : 0.f;
+            const float bssn = keep_if<EXACT>(((g2 + g2prev) * 0.5f) * bsprev, inplane && spb_in, in_f * spb_f);
             if (is_tile && sp >= s_begin && sp < s_end)
-                A.dst_b[par][SL_BS][col_off + (long long)sp * A.plane_stride] = bssn;
+                d_bs[col_off + (unsigned int)sp * plane_stride] = bssn;
             bss_old = bss_cur;
             bss_cur = bssn;
             g2prev = g2;
@@ -309,31 +334,30 @@ __global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
             {
                 const float g2_up = __shfl_up_sync(0xffffffffu, g2, 1);
                 const float g2_dn = __shfl_down_sync(0xffffffffu, g2, 1);
-                const bool sp_in = (sp >= 0 && sp < ns);
-                const float brr = (fr_ok && sp_in) ? ((g2 + g2_up) * 0.5f) * br_prev : 0.f;
-                const float brr1 = (fr1_ok && sp_in) ? ((g2_dn + g2) * 0.5f) * br_dn : 0.f;
+                const float brr = keep_if<EXACT>(((g2 + g2_up) * 0.5f) * br_prev, fr_ok && sp_in, fr_f * sp_f);
+                const float brr1 = keep_if<EXACT>(((g2_dn + g2) * 0.5f) * br_dn, fr1_ok && sp_in, fr1_f * sp_f);
                 float dn = brr1 - brr;
                 float bcc = 0.f;
                 if constexpr (DIM == 3) {
-                    const float g2_l = (w >= 1) ? G2p[gi - 32] : 1.f;
-                    const float g2_r = (w + 1 < NW) ? G2p[gi + 32] : 1.f;
-                    bcc = (fc_ok && sp_in) ? ((g2 + g2_l) * 0.5f) * bc_prev : 0.f;
-                    const float bcc1 = (fc1_ok && sp_in) ? ((g2_r + g2) * 0.5f) * bc_rt : 0.f;
+                    const float g2_l = G2p[gi_left];
+                    const float g2_r = G2p[gi_right];
+                    bcc = keep_if<EXACT>(((g2 + g2_l) * 0.5f) * bc_prev, fc_ok && sp_in, fc_f * sp_f);
+                    const float bcc1 = keep_if<EXACT>(((g2_r + g2) * 0.5f) * bc_rt, fc1_ok && sp_in, fc1_f * sp_f);
                     dn = dn + bcc1;
                     dn = dn - bcc;
                 }
                 if (is_tile) {
                     if (sp >= s_begin && sp < s_end) {
-                        const long long o = col_off + (long long)sp * A.plane_stride;
-                        A.dst_b[par][SL_BR][o] = brr;
+                        const unsigned int o = col_off + (unsigned int)sp * plane_stride;
+                        d_br[o] = brr;
                         if constexpr (DIM == 3)
-                            A.dst_b[par][SL_BC][o] = bcc;
+                            d_bc[o] = bcc;
                     }
                     const int so = s - 2;
                     if (so >= s_begin && so < s_end) {
                         float dv = dvp + bss_cur;
                         dv = dv - bss_old;
-                        const long long o = col_off + (long long)so * A.plane_stride;
+                        const unsigned int o = col_off + (unsigned int)so * plane_stride;
                         if constexpr (EPI == EPI_BINARY) {
                             const float pt = tile_slot(st_cur, TS_S1)[ti];
                             const float u = tile_slot(st_cur, TS_S2)[ti];
@@ -341,16 +365,16 @@ __global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
                             const float ctv = tile_slot(st_cur, TS_CT)[ti];
                             const float ucc = div_by(u, cc, inv_cc);
                             float ps_n = ((pt - ucc) + dv) + inv_cc;
-                            ps_n = min_ref(ps_n, csv);
+                            ps_n = min_sel<EXACT>(ps_n, csv);
                             float pt_n = (ps_n + ucc) - dv;
-                            pt_n = min_ref(pt_n, ctv);
+                            pt_n = min_sel<EXACT>(pt_n, ctv);
                             const float e = cc * ((pt_n + dv) - ps_n);
                             erru += abs_ref(e);
-                            A.dst_s[par][0][o] = ps_n;
-                            A.dst_s[par][1][o] = pt_n;
-                            A.dst_s[par][2][o] = u - e;
+                            d_s0[o] = ps_n;
+                            d_s1[o] = pt_n;
+                            d_s2[o] = u - e;
                         } else {
-                            A.dst_s[par][0][o] = dv;
+                            d_s0[o] = dv;
                         }
                     }
                 }

@@ -74,14 +74,26 @@ int choose_zchunks(const StencilProblem &p, const StencilVariant &v, long long s
 {
     const long long tiles = (long long)((p.nr + v.tr - 1) / v.tr) *
                             ((v.dim == 3) ? (p.nc + v.tc - 1) / v.tc : 1) * p.flow_labels;
-    // as many chunks as fit the resident blocks, each at least 8 planes long
-    long long k = slots / (tiles > 0 ? tiles : 1);
-    const long long max_k = p.ns / 8;
-    if (k > max_k)
-        k = max_k;
-    if (k < 1)
-        k = 1;
-    return (int)k;
+    if (slots < 1 || tiles < 1)
+        return 1;
+    // Items (tile, chunk) run in waves of `slots` blocks; each chunk pays a
+    // 4-plane warm-up.  Pick the chunk count with the best
+    // (wave fill) x (useful planes / swept planes), chunks >= 8 planes.
+    const long long max_k = p.ns / 8 > 1 ? p.ns / 8 : 1;
+    int best = 1;
+    double best_eff = 0.0;
+    for (long long k = 1; k <= max_k && k <= 64; ++k) {
+        const long long items = tiles * k;
+        const long long waves = (items + slots - 1) / slots;
+        const double fill = (double)items / (double)(waves * slots);
+        const double planes = (double)p.ns / (double)k;
+        const double eff = fill * planes / (planes + 4.0);
+        if (eff > best_eff + 1e-9) {
+            best_eff = eff;
+            best = (int)k;
+        }
+    }
+    return best;
 }
 
 }  // namespace asets
