@@ -189,6 +189,18 @@ __device__ __forceinline__ float div_by(float x, float d, float rd)
     return __fdiv_rn(x, d);
 }
 
+// u/cc: EXACT takes the correctly rounded quotient (the reference's float
+// division); the fast path multiplies by the rounded reciprocal (within one
+// ulp of it).
+template <bool EXACT>
+__device__ __forceinline__ float div_cc(float x, float cc, float inv_cc)
+{
+    if constexpr (EXACT)
+        return div_by(x, cc, inv_cc);
+    else
+        return x * inv_cc;
+}
+
 // MIN of the reference macros: `a < b ? a : b` (NaN picks b).
 __device__ __forceinline__ float min_ref(float a, float b) { return (a < b) ? a : b; }
 // ABS of the reference macros; identical to fabsf except for the sign of a NaN.

@@ -87,8 +87,8 @@ struct ColGeom {
     }
 };
 
-template <int DIM, int NW, int NSTAGE, int EPI, bool EXACT>
-__global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
+template <int DIM, int NW, int NSTAGE, int EPI, bool EXACT, int MINB>
+__global__ void __launch_bounds__(32 * NW, MINB)
     stencil_col_kernel(const __grid_constant__ StencilArgs2 A)
 {
     using G = ColGeom<DIM, NW>;
@@ -127,6 +127,17 @@ __global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
         off += ts * G::align128(G::tile_floats() * 4);
         return reinterpret_cast<float *>(smem + off);
     };
+    // float offsets of each slot inside a stage (compile-time constants)
+    constexpr int OFF_BC = 0;
+    constexpr int OFF_BR = OFF_BC + (G::has_slot(SL_BC) ? G::align128(G::halo_floats(SL_BC) * 4) / 4 : 0);
+    constexpr int OFF_BS = OFF_BR + G::align128(G::halo_floats(SL_BR) * 4) / 4;
+    constexpr int OFF_S0 = OFF_BS + G::align128(G::halo_floats(SL_BS) * 4) / 4;
+    constexpr int OFF_S1 = OFF_S0 + G::align128(G::halo_floats(SL_S0) * 4) / 4;
+    constexpr int OFF_S2 = OFF_S1 + G::align128(G::halo_floats(SL_S1) * 4) / 4;
+    constexpr int OFF_AL = OFF_S2 + G::align128(G::halo_floats(SL_S2) * 4) / 4;
+    constexpr int OFF_T0 = OFF_AL + G::align128(G::halo_floats(SL_ALPHA) * 4) / 4;
+    constexpr int TSZ = G::align128(G::tile_floats() * 4) / 4;
+    const float *stages = reinterpret_cast<const float *>(smem);
     float *planes = reinterpret_cast<float *>(smem + NSTAGE * SB);
     constexpr int PF = G::plane_bytes() / 4;
     float *GK = planes;
@@ -268,26 +279,25 @@ __global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
             const float sp_f = sp_in ? 1.f : 0.f, spb_f = spb_in ? 1.f : 0.f;
 
             // ---- X: gk(s) from the old state
+            const float *Sc = stages + st_cur * (SB / 4) + si;   // this column in stage s
+            const float *Sn = stages + st_nxt * (SB / 4) + si;   // and in stage s+1
             float gk, by_own, bx_own = 0.f, bs_own, alpha_cur;
             {
-                const float *S_br = halo_slot(st_cur, SL_BR);
-                const float *S_bs = halo_slot(st_cur, SL_BS);
-                by_own = S_br[si];
-                float d = S_br[si + 1] - by_own;
+                by_own = Sc[OFF_BR];
+                float d = Sc[OFF_BR + 1] - by_own;
                 if constexpr (DIM == 3) {
-                    const float *S_bc = halo_slot(st_cur, SL_BC);
-                    bx_own = S_bc[si];
-                    d = d + S_bc[si + G::LR];
+                    bx_own = Sc[OFF_BC];
+                    d = d + Sc[OFF_BC + G::LR];
                     d = d - bx_own;
                 }
-                bs_own = S_bs[si];
-                d = d + halo_slot(st_nxt, SL_BS)[si];
+                bs_own = Sc[OFF_BS];
+                d = d + Sn[OFF_BS];
                 d = d - bs_own;
-                const float s0 = halo_slot(st_cur, SL_S0)[si];
-                const float s1 = halo_slot(st_cur, SL_S1)[si];
-                const float s2 = halo_slot(st_cur, SL_S2)[si];
-                gk = d - ((s0 - s1) + div_by(s2, cc, inv_cc));
-                alpha_cur = halo_slot(st_cur, SL_ALPHA)[si];
+                const float s0 = Sc[OFF_S0];
+                const float s1 = Sc[OFF_S1];
+                const float s2 = Sc[OFF_S2];
+                gk = d - ((s0 - s1) + div_cc<EXACT>(s2, cc, inv_cc));
+                alpha_cur = Sc[OFF_AL];
                 if constexpr (DIM == 3)
                     GK[gi] = gk;
             }
@@ -359,11 +369,12 @@ __global__ void __launch_bounds__(32 * NW, (DIM == 3 ? 2 : 4))
                         dv = dv - bss_old;
                         const unsigned int o = col_off + (unsigned int)so * plane_stride;
                         if constexpr (EPI == EPI_BINARY) {
-                            const float pt = tile_slot(st_cur, TS_S1)[ti];
-                            const float u = tile_slot(st_cur, TS_S2)[ti];
-                            const float csv = tile_slot(st_cur, TS_CS)[ti];
-                            const float ctv = tile_slot(st_cur, TS_CT)[ti];
-                            const float ucc = div_by(u, cc, inv_cc);
+                            const float *T = stages + st_cur * (SB / 4) + OFF_T0 + ti;
+                            const float pt = T[TS_S1 * TSZ];
+                            const float u = T[TS_S2 * TSZ];
+                            const float csv = T[TS_CS * TSZ];
+                            const float ctv = T[TS_CT * TSZ];
+                            const float ucc = div_cc<EXACT>(u, cc, inv_cc);
                             float ps_n = ((pt - ucc) + dv) + inv_cc;
                             ps_n = min_sel<EXACT>(ps_n, csv);
                             float pt_n = (ps_n + ucc) - dv;

@@ -6,7 +6,7 @@
 
 namespace asets {
 
-template <int DIM, int NW, int NSTAGE, int EPI, bool EXACT>
+template <int DIM, int NW, int NSTAGE, int EPI, bool EXACT, int MINB = (DIM == 3 ? 2 : 4)>
 StencilVariant make_variant()
 {
     using G = ColGeom<DIM, NW>;
@@ -22,7 +22,7 @@ StencilVariant make_variant()
     v.box_rows = G::LR;
     v.box_cols = G::LC;
     v.box_cols_bc = G::LC_BC;
-    v.fn = reinterpret_cast<const void *>(&stencil_col_kernel<DIM, NW, NSTAGE, EPI, EXACT>);
+    v.fn = reinterpret_cast<const void *>(&stencil_col_kernel<DIM, NW, NSTAGE, EPI, EXACT, MINB>);
     return v;
 }
 
