@@ -180,8 +180,9 @@ struct Proj<false> {
 __device__ __forceinline__ float div_by(float x, float d, float rd)
 {
     const float ax = fabsf(x);
-    if ((ax >= 0x1p-100f && ax <= 0x1p100f) || ax == 0.0f) {
-        // (+-0 * rd is +-0, the IEEE quotient of a zero dividend)
+    if (ax == 0.0f)
+        return __fmul_rn(x, rd);  // +-0: the IEEE quotient keeps the sign
+    if (ax >= 0x1p-100f && ax <= 0x1p100f) {
         const float q = __fmul_rn(x, rd);
         const float r = __fmaf_rn(-q, d, x);
         return __fmaf_rn(r, rd, q);
