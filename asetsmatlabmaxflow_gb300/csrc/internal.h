@@ -42,12 +42,15 @@ struct StencilProblem {
     float *dst_s[2][3];          // binary: new ps/pt/u; labelled: [.][0] = divergence
 };
 
-// Fill the TMA descriptors and destinations of `A` for variant `v`.
+// Fill the TMA descriptors, destinations and geometry of problem `d` for
+// variant `v` (ctl/cvg/item_partials/items/cc are set by the caller).
 // Returns 0, or the CUresult of a failed encode.
-int build_stencil_args(EncodeTiledFn encode, const StencilVariant &v, const StencilProblem &p,
-                       StencilArgs2 *A);
+int build_problem_desc(EncodeTiledFn encode, const StencilVariant &v, const StencilProblem &p,
+                       ProblemDesc *d);
 // Work split: stream-axis chunks per tile for `slots` resident blocks.
 int choose_zchunks(const StencilProblem &p, const StencilVariant &v, long long slots);
+// Items of one problem with the given chunk count.
+int problem_items(const StencilProblem &p, const StencilVariant &v, int zchunks);
 
 // Variant tables, one per translation unit.
 const StencilVariant *binary3d_variants(int *count);

@@ -72,13 +72,15 @@ struct StencilArgs {
 // old ps/pt/u and the capacities of the plane two steps behind (binary).
 enum TileSlot : int { TS_S0 = 0, TS_S1 = 1, TS_S2 = 2, TS_CS = 3, TS_CT = 4, NUM_TILE_SLOTS = 5 };
 
-struct StencilArgs2 {
+// One problem of a launch, in device memory (TMA descriptors need 64-byte
+// alignment, which the CUtensorMap members give the struct).
+struct ProblemDesc {
     CUtensorMap halo[2][NUM_SLOTS];        // [source parity][slot]
     CUtensorMap tile[2][NUM_TILE_SLOTS];   // binary only
     float *dst_b[2][3];                    // [source parity][SL_BC, SL_BR, SL_BS]
     float *dst_s[2][3];                    // binary: ps, pt, u; EPI_DIV: [.][0] = divergence
     IterControl *ctl;
-    double *partials;
+    double *item_partials;                 // binary: one erriter partial per item
     float *cvg;
     long long pitch;
     long long plane_stride;
@@ -87,9 +89,19 @@ struct StencilArgs2 {
     int nlab_items;
     int tiles_r, tiles_c;
     int zchunks;                           // stream-axis chunks per tile
+    int item_begin, n_items;               // this problem's items in the launch
     int lab_mul[NUM_SLOTS];
     int lab_add[NUM_SLOTS];
     float cc, inv_cc, steps;
+};
+
+// A launch over one or more problems of the same kind (dimension, model).
+struct BatchArgs {
+    const ProblemDesc *probs;
+    const int *item_problem;   // item -> problem index
+    int total_items;
+    unsigned int *queue;       // [0] next item, [1] blocks that left
+    unsigned int *done_count;  // problems that have finished (shared by the launches of a batch)
 };
 
 }  // namespace asets

@@ -38,8 +38,12 @@ constexpr size_t kFieldBytes = (size_t)kNoallocMaxCells * sizeof(float);
 constexpr size_t kNumFields = 3 + 2 * 6;
 constexpr size_t kControlBytes = 256;
 constexpr int kMaxBlocks = 1024;
-constexpr size_t kPartialBytes = kMaxBlocks * sizeof(double);
-constexpr size_t kNoallocScratchBytes = kNumFields * kFieldBytes + kControlBytes + kPartialBytes;
+constexpr int kMaxItems = 16384;              // work items of one launch
+constexpr size_t kDescBytes = (sizeof(ProblemDesc) + 255) / 256 * 256;
+constexpr size_t kQueueBytes = 256;
+constexpr size_t kItemBytes = kMaxItems * (sizeof(int) + sizeof(double));
+constexpr size_t kNoallocScratchBytes =
+    kNumFields * kFieldBytes + kControlBytes + kDescBytes + kQueueBytes + kItemBytes;
 
 }  // namespace
 
@@ -169,8 +173,14 @@ extern "C" ASETS_API asets_status asets_binary_mf3d_noalloc(
         pt[par] = field(3 + par * 6 + 4);
         uu[par] = field(3 + par * 6 + 5);
     }
-    IterControl *ctl = reinterpret_cast<IterControl *>(base + kNumFields * kFieldBytes);
-    double *partials = reinterpret_cast<double *>(base + kNumFields * kFieldBytes + kControlBytes);
+    unsigned char *tail = base + kNumFields * kFieldBytes;
+    IterControl *ctl = reinterpret_cast<IterControl *>(tail);
+    ProblemDesc *d_desc = reinterpret_cast<ProblemDesc *>(tail + kControlBytes);
+    unsigned int *queue = reinterpret_cast<unsigned int *>(tail + kControlBytes + kDescBytes);
+    double *item_partials =
+        reinterpret_cast<double *>(tail + kControlBytes + kDescBytes + kQueueBytes);
+    int *item_problem = reinterpret_cast<int *>(tail + kControlBytes + kDescBytes + kQueueBytes +
+                                                kMaxItems * sizeof(double));
 
 #define NA_TRY(call)                                                                     \
     do {                                                                                 \
@@ -258,23 +268,38 @@ extern "C" ASETS_API asets_status asets_binary_mf3d_noalloc(
     p.alpha_labels = 1;
     p.cs = cs;
     p.ct = ct;
-    StencilArgs2 A;
-    const int r = build_stencil_args(reinterpret_cast<EncodeTiledFn>(d->encode), *v, p, &A);
+    ProblemDesc A;
+    const int r = build_problem_desc(reinterpret_cast<EncodeTiledFn>(d->encode), *v, p, &A);
     if (r)
         return na_fail(ASETS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", r);
-    A.ctl = ctl;
-    A.partials = partials;
-    A.cvg = cvg;
-    A.cc = cc;
-    A.inv_cc = 1.0f / cc;
-    A.steps = steps;
     NA_TRY(cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 v->smem_bytes));
     int per_sm = 0;
     NA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, v->nt, v->smem_bytes));
     const long long slots = (long long)d->num_sms * (per_sm > 0 ? per_sm : 1);
     A.zchunks = choose_zchunks(p, *v, slots);
-    long long grid = (long long)A.tiles_r * A.tiles_c * A.zchunks;
+    const int items = problem_items(p, *v, A.zchunks);
+    if (items > kMaxItems)
+        return na_fail(ASETS_ERR_INVALID_ARG, "problem splits into %d work items; the "
+                       "allocation-free entry point handles at most %d", items, kMaxItems);
+    A.item_begin = 0;
+    A.n_items = items;
+    A.ctl = ctl;
+    A.item_partials = item_partials;
+    A.cvg = cvg;
+    A.cc = cc;
+    A.inv_cc = 1.0f / cc;
+    A.steps = steps;
+    NA_TRY(cudaMemcpyAsync(d_desc, &A, sizeof A, cudaMemcpyHostToDevice, sm));
+    NA_TRY(cudaMemsetAsync(item_problem, 0, sizeof(int) * items, sm));
+    NA_TRY(cudaMemsetAsync(queue, 0, kQueueBytes, sm));
+    BatchArgs bargs;
+    bargs.probs = d_desc;
+    bargs.item_problem = item_problem;
+    bargs.total_items = items;
+    bargs.queue = queue;
+    bargs.done_count = queue + 2;
+    long long grid = items;
     if (grid > slots)
         grid = slots;
     if (grid > kMaxBlocks)
@@ -284,7 +309,7 @@ extern "C" ASETS_API asets_status asets_binary_mf3d_noalloc(
 
     // All maxIt iterations are queued; once erriter meets errBound the
     // remaining launches return at entry.
-    void *params[] = {&A};
+    void *params[] = {&bargs};
     for (int i = 0; i < maxIt; ++i)
         NA_TRY(cudaLaunchKernel(v->fn, dim3((unsigned)grid), dim3(v->nt), params, v->smem_bytes,
                                 sm));

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <cstdarg>
 #include <cstdio>
@@ -82,6 +83,20 @@ struct asets_context {
     int *pinned_flags = nullptr;     // host-visible done flags of in-flight chunks
 };
 
+struct ChunkGraph {
+    cudaGraphExec_t exec = nullptr;
+    const void *key_fn = nullptr;
+    float key_cc = 0.f;
+    const void *key_cvg = nullptr;
+    void reset()
+    {
+        if (exec)
+            cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        key_fn = nullptr;
+    }
+};
+
 struct asets_solver {
     asets_context *ctx = nullptr;
     asets_model model = ASETS_BINARY;
@@ -112,10 +127,18 @@ struct asets_solver {
     int last_launches = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t flag_ev[2] = {nullptr, nullptr};
-    // kernel setup cache
+    // kernel setup cache: this problem as a batch of one
     const StencilVariant *variant = nullptr;
     int grid = 0;
-    StencilArgs2 args;
+    ProblemDesc desc;                  // host copy, uploaded at each run
+    ProblemDesc *d_desc = nullptr;
+    int *d_item_problem = nullptr;
+    double *d_item_partials = nullptr;
+    unsigned int *d_queue = nullptr;
+    int items_cap = 0;
+    BatchArgs bargs;
+    ChunkGraph graph;
+    int last_iters = 0;  // iterations executed by the last run
 };
 
 static asets_status get_encoder(asets_context *ctx)
@@ -251,6 +274,7 @@ extern "C" ASETS_API void asets_solver_destroy(asets_solver *s)
         return;
     DeviceGuard guard(s->ctx->device);
     cudaStreamSynchronize(s->ctx->stream);
+    s->graph.reset();
     for (void *p : s->allocations)
         cudaFree(p);
     if (s->ev0)
@@ -359,11 +383,10 @@ static asets_status setup_kernel(asets_solver *s, int exact, int tile_config)
     p.alpha_labels = s->alpha_labels;
     p.cs = s->cs;
     p.ct = s->ct;
-    StencilArgs2 &A = s->args;
-    int r = build_stencil_args(s->ctx->encode, *v, p, &A);
+    ProblemDesc &A = s->desc;
+    int r = build_problem_desc(s->ctx->encode, *v, p, &A);
     if (r)
         return fail(ASETS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", r);
-    A.ctl = s->ctl;
 
     CU_TRY(cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 v->smem_bytes));
@@ -373,10 +396,39 @@ static asets_status setup_kernel(asets_solver *s, int exact, int tile_config)
         return fail(ASETS_ERR_UNSUPPORTED, "stencil kernel does not fit on an SM");
     const long long slots = (long long)s->ctx->num_sms * per_sm;
     A.zchunks = choose_zchunks(p, *v, slots);
-    const long long items = (long long)s->flow_labels * A.tiles_r * A.tiles_c * A.zchunks;
-    s->grid = (int)std::max<long long>(1, std::min(items, slots));
-    // one erriter partial per block of the stencil or label kernel
-    const int need = std::max({s->grid, s->ctx->num_sms * 8, 1024});
+    const int items = problem_items(p, *v, A.zchunks);
+    A.item_begin = 0;
+    A.n_items = items;
+    s->grid = (int)std::max<long long>(1, std::min<long long>(items, slots));
+    if (!s->d_desc) {
+        void *ptr = nullptr;
+        CU_TRY(cudaMalloc(&ptr, sizeof(ProblemDesc)));
+        s->allocations.push_back(ptr);
+        s->d_desc = static_cast<ProblemDesc *>(ptr);
+        CU_TRY(cudaMalloc(&ptr, 4 * sizeof(unsigned int)));
+        s->allocations.push_back(ptr);
+        s->d_queue = static_cast<unsigned int *>(ptr);
+    }
+    if (items > s->items_cap) {
+        void *ptr = nullptr;
+        CU_TRY(cudaMalloc(&ptr, sizeof(int) * items));
+        s->allocations.push_back(ptr);
+        s->d_item_problem = static_cast<int *>(ptr);
+        CU_TRY(cudaMemsetAsync(s->d_item_problem, 0, sizeof(int) * items, s->ctx->stream));
+        CU_TRY(cudaMalloc(&ptr, sizeof(double) * items));
+        s->allocations.push_back(ptr);
+        s->d_item_partials = static_cast<double *>(ptr);
+        s->items_cap = items;
+    }
+    A.ctl = s->ctl;
+    A.item_partials = s->d_item_partials;
+    s->bargs.probs = s->d_desc;
+    s->bargs.item_problem = s->d_item_problem;
+    s->bargs.total_items = items;
+    s->bargs.queue = s->d_queue;
+    s->bargs.done_count = s->d_queue + 2;
+    // erriter partials of the label kernels (labelled models)
+    const int need = std::max(s->ctx->num_sms * 8, 1024);
     if (need > s->partials_cap) {
         void *ptr = nullptr;
         CU_TRY(cudaMalloc(&ptr, sizeof(double) * need));
@@ -384,7 +436,6 @@ static asets_status setup_kernel(asets_solver *s, int exact, int tile_config)
         s->partials = static_cast<double *>(ptr);
         s->partials_cap = need;
     }
-    A.partials = s->partials;
     s->variant = v;
     return ASETS_OK;
 }
@@ -616,7 +667,7 @@ extern "C" ASETS_API asets_status asets_solver_set_initial(asets_solver *s, aset
 static cudaError_t launch_stencil(asets_solver *s)
 {
     const StencilVariant *v = s->variant;
-    void *params[] = {&s->args};
+    void *params[] = {&s->bargs};
     return cudaLaunchKernel(v->fn, dim3(s->grid), dim3(v->nt), params, v->smem_bytes,
                             s->ctx->stream);
 }
@@ -638,33 +689,25 @@ static LabelArgs label_args(asets_solver *s)
     a.pitch = (int)s->pitch;
     a.nr = s->nr;
     a.nlab = s->nlab;
-    a.cc = s->args.cc;
-    a.inv_cc = s->args.inv_cc;
+    a.cc = s->desc.cc;
+    a.inv_cc = s->desc.inv_cc;
     // `1/(cc*nLab)` of updatePSU: cc*nLab rounded to float, then divided
-    a.inv_cc_l = 1.0f / (s->args.cc * (float)s->nlab);
+    a.inv_cc_l = 1.0f / (s->desc.cc * (float)s->nlab);
     return a;
 }
 
-extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_options *opt,
-                                                   int maxIt, float errBound, float cc,
-                                                   float steps, int *itNum)
+// Reset the solver's iteration state for a run of maxIt iterations and queue
+// its initial state (zero flows; u/ps/pt from init or the warm start).
+static asets_status prepare_run(asets_solver *s, int flags, int tile_config, int maxIt,
+                                float errBound, float cc, float steps)
 {
-    if (!s)
-        return fail(ASETS_ERR_INVALID_ARG, "solver is NULL");
-    if (maxIt < 0)
-        return fail(ASETS_ERR_INVALID_ARG, "maxIt must be >= 0");
-    if (!s->inputs_set)
-        return fail(ASETS_ERR_INVALID_ARG, "inputs not set");
-    const int flags = opt ? opt->flags : 0;
-    const int exact = (flags & ASETS_FLAG_EXACT) ? 1 : 0;
-    std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
-    DeviceGuard guard(s->ctx->device);
     cudaStream_t st = s->ctx->stream;
     if (maxIt >= 1 && !s->alpha_ok && !(flags & ASETS_FLAG_NO_ALPHA_CHECK))
         return fail(ASETS_ERR_ALPHA, "%s", s->alpha_labels > 1 && s->model != ASETS_BINARY
                                                ? "alpha(x,l) must be positive. Exiting..."
                                                : "alpha(x) must be positive. Exiting...");
-    asets_status ss = setup_kernel(s, exact, opt ? opt->tile_config : 0);
+    const int exact = (flags & ASETS_FLAG_EXACT) ? 1 : 0;
+    asets_status ss = setup_kernel(s, exact, tile_config);
     if (ss != ASETS_OK)
         return ss;
     if (maxIt > s->cvg_cap) {
@@ -675,31 +718,26 @@ extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_
         s->cvg = p;
         s->cvg_cap = maxIt;
     }
-    StencilArgs2 &A = s->args;
+    ProblemDesc &A = s->desc;
     A.cvg = s->cvg;
     A.cc = cc;
     A.inv_cc = 1.0f / cc;  // `1/cc` of the reference, a float division
     A.steps = steps;
+    CU_TRY(cudaMemcpyAsync(s->d_desc, &A, sizeof A, cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemsetAsync(s->d_queue, 0, 4 * sizeof(unsigned int), st));
 
-    // control block
     IterControl c;
     memset(&c, 0, sizeof c);
-    c.iter = 0;
     c.done = (maxIt == 0) ? 1 : 0;
-    c.it_num = 0;
     c.last_iter = -1;
     c.max_it = maxIt;
     c.err_bound = errBound;
     c.break_lt = (s->model == ASETS_ISHIKAWA && s->dim == 2) ? 1 : 0;
-    {
-        long long denom = (long long)s->ny * s->nx * s->nz * s->u_labels;
-        c.denom = (float)(int)denom;  // (float)(Nx*Ny*Nz[*L]) in int arithmetic
-    }
+    c.denom = (float)(int)((long long)s->ny * s->nx * s->nz * s->u_labels);  // (float)(Nx*Ny*Nz[*L])
     CU_TRY(cudaMemcpyAsync(s->ctl, &c, sizeof c, cudaMemcpyHostToDevice, st));
     if (maxIt > 0)
         CU_TRY(cudaMemsetAsync(s->cvg, 0, sizeof(float) * maxIt, st));
 
-    // initial state: flows zero, (u, ps, pt) from init or the warm start
     const size_t n = (size_t)s->cells;
     for (int k = 0; k < 3; ++k) {
         if (s->dim == 2 && k == 0)
@@ -718,45 +756,123 @@ extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_
         InitArgs ia = init_args(s);
         CU_TRY(launch_init((int)s->model, ia, s->ctx->num_sms, st));
     }
+    s->last_max_it = maxIt;
+    return ASETS_OK;
+}
 
-    // iterate: the kernels stop by themselves once `done` is set; the host
-    // stops launching when a chunk it has already checked reports done.
-    const bool binary = (s->model == ASETS_BINARY);
-    LabelArgs la;
-    int label_grid = 0;
-    if (!binary) {
-        la = label_args(s);
-        label_grid = label_kernel_grid(s->cells, s->ctx->num_sms);
+// Kernels of one ALM iteration of a single solver.
+static cudaError_t launch_iteration(asets_solver *s)
+{
+    cudaError_t e = launch_stencil(s);
+    if (e != cudaSuccess || s->model == ASETS_BINARY)
+        return e;
+    LabelArgs la = label_args(s);
+    const int grid = label_kernel_grid(s->cells, s->ctx->num_sms);
+    return s->model == ASETS_POTTS ? launch_potts_labels(la, grid, s->ctx->stream)
+                                   : launch_ishikawa_labels(la, grid, s->ctx->stream);
+}
+
+// Iteration chunks of kGraphIters iterations are captured once into a CUDA
+// graph and replayed; the kernels skip work once their problem is done.
+static constexpr int kGraphIters = 16;
+
+
+template <class LaunchOne>
+static asets_status capture_chunk(ChunkGraph &g, cudaStream_t st, LaunchOne launch_one)
+{
+    g.reset();
+    cudaGraph_t graph = nullptr;
+    CU_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < kGraphIters && e == cudaSuccess; ++i)
+        e = launch_one();
+    cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+        if (graph)
+            cudaGraphDestroy(graph);
+        return cuda_fail(e != cudaSuccess ? e : e2, "capturing an iteration chunk");
     }
-    CU_TRY(cudaEventRecord(s->ev0, st));
-    // Chunks of kChunk iterations; at most two chunks are queued.  Before
-    // queueing chunk c the host waits for chunk c-2's done flag, so a
-    // converged solve stops launching within two chunks.
-    const int kChunk = 16;
-    int launched = 0, launches = 0, chunk = 0;
-    int *flags_h = s->ctx->pinned_flags;
+    e = cudaGraphInstantiate(&g.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "cudaGraphInstantiate");
+    return ASETS_OK;
+}
+
+// Replay chunks until `launched` reaches maxIt or the done flag read back at
+// `done_dev` equals `done_target`.  At most two chunks are queued: before
+// queueing chunk c the host looks at the flag copied after chunk c-2.
+static asets_status run_chunks(asets_context *ctx, cudaGraphExec_t exec, int maxIt,
+                               const unsigned int *done_dev, unsigned int done_target,
+                               cudaEvent_t flag_ev[2], int *chunks_out)
+{
+    cudaStream_t st = ctx->stream;
+    int *flags_h = ctx->pinned_flags;
+    int launched = 0, chunk = 0;
     while (launched < maxIt) {
         if (chunk >= 2) {
-            CU_TRY(cudaEventSynchronize(s->flag_ev[chunk % 2]));
-            if (flags_h[chunk % 2])
+            CU_TRY(cudaEventSynchronize(flag_ev[chunk % 2]));
+            if ((unsigned int)flags_h[chunk % 2] >= done_target)
                 break;
         }
-        const int nit = std::min(kChunk, maxIt - launched);
-        for (int i = 0; i < nit; ++i) {
-            CU_TRY(launch_stencil(s));
-            ++launches;
-            if (!binary) {
-                CU_TRY(s->model == ASETS_POTTS ? launch_potts_labels(la, label_grid, st)
-                                               : launch_ishikawa_labels(la, label_grid, st));
-                ++launches;
-            }
-        }
-        launched += nit;
-        CU_TRY(cudaMemcpyAsync(&flags_h[chunk % 2], &s->ctl->done, sizeof(int),
-                               cudaMemcpyDeviceToHost, st));
-        CU_TRY(cudaEventRecord(s->flag_ev[chunk % 2], st));
+        CU_TRY(cudaGraphLaunch(exec, st));
+        launched += kGraphIters;
+        CU_TRY(cudaMemcpyAsync(&flags_h[chunk % 2], done_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaEventRecord(flag_ev[chunk % 2], st));
         ++chunk;
     }
+    *chunks_out = chunk;
+    return ASETS_OK;
+}
+
+// Read back the control block after the run and record the result.
+static asets_status finish_run(asets_solver *s, const IterControl &out, int *itNum)
+{
+    const int maxIt = s->last_max_it;
+    if (out.error & DEV_ERR_TIMEOUT)
+        return fail(ASETS_ERR_TIMEOUT, "a device-side wait for a TMA load timed out");
+    if (maxIt > 0 && !out.done)
+        return fail(ASETS_ERR_CUDA, "iteration loop ended without completion (iter=%d)", out.iter);
+    s->final_parity = (s->model == ASETS_BINARY) ? ((out.last_iter + 1) & 1) : 0;
+    if (itNum)
+        *itNum = (maxIt == 0) ? 0 : out.it_num;
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_options *opt,
+                                                   int maxIt, float errBound, float cc,
+                                                   float steps, int *itNum)
+{
+    if (!s)
+        return fail(ASETS_ERR_INVALID_ARG, "solver is NULL");
+    if (maxIt < 0)
+        return fail(ASETS_ERR_INVALID_ARG, "maxIt must be >= 0");
+    if (!s->inputs_set)
+        return fail(ASETS_ERR_INVALID_ARG, "inputs not set");
+    const int flags = opt ? opt->flags : 0;
+    std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
+    DeviceGuard guard(s->ctx->device);
+    cudaStream_t st = s->ctx->stream;
+    asets_status ss = prepare_run(s, flags, opt ? opt->tile_config : 0, maxIt, errBound, cc, steps);
+    if (ss != ASETS_OK)
+        return ss;
+    // the labelled models pass cc by value to the label kernel: recapture
+    // when it changes
+    if (!s->graph.exec || s->graph.key_fn != s->variant->fn ||
+        (s->model != ASETS_BINARY && (s->graph.key_cc != cc || s->graph.key_cvg != s->cvg))) {
+        ss = capture_chunk(s->graph, st, [&] { return launch_iteration(s); });
+        if (ss != ASETS_OK)
+            return ss;
+        s->graph.key_fn = s->variant->fn;
+        s->graph.key_cc = cc;
+        s->graph.key_cvg = s->cvg;
+    }
+    CU_TRY(cudaEventRecord(s->ev0, st));
+    int chunks = 0;
+    ss = run_chunks(s->ctx, s->graph.exec, maxIt, reinterpret_cast<const unsigned int *>(&s->ctl->done),
+                    1u, s->flag_ev, &chunks);
+    if (ss != ASETS_OK)
+        return ss;
     CU_TRY(cudaEventRecord(s->ev1, st));
     IterControl out;
     CU_TRY(cudaMemcpyAsync(&out, s->ctl, sizeof out, cudaMemcpyDeviceToHost, st));
@@ -764,16 +880,9 @@ extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_
     float ms = 0.f;
     CU_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
     s->last_ms = ms;
-    s->last_launches = launches;
-    s->last_max_it = maxIt;
-    if (out.error & DEV_ERR_TIMEOUT)
-        return fail(ASETS_ERR_TIMEOUT, "a device-side wait for a TMA load timed out");
-    if (maxIt > 0 && !out.done)
-        return fail(ASETS_ERR_CUDA, "iteration loop ended without completion (iter=%d)", out.iter);
-    s->final_parity = binary ? ((out.last_iter + 1) & 1) : 0;
-    if (itNum)
-        *itNum = (maxIt == 0) ? 0 : out.it_num;
-    return ASETS_OK;
+    s->last_launches = chunks * kGraphIters * (s->model == ASETS_BINARY ? 1 : 2);
+    s->last_iters = (maxIt == 0) ? 0 : out.last_iter + 1;
+    return finish_run(s, out, itNum);
 }
 
 extern "C" ASETS_API asets_status asets_solver_get_u(asets_solver *s, asets_memory where, float *u)
@@ -834,6 +943,379 @@ extern "C" ASETS_API asets_status asets_solver_last_run_stats(asets_solver *s, f
         *ms = s->last_ms;
     if (kernel_launches)
         *kernel_launches = s->last_launches;
+    return ASETS_OK;
+}
+
+// ---------------------------------------------------------------- batch
+// Many independent binary problems solved together: one launch per
+// dimension group and iteration over all live problems' work items; each
+// problem converges (and retires) on its own.
+struct asets_batch {
+    asets_context *ctx = nullptr;
+    std::vector<asets_solver *> members;
+    struct Group {
+        std::vector<int> idx;  // members of this group
+        const StencilVariant *v = nullptr;
+        ProblemDesc *d_desc = nullptr;
+        int desc_cap = 0;
+        int *d_item_problem = nullptr;
+        int items_cap = 0;
+        unsigned int *d_queue = nullptr;
+        BatchArgs bargs;
+        int grid = 0;
+        int tile_config = 0;
+    } groups[2];  // [0] 2D, [1] 3D
+    unsigned int *d_done = nullptr;
+    ChunkGraph graph;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, flag_ev[2] = {nullptr, nullptr};
+    std::vector<void *> allocations;
+    float last_ms = 0.f;
+    int last_launches = 0;
+};
+
+extern "C" ASETS_API asets_status asets_batch_create(asets_context *ctx, asets_batch **out)
+{
+    if (!ctx || !out)
+        return fail(ASETS_ERR_INVALID_ARG, "ctx/out is NULL");
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    DeviceGuard guard(ctx->device);
+    std::unique_ptr<asets_batch> b(new asets_batch);
+    b->ctx = ctx;
+    void *p = nullptr;
+    CU_TRY(cudaMalloc(&p, 16 * sizeof(unsigned int)));
+    b->allocations.push_back(p);
+    b->d_done = static_cast<unsigned int *>(p);
+    b->groups[0].d_queue = b->d_done + 4;
+    b->groups[1].d_queue = b->d_done + 8;
+    CU_TRY(cudaEventCreate(&b->ev0));
+    CU_TRY(cudaEventCreate(&b->ev1));
+    CU_TRY(cudaEventCreateWithFlags(&b->flag_ev[0], cudaEventDisableTiming));
+    CU_TRY(cudaEventCreateWithFlags(&b->flag_ev[1], cudaEventDisableTiming));
+    *out = b.release();
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API void asets_batch_destroy(asets_batch *b)
+{
+    if (!b)
+        return;
+    DeviceGuard guard(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    b->graph.reset();
+    for (void *p : b->allocations)
+        cudaFree(p);
+    for (cudaEvent_t e : {b->ev0, b->ev1, b->flag_ev[0], b->flag_ev[1]})
+        if (e)
+            cudaEventDestroy(e);
+    delete b;
+}
+
+extern "C" ASETS_API asets_status asets_batch_add(asets_batch *b, asets_solver *s)
+{
+    if (!b || !s)
+        return fail(ASETS_ERR_INVALID_ARG, "NULL argument");
+    if (s->ctx != b->ctx)
+        return fail(ASETS_ERR_INVALID_ARG, "solver belongs to another context");
+    if (s->model != ASETS_BINARY)
+        return fail(ASETS_ERR_UNSUPPORTED, "batches hold binary problems");
+    for (asets_solver *m : b->members)
+        if (m == s)
+            return fail(ASETS_ERR_INVALID_ARG, "solver already in the batch");
+    b->members.push_back(s);
+    b->graph.reset();
+    return ASETS_OK;
+}
+
+// Per-item partial storage of a member sized for `items`.
+static asets_status ensure_items(asets_solver *s, int items)
+{
+    if (items <= s->items_cap)
+        return ASETS_OK;
+    void *ptr = nullptr;
+    CU_TRY(cudaMalloc(&ptr, sizeof(int) * items));
+    s->allocations.push_back(ptr);
+    s->d_item_problem = static_cast<int *>(ptr);
+    CU_TRY(cudaMalloc(&ptr, sizeof(double) * items));
+    s->allocations.push_back(ptr);
+    s->d_item_partials = static_cast<double *>(ptr);
+    s->items_cap = items;
+    return ASETS_OK;
+}
+
+static asets_status batch_buffer(asets_batch *b, void **p, size_t bytes)
+{
+    CU_TRY(cudaMalloc(p, bytes));
+    b->allocations.push_back(*p);
+    return ASETS_OK;
+}
+
+// Lay out one group's descriptors and item map for a run.
+static asets_status batch_layout(asets_batch *b, asets_batch::Group &g)
+{
+    if (g.idx.empty())
+        return ASETS_OK;
+    std::vector<ProblemDesc> descs;
+    std::vector<int> item_problem;
+    for (size_t j = 0; j < g.idx.size(); ++j) {
+        asets_solver *s = b->members[g.idx[j]];
+        ProblemDesc d = s->desc;
+        // chunks of about 64 planes: the batch already fills the GPU
+        d.zchunks = std::max(1, (s->ns + 32) / 64);
+        StencilProblem sp;
+        memset(&sp, 0, sizeof sp);
+        sp.nr = s->nr;
+        sp.nc = s->nc;
+        sp.ns = s->ns;
+        sp.flow_labels = 1;
+        const int items = problem_items(sp, *g.v, d.zchunks);
+        asets_status st = ensure_items(s, items);
+        if (st != ASETS_OK)
+            return st;
+        d.item_begin = (int)item_problem.size();
+        d.n_items = items;
+        d.item_partials = s->d_item_partials;
+        s->desc.zchunks = d.zchunks;
+        s->desc.n_items = items;
+        s->desc.item_begin = d.item_begin;
+        item_problem.insert(item_problem.end(), items, (int)j);
+        descs.push_back(d);
+    }
+    cudaStream_t st = b->ctx->stream;
+    if ((int)descs.size() > g.desc_cap) {
+        void *p = nullptr;
+        asets_status s2 = batch_buffer(b, &p, sizeof(ProblemDesc) * descs.size());
+        if (s2 != ASETS_OK)
+            return s2;
+        g.d_desc = static_cast<ProblemDesc *>(p);
+        g.desc_cap = (int)descs.size();
+    }
+    if ((int)item_problem.size() > g.items_cap) {
+        void *p = nullptr;
+        asets_status s2 = batch_buffer(b, &p, sizeof(int) * item_problem.size());
+        if (s2 != ASETS_OK)
+            return s2;
+        g.d_item_problem = static_cast<int *>(p);
+        g.items_cap = (int)item_problem.size();
+    }
+    CU_TRY(cudaMemcpyAsync(g.d_desc, descs.data(), sizeof(ProblemDesc) * descs.size(),
+                           cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemcpyAsync(g.d_item_problem, item_problem.data(), sizeof(int) * item_problem.size(),
+                           cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaStreamSynchronize(st));  // host vectors go out of scope
+    int per_sm = 0;
+    CU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g.v->fn, g.v->nt,
+                                                         g.v->smem_bytes));
+    const long long slots = (long long)b->ctx->num_sms * std::max(per_sm, 1);
+    g.grid = (int)std::min<long long>((long long)item_problem.size(), slots);
+    g.bargs.probs = g.d_desc;
+    g.bargs.item_problem = g.d_item_problem;
+    g.bargs.total_items = (int)item_problem.size();
+    g.bargs.queue = g.d_queue;
+    g.bargs.done_count = b->d_done;
+    return ASETS_OK;
+}
+
+static cudaError_t batch_launch_iteration(asets_batch *b)
+{
+    for (auto &g : b->groups) {
+        if (g.idx.empty())
+            continue;
+        void *params[] = {&g.bargs};
+        cudaError_t e = cudaLaunchKernel(g.v->fn, dim3(g.grid), dim3(g.v->nt), params,
+                                         g.v->smem_bytes, b->ctx->stream);
+        if (e != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
+}
+
+// Prepare every member and lay out the groups for the given tile configs.
+static asets_status batch_prepare(asets_batch *b, int flags, const int tile_config[2], int maxIt,
+                                  float errBound, float cc, float steps)
+{
+    for (auto &g : b->groups) {
+        g.idx.clear();
+        g.v = nullptr;
+    }
+    for (size_t i = 0; i < b->members.size(); ++i) {
+        asets_solver *s = b->members[i];
+        if (!s->inputs_set)
+            return fail(ASETS_ERR_INVALID_ARG, "batch member %zu has no inputs", i);
+        const int gi = (s->dim == 3) ? 1 : 0;
+        asets_status st = prepare_run(s, flags, tile_config[gi], maxIt, errBound, cc, steps);
+        if (st != ASETS_OK)
+            return st;
+        b->groups[gi].idx.push_back((int)i);
+        b->groups[gi].v = s->variant;
+        b->groups[gi].tile_config = tile_config[gi];
+    }
+    cudaStream_t st = b->ctx->stream;
+    CU_TRY(cudaMemsetAsync(b->d_done, 0, 16 * sizeof(unsigned int), st));
+    for (auto &g : b->groups) {
+        asets_status s2 = batch_layout(b, g);
+        if (s2 != ASETS_OK)
+            return s2;
+    }
+    return ASETS_OK;
+}
+
+static asets_status batch_execute(asets_batch *b, int maxIt, int *chunks)
+{
+    cudaStream_t st = b->ctx->stream;
+    asets_status ss = capture_chunk(b->graph, st, [&] { return batch_launch_iteration(b); });
+    if (ss != ASETS_OK)
+        return ss;
+    return run_chunks(b->ctx, b->graph.exec, maxIt, b->d_done, (unsigned int)b->members.size(),
+                      b->flag_ev, chunks);
+}
+
+// Tile configuration per dimension group, chosen by timing each candidate
+// for a few iterations on this batch; cached per (group, exactness, size).
+static std::mutex g_tune_mu;
+static std::vector<std::pair<std::string, int>> g_tune_cache;
+
+static asets_status batch_autotune(asets_batch *b, int flags, float cc, float steps, int tile_config[2])
+{
+    const int exact = (flags & ASETS_FLAG_EXACT) ? 1 : 0;
+    for (int gi = 0; gi < 2; ++gi) {
+        long long vox = 0;
+        int count = 0;
+        for (asets_solver *s : b->members)
+            if ((s->dim == 3) == (gi == 1)) {
+                vox += s->cells;
+                ++count;
+            }
+        if (!count)
+            continue;
+        char key[96];
+        snprintf(key, sizeof key, "dim%d/exact%d/n%d/logvox%d", gi + 2, exact, count,
+                 (int)std::log2((double)std::max(vox, 1LL)));
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            bool found = false;
+            for (auto &kv : g_tune_cache)
+                if (kv.first == key) {
+                    tile_config[gi] = kv.second;
+                    found = true;
+                }
+            if (found)
+                continue;
+        }
+        int n = 0;
+        if (gi == 1)
+            binary3d_variants(&n);
+        else
+            binary2d_variants(&n);
+        int best = 1;
+        float best_ms = 1e30f;
+        for (int cand = 1; cand <= n / 2; ++cand) {
+            int tc[2] = {tile_config[0], tile_config[1]};
+            tc[gi] = cand;
+            asets_status st = batch_prepare(b, flags, tc, kGraphIters, 0.0f, cc, steps);
+            if (st != ASETS_OK)
+                return st;
+            int chunks = 0;
+            CU_TRY(cudaEventRecord(b->ev0, b->ctx->stream));
+            st = batch_execute(b, kGraphIters, &chunks);
+            if (st != ASETS_OK)
+                return st;
+            CU_TRY(cudaEventRecord(b->ev1, b->ctx->stream));
+            CU_TRY(cudaEventSynchronize(b->ev1));
+            float ms = 0.f;
+            CU_TRY(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = cand;
+            }
+        }
+        tile_config[gi] = best;
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache.emplace_back(key, best);
+    }
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_batch_run(asets_batch *b, const asets_options *opt,
+                                                  int maxIt, float errBound, float cc,
+                                                  float steps, int *itNums)
+{
+    if (!b)
+        return fail(ASETS_ERR_INVALID_ARG, "batch is NULL");
+    if (maxIt < 0)
+        return fail(ASETS_ERR_INVALID_ARG, "maxIt must be >= 0");
+    if (b->members.empty())
+        return ASETS_OK;
+    const int flags = opt ? opt->flags : 0;
+    std::lock_guard<std::recursive_mutex> lock(b->ctx->mu);
+    DeviceGuard guard(b->ctx->device);
+    cudaStream_t st = b->ctx->stream;
+    // one kernel variant per dimension group (default: the first)
+    const int tc0 = (opt && opt->tile_config > 0) ? opt->tile_config : 1;
+    int tile_config[2] = {tc0, tc0};
+    if ((flags & ASETS_FLAG_AUTOTUNE) && maxIt > 0) {
+        asets_status ts = batch_autotune(b, flags, cc, steps, tile_config);
+        if (ts != ASETS_OK)
+            return ts;
+    }
+    asets_status ss = batch_prepare(b, flags, tile_config, maxIt, errBound, cc, steps);
+    if (ss != ASETS_OK)
+        return ss;
+    CU_TRY(cudaEventRecord(b->ev0, st));
+    int chunks = 0;
+    if (maxIt > 0) {
+        ss = batch_execute(b, maxIt, &chunks);
+        if (ss != ASETS_OK)
+            return ss;
+    }
+    CU_TRY(cudaEventRecord(b->ev1, st));
+    std::vector<IterControl> outs(b->members.size());
+    for (size_t i = 0; i < b->members.size(); ++i)
+        CU_TRY(cudaMemcpyAsync(&outs[i], b->members[i]->ctl, sizeof(IterControl),
+                               cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    CU_TRY(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+    b->last_ms = ms;
+    int ngroups = 0;
+    for (auto &g : b->groups)
+        ngroups += g.idx.empty() ? 0 : 1;
+    b->last_launches = chunks * kGraphIters * ngroups;
+    b->groups[0].tile_config = tile_config[0];
+    b->groups[1].tile_config = tile_config[1];
+    for (size_t i = 0; i < b->members.size(); ++i) {
+        asets_solver *s = b->members[i];
+        s->last_ms = ms;
+        s->last_iters = (maxIt == 0) ? 0 : outs[i].last_iter + 1;
+        int it = 0;
+        asets_status fs = finish_run(s, outs[i], &it);
+        if (fs != ASETS_OK)
+            return fs;
+        if (itNums)
+            itNums[i] = it;
+    }
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_batch_last_run_stats(asets_batch *b, float *ms,
+                                                             int *kernel_launches,
+                                                             int *iterations, int *tile_configs)
+{
+    if (!b)
+        return fail(ASETS_ERR_INVALID_ARG, "batch is NULL");
+    if (ms)
+        *ms = b->last_ms;
+    if (kernel_launches)
+        *kernel_launches = b->last_launches;
+    if (iterations) {
+        long long total = 0;
+        for (asets_solver *s : b->members)
+            total += s->last_iters;
+        *iterations = (int)total;
+    }
+    if (tile_configs) {
+        tile_configs[0] = b->groups[0].tile_config;
+        tile_configs[1] = b->groups[1].tile_config;
+    }
     return ASETS_OK;
 }
 

@@ -24,9 +24,12 @@
 // plane the step writes.  Out-of-grid elements load as 0: the zero-flux
 // border of the reference.
 //
-// Work split: (label, tile, stream chunk) items ordered chunk-major so that
-// the blocks running at the same time hold neighbouring tiles at the same
-// planes and share their halos through L2.
+// Work split: each problem's (label, stream chunk, tile) items, ordered
+// chunk-major so that blocks running at the same time hold neighbouring tiles
+// at the same planes and share their halos through L2, are handed out by an
+// atomic queue.  One launch serves several independent problems of one kind
+// (a batch); each problem advances its own iteration when its last item
+// finishes, and items of converged problems are skipped.
 //
 // Arithmetic follows the reference's float expressions (build flags:
 // --fmad=false, IEEE div/sqrt).  EXACT forms |p| in double as projStep does;
@@ -87,9 +90,60 @@ struct ColGeom {
     }
 };
 
+template <int NT>
+__device__ __forceinline__ void finish_item(float erru, const ProblemDesc &P, int li, int it,
+                                            unsigned int *done_count, double *s_red,
+                                            int *s_is_last)
+{
+    // erriter of this item in double, then the last item of the problem's
+    // iteration sums the item partials in item order (deterministic)
+    const double part = block_sum_double<NT>(erru, s_red);
+    IterControl *ctl = P.ctl;
+    if (threadIdx.x == 0) {
+        P.item_partials[li] = part;
+        __threadfence();
+        const unsigned int ticket = atomicAdd(&ctl->ticket, 1u);
+        *s_is_last = (ticket == (unsigned int)P.n_items - 1);
+    }
+    __syncthreads();
+    if (*s_is_last && threadIdx.x < 32) {
+        __threadfence();
+        double acc = 0.0;
+        for (int b = threadIdx.x; b < P.n_items; b += 32)
+            acc += __ldcg(P.item_partials + b);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (threadIdx.x == 0) {
+            // cvg[i] = total_err / (float)N, total_err a float
+            // (maxflow/asetsBinaryMF3D_mex.c:183)
+            const float c = __fdiv_rn((float)acc, ctl->denom);
+            P.cvg[it] = c;
+            ctl->last_iter = it;
+            const bool conv = ctl->break_lt ? (c < ctl->err_bound) : (c <= ctl->err_bound);
+            int done = 0;
+            if (ctl->error || conv) {
+                done = 1;
+                ctl->it_num = it;
+            } else if (it + 1 >= ctl->max_it) {
+                done = 1;
+                ctl->it_num = ctl->max_it;
+            }
+            ctl->ticket = 0;
+            ctl->iter = it + 1;
+            if (done) {
+                ctl->done = 1;
+                atomicAdd(done_count, 1u);
+            }
+            __threadfence();
+        }
+    }
+    __syncthreads();
+}
+
 template <int DIM, int NW, int NSTAGE, int EPI, bool EXACT, int MINB>
 __global__ void __launch_bounds__(32 * NW, MINB)
-    stencil_col_kernel(const __grid_constant__ StencilArgs2 A)
+    stencil_col_kernel(const __grid_constant__ BatchArgs B)
 {
     using G = ColGeom<DIM, NW>;
     constexpr int NT = G::NT;
@@ -99,14 +153,8 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     __shared__ int s_abort;
     __shared__ double s_red[NT / 32];
     __shared__ int s_is_last;
+    __shared__ int s_item;
 
-    IterControl *ctl = A.ctl;
-    if (*(volatile int *)&ctl->done)
-        return;
-    const int it = *(volatile int *)&ctl->iter;
-    const int par = it & 1;
-    const CUtensorMap *hmaps = A.halo[par];
-    const CUtensorMap *tmaps = A.tile[par];
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
 
     unsigned char *smem = reinterpret_cast<unsigned char *>(
@@ -153,11 +201,6 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     }
     __syncthreads();
 
-    const int nr = A.nr, nc = A.nc, ns = A.ns;
-    const float cc = A.cc, inv_cc = A.inv_cc, steps = A.steps;
-    const int tiles = A.tiles_r * A.tiles_c;
-    const long long items = (long long)A.nlab_items * tiles * A.zchunks;
-
     // per-thread constants
     const int row_in_tile = (DIM == 3) ? lane : G::TRW * w + lane;   // G-row index + 0
     const int si = row_in_tile + 2 + ((DIM == 3) ? w * G::LR : 0);   // halo box index
@@ -166,38 +209,64 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     const int gi_right = (w + 1 < NW) ? gi + 32 : gi;                 // column c+1 (clamped)
     const bool tile_row = (lane >= 2 && lane < 30);
     const bool tile_col = (DIM == 3) ? (w >= 2 && w < G::TC + 2) : true;
-    const bool r1_row = (lane >= 1 && lane < 31);
-    const bool r1_col = (DIM == 3) ? (w >= 1 && w < G::TC + 3) : true;
     const int ti = (DIM == 3) ? (lane - 2) + (w - 2) * G::TRW : (row_in_tile - 2);
     // The thread that issues the TMA loads and waits on their barriers; the
     // other threads block in the following CTA barrier instead of polling.
     const bool producer = (tid == NT - 32);
 
-    float erru = 0.0f;
     unsigned int q0 = 0;
     bool aborted = false;
 
-    for (long long item = blockIdx.x; item < items && !aborted; item += gridDim.x) {
+    __shared__ int s_iter;
+    while (!aborted) {
+        // thread 0 takes the next item and reads its problem's iteration
+        // state once for the whole block
+        if (tid == 0) {
+            const int itm = (int)atomicAdd(&B.queue[0], 1u);
+            int iter = -1;
+            if (itm < B.total_items) {
+                const IterControl *c = B.probs[B.item_problem[itm]].ctl;
+                iter = *(const volatile int *)&c->done ? -1 : *(const volatile int *)&c->iter;
+            }
+            s_item = itm;
+            s_iter = iter;
+        }
+        __syncthreads();
+        const int item = s_item;
+        const int it = s_iter;
+        __syncthreads();  // s_item/s_iter are rewritten by the next fetch
+        if (item >= B.total_items)
+            break;
+        if (it < 0)
+            continue;  // the problem has converged
+        const ProblemDesc &P = B.probs[B.item_problem[item]];
+        IterControl *ctl = P.ctl;
+        const int par = it & 1;
+        const CUtensorMap *hmaps = P.halo[par];
+        const CUtensorMap *tmaps = P.tile[par];
+        const int nr = P.nr, nc = P.nc, ns = P.ns;
+        const float cc = P.cc, inv_cc = P.inv_cc, steps = P.steps;
+        const int tiles = P.tiles_r * P.tiles_c;
+        const int li = item - P.item_begin;
         // chunk-major order: neighbouring tiles of one chunk run together
-        const int tile = (int)(item % tiles);
-        const long long rest = item / tiles;
-        const int chunk = (int)(rest % A.zchunks);
-        const int k = (int)(rest / A.zchunks);
-        const int s_begin = (int)((long long)ns * chunk / A.zchunks);
-        const int s_end = (int)((long long)ns * (chunk + 1) / A.zchunks);
-        if (s_end <= s_begin)
-            continue;
-        const int r0 = (tile % A.tiles_r) * G::TR;
-        const int c0 = (DIM == 3) ? (tile / A.tiles_r) * G::TC : 0;
+        const int tile = li % tiles;
+        const int rest = li / tiles;
+        const int chunk = rest % P.zchunks;
+        const int k = rest / P.zchunks;
+        const int s_begin = (int)((long long)ns * chunk / P.zchunks);
+        const int s_end = (int)((long long)ns * (chunk + 1) / P.zchunks);
+        float erru = 0.0f;
+        const int r0 = (tile % P.tiles_r) * G::TR;
+        const int c0 = (DIM == 3) ? (tile / P.tiles_r) * G::TC : 0;
         const int n_steps = s_end - s_begin + 4;
         const int n_loads = n_steps + 1;
         const int p_first = s_begin - 2;
-        const long long lab_off = (long long)k * A.label_stride;
+        const long long lab_off = (long long)k * P.label_stride;
 
         int lab_coord[NUM_SLOTS];
 #pragma unroll
         for (int s = 0; s < NUM_SLOTS; ++s)
-            lab_coord[s] = k * A.lab_mul[s] + A.lab_add[s];
+            lab_coord[s] = k * P.lab_mul[s] + P.lab_add[s];
 
         auto issue_load = [&](int j) {
             const unsigned int q = q0 + j;
@@ -235,14 +304,14 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         const float fc_f = fc_ok ? 1.f : 0.f, fc1_f = fc1_ok ? 1.f : 0.f;
         const float in_f = inplane ? 1.f : 0.f;
         // element offsets fit 32 bits: solves are limited to 2^31 - 1 voxel-labels
-        const unsigned int col_off = (unsigned int)(lab_off + (long long)c * A.pitch + r);
-        const unsigned int plane_stride = (unsigned int)A.plane_stride;
-        float *__restrict__ d_bs = A.dst_b[par][SL_BS];
-        float *__restrict__ d_br = A.dst_b[par][SL_BR];
-        float *__restrict__ d_bc = A.dst_b[par][SL_BC];
-        float *__restrict__ d_s0 = A.dst_s[par][0];
-        float *__restrict__ d_s1 = A.dst_s[par][1];
-        float *__restrict__ d_s2 = A.dst_s[par][2];
+        const unsigned int col_off = (unsigned int)(lab_off + (long long)c * P.pitch + r);
+        const unsigned int plane_stride = (unsigned int)P.plane_stride;
+        float *__restrict__ d_bs = P.dst_b[par][SL_BS];
+        float *__restrict__ d_br = P.dst_b[par][SL_BR];
+        float *__restrict__ d_bc = P.dst_b[par][SL_BC];
+        float *__restrict__ d_s0 = P.dst_s[par][0];
+        float *__restrict__ d_s1 = P.dst_s[par][1];
+        float *__restrict__ d_s2 = P.dst_s[par][2];
 
         float gkprev = 0.f, bsprev = 0.f, g2prev = 1.f, alpha_prev = 1.f;
         float br_prev = 0.f, bc_prev = 0.f, bss_cur = 0.f, bss_old = 0.f, dvp = 0.f;
@@ -396,10 +465,19 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         }
         q0 += n_loads;
         __syncthreads();  // stage slots and shared planes are reused by the next item
+        if constexpr (EPI == EPI_BINARY)
+            finish_item<NT>(erru, P, li, it, B.done_count, s_red, &s_is_last);
     }
 
-    if constexpr (EPI == EPI_BINARY)
-        finish_iteration<NT>(erru, ctl, A.partials, A.cvg, it, s_red, &s_is_last);
+    // the last block to leave re-arms the queue for the next launch
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&B.queue[1], 1u) == gridDim.x - 1) {
+            B.queue[0] = 0;
+            B.queue[1] = 0;
+            __threadfence();
+        }
+    }
 }
 
 }  // namespace asets

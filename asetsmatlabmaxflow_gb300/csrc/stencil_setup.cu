@@ -21,8 +21,8 @@ static int encode(EncodeTiledFn fn, CUtensorMap *map, float *base, const Stencil
     return (int)r;
 }
 
-int build_stencil_args(EncodeTiledFn fn, const StencilVariant &v, const StencilProblem &p,
-                       StencilArgs2 *A)
+int build_problem_desc(EncodeTiledFn fn, const StencilVariant &v, const StencilProblem &p,
+                       ProblemDesc *A)
 {
     memset(A, 0, sizeof *A);
     const bool binary = (v.epi == EPI_BINARY);
@@ -68,6 +68,13 @@ int build_stencil_args(EncodeTiledFn fn, const StencilVariant &v, const StencilP
     A->tiles_c = (v.dim == 3) ? (p.nc + v.tc - 1) / v.tc : 1;
     A->zchunks = 1;
     return 0;
+}
+
+int problem_items(const StencilProblem &p, const StencilVariant &v, int zchunks)
+{
+    const long long tiles = (long long)((p.nr + v.tr - 1) / v.tr) *
+                            ((v.dim == 3) ? (p.nc + v.tc - 1) / v.tc : 1);
+    return (int)(tiles * p.flow_labels * zchunks);
 }
 
 int choose_zchunks(const StencilProblem &p, const StencilVariant &v, long long slots)

@@ -27,6 +27,7 @@ MODELS = {"binary": BINARY, "potts": POTTS, "ishikawa": ISHIKAWA}
 HOST, DEVICE = 0, 1
 FLAG_EXACT = 0x1
 FLAG_NO_ALPHA_CHECK = 0x2
+FLAG_AUTOTUNE = 0x4
 
 _FP = ctypes.POINTER(ctypes.c_float)
 _VP = ctypes.c_void_p
@@ -92,6 +93,14 @@ _SIGS = {
     "asets_solver_get_flows": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP]),
     "asets_solver_last_run_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_float),
                                                    ctypes.POINTER(ctypes.c_int)]),
+    "asets_batch_create": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
+    "asets_batch_destroy": (None, [_VP]),
+    "asets_batch_add": (ctypes.c_int, [_VP, _VP]),
+    "asets_batch_run": (ctypes.c_int, [_VP, _VP, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                       ctypes.c_float, _VP]),
+    "asets_batch_last_run_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_float),
+                                                  ctypes.POINTER(ctypes.c_int),
+                                                  ctypes.POINTER(ctypes.c_int), _VP]),
     "asets_binary_mf3d_noalloc": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int,
                                                  ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                                  ctypes.c_float, ctypes.c_float, _VP, _VP,
@@ -262,6 +271,53 @@ class Solver:
     def close(self) -> None:
         if self._h:
             lib().asets_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many binary solvers run together (asets_batch_*)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        h = _VP()
+        check(lib().asets_batch_create(ctx.handle, ctypes.byref(h)))
+        self._h = h.value
+        self.members: list[Solver] = []
+
+    def add(self, s: Solver) -> None:
+        check(lib().asets_batch_add(self._h, s._h))
+        self.members.append(s)
+
+    def run(self, max_it: int, err_bound: float, cc: float, steps: float, *, exact: bool = False,
+            autotune: bool = False, tile_config: int = 0) -> list[int]:
+        flags = (FLAG_EXACT if exact else 0) | (FLAG_AUTOTUNE if autotune else 0)
+        opt = Options(flags=flags, tile_config=tile_config)
+        its = (ctypes.c_int * max(len(self.members), 1))()
+        check(lib().asets_batch_run(self._h, ctypes.byref(opt), max_it, err_bound, cc, steps,
+                                    ctypes.addressof(its)))
+        for s in self.members:
+            s.last_max_it = max_it
+        return list(its[:len(self.members)])
+
+    def last_run_stats(self) -> dict:
+        ms = ctypes.c_float(0)
+        n = ctypes.c_int(0)
+        iters = ctypes.c_int(0)
+        tc = (ctypes.c_int * 2)()
+        check(lib().asets_batch_last_run_stats(self._h, ctypes.byref(ms), ctypes.byref(n),
+                                               ctypes.byref(iters), ctypes.addressof(tc)))
+        return {"ms": ms.value, "launches": n.value, "iterations": iters.value,
+                "tile_config_2d": tc[0], "tile_config_3d": tc[1]}
+
+    def close(self) -> None:
+        if self._h:
+            lib().asets_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

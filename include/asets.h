@@ -49,7 +49,7 @@ typedef enum asets_memory { ASETS_HOST = 0, ASETS_DEVICE = 1 } asets_memory;
 /* Solve options; pass NULL for the defaults. */
 typedef struct asets_options {
     int flags;       /* ASETS_FLAG_* */
-    int tile_config; /* 0 = autotuned/default, else an index from asets_tile_configs */
+    int tile_config; /* 0 = default; k >= 1 selects the k-th tile variant of the kernel */
     int reserved[6];
 } asets_options;
 
@@ -59,6 +59,9 @@ typedef struct asets_options {
 #define ASETS_FLAG_EXACT 0x1
 /* Skip the alpha(x) > 0 validation pass. */
 #define ASETS_FLAG_NO_ALPHA_CHECK 0x2
+/* Batches: time the tile configurations on the batch before solving and
+ * use the fastest (the choice is cached per process). */
+#define ASETS_FLAG_AUTOTUNE 0x4
 
 ASETS_API int asets_abi_version(void);
 ASETS_API const char *asets_status_string(asets_status s);
@@ -168,6 +171,30 @@ ASETS_API asets_status asets_solver_get_flows(asets_solver *s, asets_memory wher
  * launch stream, and the number of kernel launches it made. */
 ASETS_API asets_status asets_solver_last_run_stats(asets_solver *s, float *ms,
                                                    int *kernel_launches);
+
+/* ------------------------------------------------------------------------
+ * Batches: many independent binary problems (2D and 3D, any sizes) solved
+ * together.  Each iteration is one persistent launch per dimension over the
+ * work items of all problems that have not converged; every problem keeps
+ * the reference's own stopping rule, erriter and itNum, exactly as if solved
+ * alone.  Iteration chunks run as CUDA graphs.  No counterpart in the
+ * reference (which solves one problem per call).
+ * ---------------------------------------------------------------------- */
+typedef struct asets_batch asets_batch;
+
+ASETS_API asets_status asets_batch_create(asets_context *ctx, asets_batch **out);
+ASETS_API void asets_batch_destroy(asets_batch *b);
+/* Add a binary solver whose inputs are set; the batch does not own it. */
+ASETS_API asets_status asets_batch_add(asets_batch *b, asets_solver *s);
+/* Solve every member; itNums (optional) receives one itNum per member in
+ * the order they were added.  Results are read from each solver
+ * (asets_solver_get_u / _get_cvg). */
+ASETS_API asets_status asets_batch_run(asets_batch *b, const asets_options *opt, int maxIt,
+                                       float errBound, float cc, float steps, int *itNums);
+/* Device time of the last run, kernel launches, iterations summed over the
+ * members, and the tile configuration used for the 2D and 3D groups. */
+ASETS_API asets_status asets_batch_last_run_stats(asets_batch *b, float *ms, int *kernel_launches,
+                                                  int *iterations, int *tile_configs);
 
 /* ------------------------------------------------------------------------
  * Allocation-free binary 3D solve.  No counterpart in the reference: it

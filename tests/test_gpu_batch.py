@@ -1,0 +1,90 @@
+"""Batched solver: every member must come out exactly as when solved alone
+(same itNum, bit-identical u in EXACT mode, erriter up to summation order),
+while problems of different sizes and dimensions converge at different
+iterations inside one batch."""
+import numpy as np
+import pytest
+
+from tests.gpu_helpers import bits, require_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _gpu():
+    require_gpu()
+
+
+def _problems():
+    from asetsmatlabmaxflow_gb300 import synth
+
+    out = []
+    g = np.random.default_rng(5)
+    for i, shape in enumerate([(131, 77), (64, 200), (250, 256), (40, 33)]):
+        cs, ct, _ = synth.binary2d(seed=40 + i, shape=shape)
+        alpha = np.full(shape, g.uniform(0.2, 0.8), np.float32, order="F")
+        out.append((shape, cs, ct, alpha))
+    for i, shape in enumerate([(64, 70, 66), (90, 64, 75), (33, 41, 29)]):
+        cs, ct, _ = synth.binary3d(seed=60 + i, shape=shape, ncells=10)
+        alpha = np.full(shape, g.uniform(0.2, 0.8), np.float32, order="F")
+        out.append((shape, cs, ct, alpha))
+    return out
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_batch_members_equal_individual_solves(exact):
+    from asetsmatlabmaxflow_gb300 import native as N
+
+    ctx = N.Context.default()
+    probs = _problems()
+    max_it, err_bound = 400, 1e-4
+    solvers = []
+    ref = []
+    for shape, cs, ct, alpha in probs:
+        s = N.Solver(ctx, "binary", shape)
+        s.set_inputs(ct, alpha, cs)
+        cc, steps = (0.3, 0.16) if len(shape) == 2 else (0.35, 0.11)
+        it = s.run(max_it, err_bound, 0.3, 0.11, exact=exact)
+        ref.append((it, s.get_u().copy(), s.get_cvg()[:it + 1].copy()))
+        solvers.append(s)
+    b = N.Batch(ctx)
+    for s in solvers:
+        b.add(s)
+    its = b.run(max_it, err_bound, 0.3, 0.11, exact=exact)
+    assert len(set(its)) > 1  # members converge at different iterations
+    for s, it, (it_ref, u_ref, cvg_ref) in zip(solvers, its, ref):
+        assert it == it_ref
+        u = s.get_u()
+        if exact:
+            np.testing.assert_array_equal(bits(u), bits(u_ref))
+        else:
+            assert float(np.max(np.abs(u - u_ref))) <= 1e-5
+        np.testing.assert_allclose(s.get_cvg()[:it + 1], cvg_ref, rtol=1e-5)
+    st = b.last_run_stats()
+    assert st["iterations"] == sum(min(i + 1, max_it) for i in its)
+    b.close()
+    for s in solvers:
+        s.close()
+
+
+def test_batch_autotune_and_repeat_are_deterministic():
+    from asetsmatlabmaxflow_gb300 import native as N
+
+    ctx = N.Context.default()
+    solvers = []
+    for shape, cs, ct, alpha in _problems()[:5]:
+        s = N.Solver(ctx, "binary", shape)
+        s.set_inputs(ct, alpha, cs)
+        solvers.append(s)
+    b = N.Batch(ctx)
+    for s in solvers:
+        b.add(s)
+    its1 = b.run(150, 1e-4, 0.3, 0.11, autotune=True)
+    u1 = [s.get_u().copy() for s in solvers]
+    st = b.last_run_stats()
+    assert st["tile_config_2d"] >= 1 and st["tile_config_3d"] >= 1
+    its2 = b.run(150, 1e-4, 0.3, 0.11, autotune=True)  # cached choice
+    assert its1 == its2
+    for s, u in zip(solvers, u1):
+        np.testing.assert_array_equal(bits(s.get_u()), bits(u))
+    b.close()
