@@ -126,3 +126,23 @@ def potts_warmstart(seed: int, shape=(128, 128, 128), L=6):
         ct[..., l] = np.abs(img - np.float32(means[l]))
     a = np.full(shape + (L,), alpha, dtype=np.float32, order="F")
     return ct, a
+
+
+def batch_problems(seed: int = 0, n2d: int = 48, n3d: int = 16):
+    """Heterogeneous binary batch: n2d 2D problems with sides drawn from
+    128..1024 (independently per axis) and n3d 3D volumes with sides from
+    64..160, built like binary2d/binary3d with per-problem seeds, alpha a
+    constant drawn from U[0.2, 0.8].  Returns [(Cs, Ct, alpha), ...]."""
+    g = rng(seed)
+    out = []
+    for i in range(n2d):
+        shape = (int(g.integers(128, 1025)), int(g.integers(128, 1025)))
+        cs, ct, _ = binary2d(seed=1000 * (seed + 1) + i, shape=shape)
+        a = np.full(shape, g.uniform(0.2, 0.8), np.float32, order="F")
+        out.append((cs, ct, a))
+    for i in range(n3d):
+        shape = tuple(int(v) for v in g.integers(64, 161, size=3))
+        cs, ct, _ = binary3d(seed=2000 * (seed + 1) + i, shape=shape, ncells=40)
+        a = np.full(shape, g.uniform(0.2, 0.8), np.float32, order="F")
+        out.append((cs, ct, a))
+    return out

@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-solver measurement")
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="run one solve of N iterations of the workload and exit (for ncu)")
     ap.add_argument("--shape", default="256,256,256", help="volume for --profile-iters")
@@ -176,6 +177,40 @@ def traffic_per_launch():
     return None
 
 
+def batch_run(ctx) -> dict:
+    """Batched workload: 48 binary 2D (sides 128..1024) + 16 binary 3D (sides
+    64..160) problems, alpha ~ U[0.2, 0.8], errBound 1e-4, one persistent
+    launch per dimension and iteration, autotuned tile variant."""
+    from asetsmatlabmaxflow_gb300 import native as N
+    from asetsmatlabmaxflow_gb300 import synth
+
+    probs = synth.batch_problems(seed=0)
+    solvers = []
+    for cs, ct, alpha in probs:
+        s = N.Solver(ctx, "binary", cs.shape)
+        s.set_inputs(ct, alpha, cs)
+        solvers.append(s)
+    b = N.Batch(ctx)
+    for s in solvers:
+        b.add(s)
+    cc_, steps_ = 0.3, 0.16
+    b.run(2000, 1e-4, cc_, steps_, autotune=True)  # tune + warm-up
+    its = b.run(2000, 1e-4, cc_, steps_, autotune=True)
+    st = b.last_run_stats()
+    vox = sum(float(np.prod(p[0].shape)) * (i + 1) for p, i in zip(probs, its))
+    out = {"workload": "48 binary 2D (128..1024 per side) + 16 binary 3D (64..160 per side), "
+                       "errBound 1e-4, cc 0.3, steps 0.16",
+           "problems": len(probs), "ms_to_errbound_all": st["ms"],
+           "iterations_summed": st["iterations"], "max_iterations": max(its) + 1,
+           "gvoxel_iter_per_s": vox / (st["ms"] * 1e-3) / 1e9,
+           "tile_config_2d": st["tile_config_2d"], "tile_config_3d": st["tile_config_3d"],
+           "launches": st["launches"]}
+    b.close()
+    for s in solvers:
+        s.close()
+    return out
+
+
 def cpu_baseline_sample(cs, ct, alpha, iters: int) -> dict:
     """Single-core oracle solve of the same volume for `iters` iterations
     (init included, as the reference's timet)."""
@@ -266,8 +301,8 @@ def main():
         for _ in range(args.steps):
             it = s.run(ITERS, 0.0, CC, STEPS)
             ms, nl = s.last_run_stats()
-            kernel_ms.append(ms / nl)
-            launches += nl + 1  # iteration launches + the init kernel
+            kernel_ms.append(ms / ITERS)  # device time per executed iteration launch
+            launches += nl + 1  # iteration launches (graph chunks) + the init kernel
         ev1.record(stream)
         torch.cuda.synchronize()
     barrier(pg)
@@ -316,6 +351,8 @@ def main():
     e2e_value = world * nvox * ITERS * args.steps / e2e_s / 1e9
     ok = bool(np.isfinite(h_u.numpy()).all())
 
+    batch = None if args.no_batch else batch_run(ctx)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(cs, ct, alpha, 8)
@@ -341,6 +378,7 @@ def main():
             "time_to_errbound": {"err_bound": 1e-4, "iterations": conv_it, "ms": conv_ms},
             "clocks": clk.summary(),
             "gpu_launches": launches,
+            "batch": batch,
             "finite": ok,
         }
         if cpu is not None:
