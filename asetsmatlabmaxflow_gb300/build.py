@@ -43,6 +43,8 @@ CU_SOURCES = (
     "label_kernels.cu",
     "batch.cu",
     "noalloc.cu",
+    "conv_tc.cu",
+    "warmstart.cu",
 )
 
 MEX_SOLVERS = (

@@ -1,0 +1,236 @@
+// 3x3x3 convolutions of the learned warm start on the 5th-generation tensor
+// cores (tcgen05): BF16 activations and weights, FP32 accumulation in TMEM.
+//
+// Activations are channels-last, 16 channels of BF16 per voxel
+// ([z][x][y][16]).  A convolution is an implicit GEMM: an output tile is 128
+// consecutive voxels along y at one (x, z) (M = 128), each of the 27 taps is
+// one MMA with K = 16 input channels and N = 16 output channels, and the
+// accumulator (128 x 16 FP32) lives in TMEM.  One 5D TMA load per tile stages
+// the 3 x 3 neighbouring rows, y-1 .. y+128, zero-filled outside the volume
+// (the convolution's zero padding), as [row][channel half][voxel][8 channels]:
+// the no-swizzle K-major layout in which a tap's A operand is a plain offset.
+//
+// The same kernel computes the data gradient: with `flip` the taps are
+// mirrored and the weight matrix transposed.
+#include <cuda_bf16.h>
+
+#include <cstring>
+
+#include "internal.h"
+#include "tcgen05.cuh"
+
+namespace asets {
+
+constexpr int kConvThreads = 128;            // 4 warps: TMEM lanes 0..127
+constexpr int kConvRows = 9;                 // (dz, dx) neighbour rows
+constexpr int kConvVox = 130;                // y-1 .. y+128
+constexpr int kConvHalfBytes = kConvVox * 16;           // 8 channels x 2 B per voxel
+constexpr int kConvRowBytes = 2 * kConvHalfBytes;       // both channel halves
+constexpr int kConvStageBytes = kConvRows * kConvRowBytes;   // 37,440 B delivered by TMA
+constexpr int kConvStageStride = (kConvStageBytes + 127) / 128 * 128;
+constexpr int kConvTapBytes = 2 * 16 * 16;              // B operand of one tap
+constexpr int kConvWBytes = 27 * kConvTapBytes;         // 13,824 B
+// + 32 KB: operand descriptors can only address inside the allocation
+constexpr int kConvSmem = 2 * kConvStageStride + kConvWBytes + 128 + 32768;
+
+struct ConvTcArgs {
+    CUtensorMap act;           // 5D view (8 ch, y, half, x, z) of the BF16 input
+    const __nv_bfloat16 *w;    // [27][16 in][16 out]
+    const float *bias;         // [16] or null
+    const __nv_bfloat16 *mask; // [v][16] or null: output *= (mask > 0)
+    void *out;                 // [v][16] BF16 or FP32
+    int *err;
+    int ny, nx, nz, ytiles;
+    int relu, out_fp32, flip;
+};
+
+__global__ void __launch_bounds__(kConvThreads, 1) conv3_tc_kernel(const __grid_constant__ ConvTcArgs A)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ uint64_t full_bar[2], mma_bar[2];
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_abort;
+    unsigned char *smem = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
+    unsigned char *stage[2] = {smem, smem + kConvStageStride};
+    unsigned char *wsm = smem + 2 * kConvStageStride;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) {
+        s_abort = 0;
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&full_bar[i], 1);
+            mbar_init(&mma_bar[i], 1);
+        }
+        mbar_fence_init();
+    }
+    if (warp == 0)
+        tmem_alloc(&s_tmem, 32);  // two 16-column FP32 accumulators
+
+    // B operands: tap t as [k half][n][8 k] (core matrices of 8 n x 8 k)
+    for (int i = tid; i < 27 * 16 * 16; i += kConvThreads) {
+        const int t = i / 256, k = (i / 16) % 16, n = i % 16;
+        const __nv_bfloat16 v = A.flip ? A.w[(26 - t) * 256 + n * 16 + k] : A.w[t * 256 + k * 16 + n];
+        const int off = t * kConvTapBytes + (k / 8) * 256 + n * 16 + (k % 8) * 2;
+        *reinterpret_cast<__nv_bfloat16 *>(wsm + off) = v;
+    }
+    fence_proxy_async_smem();
+    tc_fence_before_sync();
+    __syncthreads();
+    tc_fence_after_sync();
+    const uint32_t tmem = s_tmem;
+
+    float bias[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c)
+        bias[c] = A.bias ? __ldg(A.bias + c) : 0.f;
+
+    const int ntiles = A.ytiles * A.nx * A.nz;
+    const uint32_t idesc = umma_idesc_bf16_f32(128, 16);
+    auto issue = [&](int tile, int st) {
+        const int yt = tile % A.ytiles, rest = tile / A.ytiles;
+        const int x = rest % A.nx, z = rest / A.nx;
+        mbar_arrive_expect_tx(&full_bar[st], kConvStageBytes);
+        tma_load_5d(stage[st], &A.act, 0, yt * 128 - 1, 0, x - 1, z - 1, &full_bar[st]);
+    };
+    if (tid == 0) {
+        if ((int)blockIdx.x < ntiles)
+            issue(blockIdx.x, 0);
+        if ((int)(blockIdx.x + gridDim.x) < ntiles)
+            issue(blockIdx.x + gridDim.x, 1);
+    }
+
+    int j = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++j) {
+        const int st = j & 1;
+        const uint32_t ph = (j >> 1) & 1;
+        bool ok = true;
+        if (tid == 0) {
+            ok = mbar_wait_bounded(&full_bar[st], ph, &s_abort);
+            if (ok) {
+                tc_fence_after_sync();
+                const uint32_t a0 = smem_addr(stage[st]);
+                const uint32_t b0 = smem_addr(wsm);
+                for (int t = 0; t < 27; ++t) {
+                    const int dz = t / 9, dx = (t / 3) % 3, dy = t % 3;
+                    const uint32_t a = a0 + (dz * 3 + dx) * kConvRowBytes + dy * 16;
+                    const uint64_t ad = umma_smem_desc(a, kConvHalfBytes, 128);
+                    const uint64_t bd = umma_smem_desc(b0 + t * kConvTapBytes, 256, 128);
+                    umma_bf16(tmem + st * 16, ad, bd, idesc, t > 0 ? 1u : 0u);
+                }
+                umma_commit(&mma_bar[st]);
+                ok = mbar_wait_bounded(&mma_bar[st], ph, &s_abort);
+            }
+        }
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0)
+                atomicOr(A.err, 1);
+            break;
+        }
+        tc_fence_after_sync();
+        float acc[16];
+        tmem_load16(tmem + ((uint32_t)(32 * warp) << 16) + st * 16, acc);
+        const int yt = tile % A.ytiles, rest = tile / A.ytiles;
+        const int x = rest % A.nx, z = rest / A.nx;
+        const int y = yt * 128 + 32 * warp + lane;
+        if (y < A.ny) {
+            const long long v = ((long long)z * A.nx + x) * A.ny + y;
+            float o[16];
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+                float s = acc[c] + bias[c];
+                if (A.relu)
+                    s = fmaxf(s, 0.f);
+                o[c] = s;
+            }
+            if (A.mask) {
+                const uint4 *mp = reinterpret_cast<const uint4 *>(A.mask + v * 16);
+                const uint4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
+                const __nv_bfloat16 *mb0 = reinterpret_cast<const __nv_bfloat16 *>(&m0);
+                const __nv_bfloat16 *mb1 = reinterpret_cast<const __nv_bfloat16 *>(&m1);
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    if (!(__bfloat162float(mb0[c]) > 0.f))
+                        o[c] = 0.f;
+                    if (!(__bfloat162float(mb1[c]) > 0.f))
+                        o[8 + c] = 0.f;
+                }
+            }
+            if (A.out_fp32) {
+                float4 *op = reinterpret_cast<float4 *>(static_cast<float *>(A.out) + v * 16);
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    op[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+            } else {
+                __align__(16) __nv_bfloat16 ob[16];
+#pragma unroll
+                for (int c = 0; c < 16; ++c)
+                    ob[c] = __float2bfloat16_rn(o[c]);
+                uint4 *op = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(A.out) + v * 16);
+                op[0] = reinterpret_cast<const uint4 *>(ob)[0];
+                op[1] = reinterpret_cast<const uint4 *>(ob)[1];
+            }
+        }
+        tc_fence_before_sync();
+        __syncthreads();  // stage st and accumulator st are free again
+        if (tid == 0 && tile + 2 * (int)gridDim.x < ntiles)
+            issue(tile + 2 * gridDim.x, st);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        // drain copies still in flight after an early exit (bounded)
+        s_abort = 0;
+        for (int i = 0; i < 2; ++i) {
+            const int jj = j + i;
+            const int t2 = blockIdx.x + jj * gridDim.x;
+            if (t2 < ntiles && jj >= 0)
+                mbar_wait_bounded(&full_bar[jj & 1], (jj >> 1) & 1, &s_abort);
+        }
+    }
+    __syncthreads();
+    tc_fence_after_sync();
+    if (warp == 0)
+        tmem_dealloc(tmem, 32);
+}
+
+int conv_smem_bytes() { return kConvSmem; }
+
+cudaError_t launch_conv3_tc(EncodeTiledFn encode, const ConvLaunch &c, int num_sms,
+                            cudaStream_t st, int *d_err)
+{
+    ConvTcArgs A;
+    memset(&A, 0, sizeof A);
+    // channels-last [z][x][y][16] BF16 seen as (8 ch, y, half, x, z)
+    cuuint64_t dims[5] = {8, (cuuint64_t)c.ny, 2, (cuuint64_t)c.nx, (cuuint64_t)c.nz};
+    cuuint64_t strides[4] = {32, 16, (cuuint64_t)32 * c.ny, (cuuint64_t)32 * c.ny * c.nx};
+    cuuint32_t box[5] = {8, kConvVox, 2, 3, 3};
+    cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    CUresult r = encode(&A.act, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(c.x), dims,
+                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    A.w = static_cast<const __nv_bfloat16 *>(c.w);
+    A.bias = c.bias;
+    A.mask = static_cast<const __nv_bfloat16 *>(c.mask);
+    A.out = c.y;
+    A.err = d_err;
+    A.ny = c.ny;
+    A.nx = c.nx;
+    A.nz = c.nz;
+    A.ytiles = (c.ny + 127) / 128;
+    A.relu = c.relu;
+    A.out_fp32 = c.out_fp32;
+    A.flip = c.flip;
+    cudaError_t e = cudaFuncSetAttribute(conv3_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kConvSmem);
+    if (e != cudaSuccess)
+        return e;
+    const int tiles = A.ytiles * c.nx * c.nz;
+    const int grid = tiles < num_sms ? tiles : num_sms;
+    conv3_tc_kernel<<<grid, kConvThreads, kConvSmem, st>>>(A);
+    return cudaGetLastError();
+}
+
+}  // namespace asets

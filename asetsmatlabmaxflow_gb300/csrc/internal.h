@@ -7,6 +7,8 @@
 
 #include "kernel_args.h"
 
+struct asets_context;
+
 namespace asets {
 
 // ---------------------------------------------------------------- stencil
@@ -96,5 +98,26 @@ cudaError_t launch_validate_alpha(const InitArgs &a, int num_sms, cudaStream_t s
 
 // Message returned by asets_last_error() on the calling thread.
 void set_last_error(const char *msg);
+
+// ---------------------------------------------------------------- context
+EncodeTiledFn context_encoder(asets_context *ctx);
+int context_num_sms(asets_context *ctx);
+int context_device(asets_context *ctx);
+cudaStream_t context_stream(asets_context *ctx);
+
+// ---------------------------------------------------------------- warm-start net
+// One 3x3x3 convolution, 16 -> 16 channels (conv_tc.cu).
+struct ConvLaunch {
+    const void *x;       // BF16 [z][x][y][16]
+    const void *w;       // BF16 [27][16 in][16 out], tap = (dz*3 + dx)*3 + dy
+    const float *bias;   // [16] or null
+    const void *mask;    // BF16 [v][16] or null: output *= (mask > 0)
+    void *y;             // BF16 or FP32 [v][16]
+    int ny, nx, nz;
+    int relu, out_fp32, flip;
+};
+cudaError_t launch_conv3_tc(EncodeTiledFn encode, const ConvLaunch &c, int num_sms,
+                            cudaStream_t st, int *d_err);
+int conv_smem_bytes();
 
 }  // namespace asets

@@ -153,6 +153,13 @@ static asets_status get_encoder(asets_context *ctx)
     return ASETS_OK;
 }
 
+namespace asets {
+EncodeTiledFn context_encoder(asets_context *ctx) { return ctx->encode; }
+int context_num_sms(asets_context *ctx) { return ctx->num_sms; }
+int context_device(asets_context *ctx) { return ctx->device; }
+cudaStream_t context_stream(asets_context *ctx) { return ctx->stream; }
+}  // namespace asets
+
 extern "C" ASETS_API int asets_abi_version(void) { return ASETS_ABI_VERSION; }
 
 extern "C" ASETS_API const char *asets_status_string(asets_status s)

@@ -197,6 +197,22 @@ ASETS_API asets_status asets_batch_last_run_stats(asets_batch *b, float *ms, int
                                                   int *iterations, int *tile_configs);
 
 /* ------------------------------------------------------------------------
+ * Learned warm start building block (no counterpart in the reference):
+ * one 3x3x3 convolution with 16 input and 16 output channels on the tensor
+ * cores, BF16 operands and FP32 accumulation, zero padding at the volume
+ * border.  x: device BF16 [Nz][Nx][Ny][16] (16-byte aligned); w: device BF16
+ * [27][16 in][16 out], tap = (dz*3 + dx)*3 + dy for offsets dz,dx,dy in
+ * -1..1; bias: device float[16] or NULL; mask: device BF16 like x or NULL
+ * (output channel c of voxel v kept only where mask[v][c] > 0); y: device
+ * BF16 or (out_fp32) float [..][16].  relu applies max(0, .).  With flip the
+ * transposed convolution is computed (taps mirrored, w[t] transposed): the
+ * gradient with respect to the input.
+ * ---------------------------------------------------------------------- */
+ASETS_API asets_status asets_conv3d_bf16(asets_context *ctx, const void *x, const void *w,
+                                         const float *bias, const void *mask, void *y, int Ny,
+                                         int Nx, int Nz, int relu, int out_fp32, int flip);
+
+/* ------------------------------------------------------------------------
  * Allocation-free binary 3D solve.  No counterpart in the reference: it
  * exists for callers that cannot allocate device memory while they run -- a
  * host whose GPU memory is owned by another allocator (a framework's caching
