@@ -81,3 +81,477 @@ extern "C" ASETS_API asets_status asets_conv3d_bf16(asets_context *ctx, const vo
     cudaSetDevice(prev);
     return st;
 }
+
+// ===================================================================== net
+// Four 3x3x3 convolutions, 16 channels, ReLU between them:
+//   input  (Ct_1..Ct_L, alpha)            channels 0..L
+//   output (u_1..u_L, ps, pt_1..pt_L)     channels 0..2L
+// Weights are kept in FP32 (Adam master copy) and used as BF16.
+namespace {
+
+constexpr int kLayers = 4;
+constexpr int kW = 27 * 16 * 16;  // weights of one layer
+constexpr int kParams = kLayers * (kW + 16);
+
+__global__ void pack_input_kernel(const float *ct, const float *alpha, __nv_bfloat16 *x,
+                                  long long n, int L)
+{
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x) {
+        __align__(16) __nv_bfloat16 v[16];
+        for (int c = 0; c < 16; ++c) {
+            float f = 0.f;
+            if (c < L)
+                f = ct[c * n + g];
+            else if (c == L)
+                f = alpha[g];
+            v[c] = __float2bfloat16_rn(f);
+        }
+        uint4 *o = reinterpret_cast<uint4 *>(x + g * 16);
+        o[0] = reinterpret_cast<const uint4 *>(v)[0];
+        o[1] = reinterpret_cast<const uint4 *>(v)[1];
+    }
+}
+
+__global__ void pack_target_kernel(const float *u, const float *ps, const float *pt, float *t,
+                                   long long n, int L)
+{
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x) {
+        float *o = t + g * 16;
+        for (int c = 0; c < 16; ++c) {
+            float f = 0.f;
+            if (c < L)
+                f = u[c * n + g];
+            else if (c == L)
+                f = ps[g];
+            else if (c <= 2 * L)
+                f = pt[(c - L - 1) * n + g];
+            o[c] = f;
+        }
+    }
+}
+
+__global__ void unpack_output_kernel(const float *out, float *u, float *ps, float *pt, long long n,
+                                     int L)
+{
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x) {
+        const float *o = out + g * 16;
+        for (int l = 0; l < L; ++l) {
+            u[l * n + g] = fminf(fmaxf(o[l], 0.f), 1.f);  // a labelling lies in [0, 1]
+            pt[l * n + g] = o[L + 1 + l];
+        }
+        ps[g] = o[L];
+    }
+}
+
+// Mean squared error over the 2L+1 used output channels; writes the
+// gradient w.r.t. the output (BF16) and accumulates the loss.
+__global__ void loss_kernel(const float *out, const float *tgt, __nv_bfloat16 *g, long long n,
+                            int used, float scale, float *loss)
+{
+    float acc = 0.f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n * 16;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(i & 15);
+        float d = 0.f;
+        if (c < used) {
+            d = out[i] - tgt[i];
+            acc += d * d;
+        }
+        g[i] = __float2bfloat16_rn(2.f * d * scale);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0)
+        atomicAdd(loss, acc * scale);
+}
+
+// dW[t][ci][co] += sum_v a[v + off_t][ci] * g[v][co], bias grad sum_v g[v][co].
+// One block per SM walks 128-voxel rows; thread (t, ci) keeps its 16 outputs
+// in registers across rows.
+constexpr int kWgThreads = 448;  // 432 (tap, channel) pairs + 16 bias lanes
+constexpr int kWgSmem = (9 * 130 * 16 + 128 * 16) * 4;
+__global__ void __launch_bounds__(kWgThreads, 1)
+    wgrad_kernel(const __nv_bfloat16 *a, const __nv_bfloat16 *g, float *dw, float *db, int ny,
+                 int nx, int nz)
+{
+    extern __shared__ float wg_smem[];
+    float(*sa)[130][16] = reinterpret_cast<float(*)[130][16]>(wg_smem);           // [9][130][16]
+    float(*sg)[16] = reinterpret_cast<float(*)[16]>(wg_smem + 9 * 130 * 16);      // [128][16]
+    const int tid = threadIdx.x;
+    const int t = tid / 16, ci = tid % 16;  // valid for tid < 432
+    const int dz = t / 9, dx = (t / 3) % 3, dy = t % 3;
+    float acc[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c)
+        acc[c] = 0.f;
+    const int ytiles = (ny + 127) / 128;
+    const int ntiles = ytiles * nx * nz;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int yt = tile % ytiles, rest = tile / ytiles;
+        const int x = rest % nx, z = rest / nx;
+        const int y0 = yt * 128;
+        __syncthreads();
+        for (int i = tid; i < 9 * 130 * 16; i += kWgThreads) {
+            const int c = i % 16, vy = (i / 16) % 130, row = i / (16 * 130);
+            const int zz = z + row / 3 - 1, xx = x + row % 3 - 1, yy = y0 + vy - 1;
+            float f = 0.f;
+            if (zz >= 0 && zz < nz && xx >= 0 && xx < nx && yy >= 0 && yy < ny)
+                f = __bfloat162float(a[(((long long)zz * nx + xx) * ny + yy) * 16 + c]);
+            sa[row][vy][c] = f;
+        }
+        for (int i = tid; i < 128 * 16; i += kWgThreads) {
+            const int c = i % 16, vy = i / 16, yy = y0 + vy;
+            sg[vy][c] = (yy < ny) ? __bfloat162float(g[(((long long)z * nx + x) * ny + yy) * 16 + c])
+                                  : 0.f;
+        }
+        __syncthreads();
+        if (tid < 432) {
+            const int row = dz * 3 + dx;
+            for (int v = 0; v < 128; ++v) {
+                const float av = sa[row][v + dy][ci];
+#pragma unroll
+                for (int c = 0; c < 16; ++c)
+                    acc[c] = fmaf(av, sg[v][c], acc[c]);
+            }
+        } else {
+            const int c = tid - 432;  // bias lanes
+            float s = 0.f;
+            for (int v = 0; v < 128; ++v)
+                s += sg[v][c];
+            acc[0] += s;
+        }
+    }
+    if (tid < 432) {
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+            atomicAdd(&dw[(t * 16 + ci) * 16 + c], acc[c]);
+    } else {
+        atomicAdd(&db[tid - 432], acc[0]);
+    }
+}
+
+// Adam on the FP32 master parameters; refreshes the BF16 weight copies and
+// clears the gradients.
+__global__ void adam_kernel(float *p, float *m, float *v, float *grad, __nv_bfloat16 *w16,
+                            int n, int nw_per_layer, float lr, float b1, float b2, float eps,
+                            float c1, float c2)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float gi = grad[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        grad[i] = 0.f;
+    }
+}
+
+__global__ void to_bf16_kernel(const float *p, __nv_bfloat16 *w16, int layers)
+{
+    // parameter block per layer: kW weights then 16 biases
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < layers * kW;
+         i += gridDim.x * blockDim.x) {
+        const int l = i / kW, j = i % kW;
+        w16[i] = __float2bfloat16_rn(p[l * (kW + 16) + j]);
+    }
+}
+
+int blocks_for(long long n, int threads, int num_sms)
+{
+    long long b = (n + threads - 1) / threads;
+    long long cap = (long long)num_sms * 8;
+    return (int)(b < 1 ? 1 : (b < cap ? b : cap));
+}
+
+}  // namespace
+
+struct asets_wsnet {
+    asets_context *ctx = nullptr;
+    int L = 6;
+    float *params = nullptr, *grads = nullptr, *m = nullptr, *v = nullptr;
+    __nv_bfloat16 *w16 = nullptr;
+    float *loss = nullptr;
+    int *err = nullptr;
+    long long vox_cap = 0;
+    __nv_bfloat16 *x0 = nullptr, *act[3] = {nullptr, nullptr, nullptr};
+    __nv_bfloat16 *gbuf[2] = {nullptr, nullptr};
+    float *out = nullptr, *tgt = nullptr;
+    int step = 0;
+};
+
+static asets_status ws_reserve(asets_wsnet *n, long long vox)
+{
+    if (vox <= n->vox_cap)
+        return ASETS_OK;
+    cudaStream_t st = context_stream(n->ctx);
+    auto fr = [&](void *p) {
+        if (p)
+            cudaFreeAsync(p, st);
+    };
+    fr(n->x0);
+    for (auto *p : n->act)
+        fr(p);
+    for (auto *p : n->gbuf)
+        fr(p);
+    fr(n->out);
+    fr(n->tgt);
+    const size_t b16 = (size_t)vox * 16 * sizeof(__nv_bfloat16), f32 = (size_t)vox * 16 * 4;
+    WS_TRY(cudaMallocAsync((void **)&n->x0, b16, st));
+    for (auto &p : n->act)
+        WS_TRY(cudaMallocAsync((void **)&p, b16, st));
+    for (auto &p : n->gbuf)
+        WS_TRY(cudaMallocAsync((void **)&p, b16, st));
+    WS_TRY(cudaMallocAsync((void **)&n->out, f32, st));
+    WS_TRY(cudaMallocAsync((void **)&n->tgt, f32, st));
+    n->vox_cap = vox;
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API int asets_wsnet_num_params(void) { return kParams; }
+
+extern "C" ASETS_API asets_status asets_wsnet_create(asets_context *ctx, int nLab,
+                                                     unsigned long long seed, asets_wsnet **out)
+{
+    if (!ctx || !out || nLab < 1 || 2 * nLab + 1 > 16)
+        return ws_fail(ASETS_ERR_INVALID_ARG, "warm-start net needs 1 <= nLab <= 7");
+    *out = nullptr;
+    cudaSetDevice(context_device(ctx));
+    asets_wsnet *n = new asets_wsnet;
+    n->ctx = ctx;
+    n->L = nLab;
+    cudaStream_t st = context_stream(ctx);
+    WS_TRY(cudaMallocAsync((void **)&n->params, kParams * 4, st));
+    WS_TRY(cudaMallocAsync((void **)&n->grads, kParams * 4, st));
+    WS_TRY(cudaMallocAsync((void **)&n->m, kParams * 4, st));
+    WS_TRY(cudaMallocAsync((void **)&n->v, kParams * 4, st));
+    WS_TRY(cudaMallocAsync((void **)&n->w16, kLayers * kW * 2, st));
+    WS_TRY(cudaMallocAsync((void **)&n->loss, 4, st));
+    WS_TRY(cudaMallocAsync((void **)&n->err, 4, st));
+    WS_TRY(cudaFuncSetAttribute(wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kWgSmem));
+    // He-normal initial weights from a seeded generator (Box-Muller on a
+    // 64-bit LCG), zero biases; unused channels stay zero.
+    float *h = new float[kParams]();
+    unsigned long long s = seed * 6364136223846793005ull + 1442695040888963407ull;
+    auto uni = [&]() {
+        s = s * 6364136223846793005ull + 1442695040888963407ull;
+        return ((s >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    };
+    for (int l = 0; l < kLayers; ++l) {
+        const int cin = (l == 0) ? nLab + 1 : 16;
+        const int cout = (l == kLayers - 1) ? 2 * nLab + 1 : 16;
+        const double sd = sqrt(2.0 / (27.0 * cin));
+        for (int t = 0; t < 27; ++t)
+            for (int i = 0; i < cin; ++i)
+                for (int o = 0; o < cout; ++o) {
+                    const double r = sqrt(-2.0 * log(uni())) * cos(6.283185307179586 * uni());
+                    h[l * (kW + 16) + (t * 16 + i) * 16 + o] = (float)(sd * r);
+                }
+    }
+    WS_TRY(cudaMemcpyAsync(n->params, h, kParams * 4, cudaMemcpyHostToDevice, st));
+    WS_TRY(cudaStreamSynchronize(st));
+    delete[] h;
+    WS_TRY(cudaMemsetAsync(n->grads, 0, kParams * 4, st));
+    WS_TRY(cudaMemsetAsync(n->m, 0, kParams * 4, st));
+    WS_TRY(cudaMemsetAsync(n->v, 0, kParams * 4, st));
+    to_bf16_kernel<<<64, 256, 0, st>>>(n->params, n->w16, kLayers);
+    WS_TRY(cudaGetLastError());
+    WS_TRY(cudaStreamSynchronize(st));
+    *out = n;
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API void asets_wsnet_destroy(asets_wsnet *n)
+{
+    if (!n)
+        return;
+    cudaStream_t st = context_stream(n->ctx);
+    void *ps[] = {n->params, n->grads, n->m, n->v, n->w16, n->loss, n->err, n->x0, n->act[0],
+                  n->act[1], n->act[2], n->gbuf[0], n->gbuf[1], n->out, n->tgt};
+    for (void *p : ps)
+        if (p)
+            cudaFreeAsync(p, st);
+    cudaStreamSynchronize(st);
+    delete n;
+}
+
+extern "C" ASETS_API asets_status asets_wsnet_get_params(asets_wsnet *n, float *host)
+{
+    if (!n || !host)
+        return ws_fail(ASETS_ERR_INVALID_ARG, "NULL argument");
+    WS_TRY(cudaMemcpyAsync(host, n->params, kParams * 4, cudaMemcpyDeviceToHost, context_stream(n->ctx)));
+    WS_TRY(cudaStreamSynchronize(context_stream(n->ctx)));
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_wsnet_set_params(asets_wsnet *n, const float *host)
+{
+    if (!n || !host)
+        return ws_fail(ASETS_ERR_INVALID_ARG, "NULL argument");
+    cudaStream_t st = context_stream(n->ctx);
+    WS_TRY(cudaMemcpyAsync(n->params, host, kParams * 4, cudaMemcpyHostToDevice, st));
+    to_bf16_kernel<<<64, 256, 0, st>>>(n->params, n->w16, kLayers);
+    WS_TRY(cudaGetLastError());
+    WS_TRY(cudaStreamSynchronize(st));
+    n->step = 0;
+    WS_TRY(cudaMemsetAsync(n->m, 0, kParams * 4, st));
+    WS_TRY(cudaMemsetAsync(n->v, 0, kParams * 4, st));
+    return ASETS_OK;
+}
+
+// Forward pass: x0 -> act[0..2] -> out (FP32).
+static asets_status ws_forward(asets_wsnet *n, int Ny, int Nx, int Nz, const float *ct,
+                               const float *alpha)
+{
+    const long long vox = (long long)Ny * Nx * Nz;
+    asets_status s = ws_reserve(n, vox);
+    if (s != ASETS_OK)
+        return s;
+    cudaStream_t st = context_stream(n->ctx);
+    const int sms = context_num_sms(n->ctx);
+    pack_input_kernel<<<blocks_for(vox, 256, sms), 256, 0, st>>>(ct, alpha, n->x0, vox, n->L);
+    WS_TRY(cudaGetLastError());
+    WS_TRY(cudaMemsetAsync(n->err, 0, 4, st));
+    const void *in = n->x0;
+    for (int l = 0; l < kLayers; ++l) {
+        ConvLaunch c;
+        memset(&c, 0, sizeof c);
+        c.x = in;
+        c.w = n->w16 + l * kW;
+        c.bias = n->params + l * (kW + 16) + kW;
+        c.ny = Ny;
+        c.nx = Nx;
+        c.nz = Nz;
+        const bool last = (l == kLayers - 1);
+        c.y = last ? static_cast<void *>(n->out) : static_cast<void *>(n->act[l]);
+        c.relu = last ? 0 : 1;
+        c.out_fp32 = last ? 1 : 0;
+        WS_TRY(launch_conv3_tc(context_encoder(n->ctx), c, sms, st, n->err));
+        in = c.y;
+    }
+    return ASETS_OK;
+}
+
+static asets_status ws_check(asets_wsnet *n)
+{
+    int herr = 0;
+    WS_TRY(cudaMemcpyAsync(&herr, n->err, 4, cudaMemcpyDeviceToHost, context_stream(n->ctx)));
+    WS_TRY(cudaStreamSynchronize(context_stream(n->ctx)));
+    if (herr)
+        return ws_fail(ASETS_ERR_TIMEOUT, "a device-side wait timed out in the warm-start net");
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_wsnet_predict(asets_wsnet *n, int Ny, int Nx, int Nz,
+                                                      const float *Ct, const float *alpha,
+                                                      float *u0, float *ps0, float *pt0)
+{
+    if (!n || !Ct || !alpha || !u0 || !ps0 || !pt0 || Ny < 1 || Nx < 1 || Nz < 1)
+        return ws_fail(ASETS_ERR_INVALID_ARG, "bad arguments");
+    cudaSetDevice(context_device(n->ctx));
+    asets_status s = ws_forward(n, Ny, Nx, Nz, Ct, alpha);
+    if (s != ASETS_OK)
+        return s;
+    const long long vox = (long long)Ny * Nx * Nz;
+    cudaStream_t st = context_stream(n->ctx);
+    unpack_output_kernel<<<blocks_for(vox, 256, context_num_sms(n->ctx)), 256, 0, st>>>(
+        n->out, u0, ps0, pt0, vox, n->L);
+    WS_TRY(cudaGetLastError());
+    return ws_check(n);
+}
+
+// Forward + backward; gradients accumulate into n->grads.
+static asets_status ws_backward(asets_wsnet *n, int Ny, int Nx, int Nz, const float *ct,
+                                const float *alpha, const float *u, const float *ps,
+                                const float *pt, float *loss_out)
+{
+    asets_status s = ws_forward(n, Ny, Nx, Nz, ct, alpha);
+    if (s != ASETS_OK)
+        return s;
+    const long long vox = (long long)Ny * Nx * Nz;
+    cudaStream_t st = context_stream(n->ctx);
+    const int sms = context_num_sms(n->ctx);
+    pack_target_kernel<<<blocks_for(vox, 256, sms), 256, 0, st>>>(u, ps, pt, n->tgt, vox, n->L);
+    WS_TRY(cudaMemsetAsync(n->loss, 0, 4, st));
+    const int used = 2 * n->L + 1;
+    const float scale = 1.0f / (float)((double)vox * used);
+    loss_kernel<<<blocks_for(vox * 16, 256, sms), 256, 0, st>>>(n->out, n->tgt, n->gbuf[0], vox,
+                                                                used, scale, n->loss);
+    WS_TRY(cudaGetLastError());
+    // layer l's input activation and the gradient w.r.t. its output
+    const __nv_bfloat16 *ins[kLayers] = {n->x0, n->act[0], n->act[1], n->act[2]};
+    int cur = 0;
+    for (int l = kLayers - 1; l >= 0; --l) {
+        float *gw = n->grads + l * (kW + 16);
+        wgrad_kernel<<<sms, kWgThreads, kWgSmem, st>>>(ins[l], n->gbuf[cur], gw, gw + kW, Ny, Nx,
+                                                        Nz);
+        WS_TRY(cudaGetLastError());
+        if (l == 0)
+            break;
+        ConvLaunch c;
+        memset(&c, 0, sizeof c);
+        c.x = n->gbuf[cur];
+        c.w = n->w16 + l * kW;
+        c.mask = ins[l];  // ReLU of the previous layer: its output = this layer's input
+        c.y = n->gbuf[cur ^ 1];
+        c.ny = Ny;
+        c.nx = Nx;
+        c.nz = Nz;
+        c.flip = 1;
+        WS_TRY(launch_conv3_tc(context_encoder(n->ctx), c, sms, st, n->err));
+        cur ^= 1;
+    }
+    s = ws_check(n);
+    if (s != ASETS_OK)
+        return s;
+    if (loss_out) {
+        WS_TRY(cudaMemcpyAsync(loss_out, n->loss, 4, cudaMemcpyDeviceToHost, st));
+        WS_TRY(cudaStreamSynchronize(st));
+    }
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_wsnet_gradients(asets_wsnet *n, int Ny, int Nx, int Nz,
+                                                        const float *Ct, const float *alpha,
+                                                        const float *u, const float *ps,
+                                                        const float *pt, float *host_grads,
+                                                        float *loss)
+{
+    if (!n || !Ct || !alpha || !u || !ps || !pt || !host_grads)
+        return ws_fail(ASETS_ERR_INVALID_ARG, "bad arguments");
+    cudaSetDevice(context_device(n->ctx));
+    cudaStream_t st = context_stream(n->ctx);
+    WS_TRY(cudaMemsetAsync(n->grads, 0, kParams * 4, st));
+    asets_status s = ws_backward(n, Ny, Nx, Nz, Ct, alpha, u, ps, pt, loss);
+    if (s != ASETS_OK)
+        return s;
+    WS_TRY(cudaMemcpyAsync(host_grads, n->grads, kParams * 4, cudaMemcpyDeviceToHost, st));
+    WS_TRY(cudaMemsetAsync(n->grads, 0, kParams * 4, st));
+    WS_TRY(cudaStreamSynchronize(st));
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_wsnet_train_step(asets_wsnet *n, int Ny, int Nx, int Nz,
+                                                         const float *Ct, const float *alpha,
+                                                         const float *u, const float *ps,
+                                                         const float *pt, float lr, float *loss)
+{
+    if (!n || !Ct || !alpha || !u || !ps || !pt)
+        return ws_fail(ASETS_ERR_INVALID_ARG, "bad arguments");
+    cudaSetDevice(context_device(n->ctx));
+    asets_status s = ws_backward(n, Ny, Nx, Nz, Ct, alpha, u, ps, pt, loss);
+    if (s != ASETS_OK)
+        return s;
+    n->step += 1;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - powf(b1, (float)n->step), c2 = 1.f - powf(b2, (float)n->step);
+    cudaStream_t st = context_stream(n->ctx);
+    adam_kernel<<<64, 256, 0, st>>>(n->params, n->m, n->v, n->grads, n->w16, kParams, kW, lr, b1,
+                                    b2, 1e-8f, c1, c2);
+    to_bf16_kernel<<<64, 256, 0, st>>>(n->params, n->w16, kLayers);
+    WS_TRY(cudaGetLastError());
+    return ASETS_OK;
+}

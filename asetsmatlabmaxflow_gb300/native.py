@@ -103,6 +103,18 @@ _SIGS = {
                                                   ctypes.POINTER(ctypes.c_int), _VP]),
     "asets_conv3d_bf16": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int,
                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "asets_wsnet_num_params": (ctypes.c_int, []),
+    "asets_wsnet_create": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_ulonglong, ctypes.POINTER(_VP)]),
+    "asets_wsnet_destroy": (None, [_VP]),
+    "asets_wsnet_get_params": (ctypes.c_int, [_VP, _VP]),
+    "asets_wsnet_set_params": (ctypes.c_int, [_VP, _VP]),
+    "asets_wsnet_predict": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP,
+                                           _VP, _VP, _VP]),
+    "asets_wsnet_gradients": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP,
+                                             _VP, _VP, _VP, _VP, _VP, ctypes.POINTER(ctypes.c_float)]),
+    "asets_wsnet_train_step": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP,
+                                              _VP, _VP, _VP, _VP, ctypes.c_float,
+                                              ctypes.POINTER(ctypes.c_float)]),
     "asets_binary_mf3d_noalloc": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int,
                                                  ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                                  ctypes.c_float, ctypes.c_float, _VP, _VP,
@@ -320,6 +332,65 @@ class Batch:
     def close(self) -> None:
         if self._h:
             lib().asets_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class WarmStartNet:
+    """The learned warm start (asets_wsnet_*): a 4-layer 3x3x3 convolutional
+    net, (Ct_1..L, alpha) -> (u_1..L, ps, pt_1..L), on the tensor cores.
+    Array arguments are device pointers / CUDA tensors in Matlab layout
+    (label slowest)."""
+
+    def __init__(self, ctx: Context, nlab: int = 6, seed: int = 0):
+        self.ctx = ctx
+        self.nlab = nlab
+        h = _VP()
+        check(lib().asets_wsnet_create(ctx.handle, nlab, seed, ctypes.byref(h)))
+        self._h = h.value
+
+    @staticmethod
+    def num_params() -> int:
+        return lib().asets_wsnet_num_params()
+
+    def get_params(self) -> np.ndarray:
+        out = np.empty(self.num_params(), np.float32)
+        check(lib().asets_wsnet_get_params(self._h, out.ctypes.data))
+        return out
+
+    def set_params(self, p) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.num_params()
+        check(lib().asets_wsnet_set_params(self._h, p.ctypes.data))
+
+    def predict(self, dims, ct, alpha, u0, ps0, pt0) -> None:
+        ny, nx, nz = dims
+        check(lib().asets_wsnet_predict(self._h, ny, nx, nz, _ptr(ct), _ptr(alpha), _ptr(u0),
+                                        _ptr(ps0), _ptr(pt0)))
+
+    def gradients(self, dims, ct, alpha, u, ps, pt):
+        ny, nx, nz = dims
+        g = np.empty(self.num_params(), np.float32)
+        loss = ctypes.c_float(0)
+        check(lib().asets_wsnet_gradients(self._h, ny, nx, nz, _ptr(ct), _ptr(alpha), _ptr(u),
+                                          _ptr(ps), _ptr(pt), g.ctypes.data, ctypes.byref(loss)))
+        return loss.value, g
+
+    def train_step(self, dims, ct, alpha, u, ps, pt, lr: float) -> float:
+        ny, nx, nz = dims
+        loss = ctypes.c_float(0)
+        check(lib().asets_wsnet_train_step(self._h, ny, nx, nz, _ptr(ct), _ptr(alpha), _ptr(u),
+                                           _ptr(ps), _ptr(pt), lr, ctypes.byref(loss)))
+        return loss.value
+
+    def close(self) -> None:
+        if self._h:
+            lib().asets_wsnet_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -213,6 +213,40 @@ ASETS_API asets_status asets_conv3d_bf16(asets_context *ctx, const void *x, cons
                                          int Nx, int Nz, int relu, int out_fp32, int flip);
 
 /* ------------------------------------------------------------------------
+ * Learned warm start for the labelled models (no counterpart in the
+ * reference): a network of four 3x3x3 convolutions with 16 channels and ReLU
+ * maps (Ct_1..Ct_L, alpha) to an initial (u_1..u_L, ps, pt_1..pt_L) for
+ * asets_solver_set_initial.  Forward and input-gradient convolutions run on
+ * the tensor cores (BF16, FP32 accumulation), weight gradients in FP32;
+ * training is Adam on an MSE loss against solver solutions.  All arrays are
+ * device pointers in Matlab layout (label slowest); alpha is one slice.
+ * Parameters: 4 x (27*16*16 weights [tap][in][out] + 16 biases), float.
+ * ---------------------------------------------------------------------- */
+typedef struct asets_wsnet asets_wsnet;
+
+ASETS_API int asets_wsnet_num_params(void);
+/* nLab <= 7; weights He-initialised from `seed`. */
+ASETS_API asets_status asets_wsnet_create(asets_context *ctx, int nLab, unsigned long long seed,
+                                          asets_wsnet **out);
+ASETS_API void asets_wsnet_destroy(asets_wsnet *n);
+ASETS_API asets_status asets_wsnet_get_params(asets_wsnet *n, float *host_params);
+ASETS_API asets_status asets_wsnet_set_params(asets_wsnet *n, const float *host_params);
+/* u0 (N*L, clamped to [0,1]), ps0 (N), pt0 (N*L) for a Ny x Nx x Nz volume. */
+ASETS_API asets_status asets_wsnet_predict(asets_wsnet *n, int Ny, int Nx, int Nz,
+                                           const float *Ct, const float *alpha, float *u0,
+                                           float *ps0, float *pt0);
+/* Loss and parameter gradients (host) against a solution (u, ps, pt). */
+ASETS_API asets_status asets_wsnet_gradients(asets_wsnet *n, int Ny, int Nx, int Nz,
+                                             const float *Ct, const float *alpha, const float *u,
+                                             const float *ps, const float *pt, float *host_grads,
+                                             float *loss);
+/* One Adam step (learning rate lr) on one solved volume; returns the loss. */
+ASETS_API asets_status asets_wsnet_train_step(asets_wsnet *n, int Ny, int Nx, int Nz,
+                                              const float *Ct, const float *alpha,
+                                              const float *u, const float *ps, const float *pt,
+                                              float lr, float *loss);
+
+/* ------------------------------------------------------------------------
  * Allocation-free binary 3D solve.  No counterpart in the reference: it
  * exists for callers that cannot allocate device memory while they run -- a
  * host whose GPU memory is owned by another allocator (a framework's caching
