@@ -45,6 +45,7 @@ CU_SOURCES = (
     "noalloc.cu",
     "conv_tc.cu",
     "warmstart.cu",
+    "multilevel.cu",
 )
 
 MEX_SOLVERS = (

@@ -11,7 +11,9 @@
 // the no-swizzle K-major layout in which a tap's A operand is a plain offset.
 //
 // The same kernel computes the data gradient: with `flip` the taps are
-// mirrored and the weight matrix transposed.
+// mirrored and the weight matrix transposed.  The epilogue adds the bias and
+// an optional FP32 addend (a second convolution's result), then applies ReLU
+// and an optional mask (the ReLU derivative of the layer below).
 #include <cuda_bf16.h>
 
 #include <cstring>
@@ -38,6 +40,7 @@ struct ConvTcArgs {
     const __nv_bfloat16 *w;    // [27][16 in][16 out]
     const float *bias;         // [16] or null
     const __nv_bfloat16 *mask; // [v][16] or null: output *= (mask > 0)
+    const float *addend;       // [v][16] FP32 or null: added before ReLU and mask
     void *out;                 // [v][16] BF16 or FP32
     int *err;
     int ny, nx, nz, ytiles;
@@ -138,10 +141,23 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv3_tc_kernel(const __grid_
             float o[16];
 #pragma unroll
             for (int c = 0; c < 16; ++c) {
-                float s = acc[c] + bias[c];
-                if (A.relu)
-                    s = fmaxf(s, 0.f);
-                o[c] = s;
+                o[c] = acc[c] + bias[c];
+            }
+            if (A.addend) {
+                const float4 *ap = reinterpret_cast<const float4 *>(A.addend + v * 16);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const float4 a4 = __ldg(ap + q);
+                    o[4 * q] += a4.x;
+                    o[4 * q + 1] += a4.y;
+                    o[4 * q + 2] += a4.z;
+                    o[4 * q + 3] += a4.w;
+                }
+            }
+            if (A.relu) {
+#pragma unroll
+                for (int c = 0; c < 16; ++c)
+                    o[c] = fmaxf(o[c], 0.f);
             }
             if (A.mask) {
                 const uint4 *mp = reinterpret_cast<const uint4 *>(A.mask + v * 16);
@@ -214,6 +230,7 @@ cudaError_t launch_conv3_tc(EncodeTiledFn encode, const ConvLaunch &c, int num_s
     A.w = static_cast<const __nv_bfloat16 *>(c.w);
     A.bias = c.bias;
     A.mask = static_cast<const __nv_bfloat16 *>(c.mask);
+    A.addend = c.addend;
     A.out = c.y;
     A.err = d_err;
     A.ny = c.ny;

@@ -107,11 +107,28 @@ cudaStream_t context_stream(asets_context *ctx);
 
 // ---------------------------------------------------------------- warm-start net
 // One 3x3x3 convolution, 16 -> 16 channels (conv_tc.cu).
+// Multilevel solve: grid geometry of one level (padded layout) and a
+// fine/coarse pair.
+constexpr int kMaxLevels = 8;
+constexpr int kMinCoarseCells = 4;
+struct GridGeom {
+    int nr, nc, ns;
+    long long pitch, plane, cells;
+};
+struct GridXfer {
+    GridGeom f, c;
+};
+cudaError_t launch_restrict(const GridXfer &X, const float *src, float *dst, int labels,
+                            float scale, int num_sms, cudaStream_t st);
+cudaError_t launch_prolong(const GridXfer &X, const float *src, float *dst, int labels,
+                           float scale, int axis, int num_sms, cudaStream_t st);
+
 struct ConvLaunch {
     const void *x;       // BF16 [z][x][y][16]
     const void *w;       // BF16 [27][16 in][16 out], tap = (dz*3 + dx)*3 + dy
     const float *bias;   // [16] or null
     const void *mask;    // BF16 [v][16] or null: output *= (mask > 0)
+    const float *addend = nullptr;  // FP32 [v][16] or null: added before ReLU/mask
     void *y;             // BF16 or FP32 [v][16]
     int ny, nx, nz;
     int relu, out_fp32, flip;

@@ -113,6 +113,8 @@ struct asets_solver {
     float *dv = nullptr;
     float *warm_u = nullptr, *warm_ps = nullptr, *warm_pt = nullptr;
     bool warm = false;
+    float *warm_b[3] = {nullptr, nullptr, nullptr};  // initial spatial flows (padded)
+    bool warm_flows = false;
     bool inputs_set = false;
     bool alpha_ok = true;
     IterControl *ctl = nullptr;
@@ -123,6 +125,12 @@ struct asets_solver {
     // results of the last run
     int last_max_it = 0;
     int final_parity = 0;
+    int flow_parity = 0;  // b[flow_parity] holds the flows after the last run
+    // multilevel solve: the next coarser level (owned) and per-level results
+    asets_solver *coarse = nullptr;
+    int ml_levels = 0;
+    int ml_iters[kMaxLevels] = {};
+    float ml_ms[kMaxLevels] = {};
     float last_ms = 0.f;
     int last_launches = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -279,6 +287,7 @@ extern "C" ASETS_API void asets_solver_destroy(asets_solver *s)
 {
     if (!s)
         return;
+    asets_solver_destroy(s->coarse);
     DeviceGuard guard(s->ctx->device);
     cudaStreamSynchronize(s->ctx->stream);
     s->graph.reset();
@@ -648,6 +657,7 @@ extern "C" ASETS_API asets_status asets_solver_set_initial(asets_solver *s, aset
     DeviceGuard guard(s->ctx->device);
     if (!u0 && !ps0 && !pt0) {
         s->warm = false;
+        s->warm_flows = false;
         return ASETS_OK;
     }
     const bool need_ps = (s->model != ASETS_ISHIKAWA);
@@ -668,6 +678,82 @@ extern "C" ASETS_API asets_status asets_solver_set_initial(asets_solver *s, aset
     if (need_ps)
         CU_TRY(copy_in(s, s->warm_ps, ps0, 1, where));
     s->warm = true;
+    return ASETS_OK;
+}
+
+// Reference flow array (bx, by, bz) -> flow slot of the kernel view.  In 2D
+// the stream axis is Matlab x, so bx lives in the stream-face slot.
+static int flow_slot(const asets_solver *s, int ref_axis)
+{
+    if (ref_axis == 1)
+        return SL_BR;
+    if (ref_axis == 0)
+        return s->dim == 3 ? SL_BC : SL_BS;
+    return SL_BS;  // bz, 3D only
+}
+
+// Zero the border faces of a padded flow array (the faces at index 0 of its
+// axis lie outside the volume and are never updated).
+static cudaError_t zero_border_faces(asets_solver *s, float *b, int slot)
+{
+    const size_t L = (size_t)s->flow_labels;
+    cudaStream_t st = s->ctx->stream;
+    if (slot == SL_BR)
+        return cudaMemset2DAsync(b, s->pitch * sizeof(float), 0, sizeof(float),
+                                 (size_t)s->nc * s->ns * L, st);
+    if (slot == SL_BC)
+        return cudaMemset2DAsync(b, s->plane * sizeof(float), 0, s->nr * sizeof(float),
+                                 (size_t)s->ns * L, st);
+    return cudaMemset2DAsync(b, s->cells * sizeof(float), 0, s->plane * sizeof(float), L, st);
+}
+
+extern "C" ASETS_API asets_status asets_solver_set_initial_flows(asets_solver *s,
+                                                                 asets_memory where,
+                                                                 const float *bx,
+                                                                 const float *by,
+                                                                 const float *bz)
+{
+    if (!s)
+        return fail(ASETS_ERR_INVALID_ARG, "solver is NULL");
+    std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
+    DeviceGuard guard(s->ctx->device);
+    if (!bx && !by && !bz) {
+        s->warm_flows = false;
+        return ASETS_OK;
+    }
+    if (!bx || !by || (s->dim == 3) != (bz != nullptr))
+        return fail(ASETS_ERR_INVALID_ARG, "initial flows need bx, by%s", s->dim == 3 ? " and bz" : " (and no bz)");
+    const size_t n = (size_t)s->cells * s->flow_labels;
+    const float *src[3] = {bx, by, bz};
+    for (int a = 0; a < s->dim; ++a) {
+        const int k = flow_slot(s, a);
+        if (!s->warm_b[k]) {
+            asets_status st = dalloc(s, &s->warm_b[k], n);
+            if (st != ASETS_OK)
+                return st;
+        }
+        CU_TRY(copy_in(s, s->warm_b[k], src[a], s->flow_labels, where));
+        CU_TRY(zero_border_faces(s, s->warm_b[k], k));
+    }
+    s->warm_flows = true;
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_solver_get_spatial_flows(asets_solver *s,
+                                                                 asets_memory where, float *bx,
+                                                                 float *by, float *bz)
+{
+    if (!s)
+        return fail(ASETS_ERR_INVALID_ARG, "NULL solver");
+    if (bz && s->dim == 2)
+        return fail(ASETS_ERR_INVALID_ARG, "a 2D problem has no bz");
+    std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
+    DeviceGuard guard(s->ctx->device);
+    float *dst[3] = {bx, by, bz};
+    for (int a = 0; a < s->dim; ++a)
+        if (dst[a])
+            CU_TRY(copy_out(s, dst[a], s->b[s->flow_parity][flow_slot(s, a)], s->flow_labels, where));
+    CU_TRY(cudaStreamSynchronize(s->ctx->stream));
     return ASETS_OK;
 }
 
@@ -749,7 +835,11 @@ static asets_status prepare_run(asets_solver *s, int flags, int tile_config, int
     for (int k = 0; k < 3; ++k) {
         if (s->dim == 2 && k == 0)
             continue;
-        CU_TRY(cudaMemsetAsync(s->b[0][k], 0, n * s->flow_labels * sizeof(float), st));
+        if (s->warm_flows)
+            CU_TRY(cudaMemcpyAsync(s->b[0][k], s->warm_b[k], n * s->flow_labels * sizeof(float),
+                                   cudaMemcpyDeviceToDevice, st));
+        else
+            CU_TRY(cudaMemsetAsync(s->b[0][k], 0, n * s->flow_labels * sizeof(float), st));
     }
     if (s->warm) {
         CU_TRY(cudaMemcpyAsync(s->u[0], s->warm_u, n * s->u_labels * sizeof(float),
@@ -841,6 +931,7 @@ static asets_status finish_run(asets_solver *s, const IterControl &out, int *itN
     if (maxIt > 0 && !out.done)
         return fail(ASETS_ERR_CUDA, "iteration loop ended without completion (iter=%d)", out.iter);
     s->final_parity = (s->model == ASETS_BINARY) ? ((out.last_iter + 1) & 1) : 0;
+    s->flow_parity = (out.last_iter + 1) & 1;
     if (itNum)
         *itNum = (maxIt == 0) ? 0 : out.it_num;
     return ASETS_OK;
@@ -938,6 +1029,187 @@ extern "C" ASETS_API asets_status asets_solver_get_flows(asets_solver *s, asets_
     if (pt)
         CU_TRY(copy_out(s, pt, s->pt[s->final_parity], s->pt_labels, where));
     CU_TRY(cudaStreamSynchronize(s->ctx->stream));
+    return ASETS_OK;
+}
+
+// ---------------------------------------------------------------- multilevel
+
+static GridGeom geom_of(const asets_solver *s)
+{
+    GridGeom g;
+    g.nr = s->nr;
+    g.nc = s->nc;
+    g.ns = s->ns;
+    g.pitch = s->pitch;
+    g.plane = s->plane;
+    g.cells = s->cells;
+    return g;
+}
+
+// Extend the chain of coarse solvers to `levels` levels where the grid
+// allows (every coarse axis keeps at least kMinCoarseCells cells) and
+// restrict the inputs down the chain.  Returns the number of levels.
+static asets_status ml_prepare(asets_solver *s, int levels, int *built)
+{
+    asets_solver *cur = s;
+    int n = 1;
+    while (n < levels && n < kMaxLevels) {
+        const int ny = (cur->ny + 1) / 2, nx = (cur->nx + 1) / 2;
+        const int nz = cur->dim == 3 ? (cur->nz + 1) / 2 : 1;
+        if (ny < kMinCoarseCells || nx < kMinCoarseCells || (cur->dim == 3 && nz < kMinCoarseCells))
+            break;
+        if (!cur->coarse) {
+            asets_solver *c = nullptr;
+            asets_status st = asets_solver_create(cur->ctx, cur->model, cur->dim, ny, nx, nz,
+                                                  cur->nlab, &c);
+            if (st != ASETS_OK)
+                return st;
+            cur->coarse = c;
+        }
+        asets_solver *c = cur->coarse;
+        GridXfer X;
+        X.f = geom_of(cur);
+        X.c = geom_of(c);
+        const int sms = cur->ctx->num_sms;
+        cudaStream_t stm = cur->ctx->stream;
+        if (cur->model == ASETS_BINARY)
+            CU_TRY(launch_restrict(X, cur->cs, c->cs, 1, 2.f, sms, stm));
+        CU_TRY(launch_restrict(X, cur->ct, c->ct, cur->ct_labels, 2.f, sms, stm));
+        CU_TRY(launch_restrict(X, cur->alpha, c->alpha, cur->alpha_labels, 1.f, sms, stm));
+        c->inputs_set = true;
+        c->alpha_ok = cur->alpha_ok;
+        cur = c;
+        ++n;
+    }
+    *built = n;
+    return ASETS_OK;
+}
+
+// Initial state of `f` from the solved state of the next coarser level `c`.
+static asets_status ml_prolong(asets_solver *c, asets_solver *f)
+{
+    const size_t n = (size_t)f->cells;
+    const bool has_ps = (f->model != ASETS_ISHIKAWA);
+    asets_status st;
+    if (!f->warm_u) {
+        if ((st = dalloc(f, &f->warm_u, n * f->u_labels)) != ASETS_OK)
+            return st;
+        if ((st = dalloc(f, &f->warm_pt, n * f->pt_labels)) != ASETS_OK)
+            return st;
+        if (has_ps && (st = dalloc(f, &f->warm_ps, n)) != ASETS_OK)
+            return st;
+    }
+    GridXfer X;
+    X.f = geom_of(f);
+    X.c = geom_of(c);
+    const int sms = f->ctx->num_sms;
+    cudaStream_t stm = f->ctx->stream;
+    CU_TRY(launch_prolong(X, c->u[c->final_parity], f->warm_u, f->u_labels, 1.f, -1, sms, stm));
+    CU_TRY(launch_prolong(X, c->pt[c->final_parity], f->warm_pt, f->pt_labels, 0.5f, -1, sms, stm));
+    if (has_ps)
+        CU_TRY(launch_prolong(X, c->ps[c->final_parity], f->warm_ps, 1, 0.5f, -1, sms, stm));
+    for (int k = 0; k < 3; ++k) {
+        if (f->dim == 2 && k == SL_BC)
+            continue;
+        if (!f->warm_b[k] && (st = dalloc(f, &f->warm_b[k], n * f->flow_labels)) != ASETS_OK)
+            return st;
+        const int axis = (k == SL_BR) ? 0 : (k == SL_BC ? 1 : 2);
+        CU_TRY(launch_prolong(X, c->b[c->flow_parity][k], f->warm_b[k], f->flow_labels, 1.f, axis,
+                              sms, stm));
+    }
+    f->warm = true;
+    f->warm_flows = true;
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_solver_multilevel_prepare(asets_solver *s, int levels,
+                                                                  int *levels_out)
+{
+    if (!s || levels < 1)
+        return fail(ASETS_ERR_INVALID_ARG, "bad multilevel arguments");
+    if (!s->inputs_set)
+        return fail(ASETS_ERR_INVALID_ARG, "inputs not set");
+    std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
+    DeviceGuard guard(s->ctx->device);
+    int built = 1;
+    asets_status st = ml_prepare(s, levels, &built);
+    if (st != ASETS_OK)
+        return st;
+    CU_TRY(cudaStreamSynchronize(s->ctx->stream));
+    if (levels_out)
+        *levels_out = built;
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_solver_level(asets_solver *s, int level, asets_solver **out)
+{
+    if (!s || !out || level < 0)
+        return fail(ASETS_ERR_INVALID_ARG, "bad arguments");
+    asets_solver *cur = s;
+    for (int k = 0; k < level && cur; ++k)
+        cur = cur->coarse;
+    if (!cur)
+        return fail(ASETS_ERR_INVALID_ARG, "level %d does not exist (call asets_solver_multilevel_prepare)", level);
+    *out = cur;
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_solver_run_multilevel(asets_solver *s,
+                                                              const asets_options *opt,
+                                                              int levels, int maxIt,
+                                                              float errBound, float cc,
+                                                              float steps, int *itNum)
+{
+    if (!s || levels < 1 || maxIt < 0)
+        return fail(ASETS_ERR_INVALID_ARG, "bad multilevel arguments");
+    if (!s->inputs_set)
+        return fail(ASETS_ERR_INVALID_ARG, "inputs not set");
+    std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
+    DeviceGuard guard(s->ctx->device);
+    int built = 1;
+    asets_status st = ml_prepare(s, levels, &built);
+    if (st != ASETS_OK)
+        return st;
+    asets_solver *lv[kMaxLevels];
+    lv[0] = s;
+    for (int k = 1; k < built; ++k)
+        lv[k] = lv[k - 1]->coarse;
+    s->ml_levels = 0;
+    for (int k = built - 1; k >= 0; --k) {
+        asets_solver *cur = lv[k];
+        if (k < built - 1 && (st = ml_prolong(lv[k + 1], cur)) != ASETS_OK)
+            return st;
+        int it = 0;
+        st = asets_solver_run(cur, opt, maxIt, errBound, cc, steps, &it);
+        if (k < built - 1) {
+            cur->warm = false;  // the prolonged state is consumed by this run
+            cur->warm_flows = false;
+        }
+        if (st != ASETS_OK)
+            return st;
+        s->ml_iters[k] = it;
+        s->ml_ms[k] = cur->last_ms;
+    }
+    s->ml_levels = built;
+    if (itNum)
+        *itNum = s->ml_iters[0];
+    return ASETS_OK;
+}
+
+extern "C" ASETS_API asets_status asets_solver_multilevel_stats(asets_solver *s, int cap,
+                                                                int *iters, float *ms,
+                                                                int *levels_out)
+{
+    if (!s)
+        return fail(ASETS_ERR_INVALID_ARG, "NULL solver");
+    for (int k = 0; k < s->ml_levels && k < cap; ++k) {
+        if (iters)
+            iters[k] = s->ml_iters[k];
+        if (ms)
+            ms[k] = s->ml_ms[k];
+    }
+    if (levels_out)
+        *levels_out = s->ml_levels;
     return ASETS_OK;
 }
 

@@ -91,6 +91,14 @@ _SIGS = {
     "asets_solver_get_u": (ctypes.c_int, [_VP, ctypes.c_int, _VP]),
     "asets_solver_get_cvg": (ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.c_int]),
     "asets_solver_get_flows": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP]),
+    "asets_solver_run_multilevel": (ctypes.c_int, [_VP, _VP, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                                    ctypes.c_float, ctypes.c_float,
+                                                    ctypes.POINTER(ctypes.c_int)]),
+    "asets_solver_multilevel_prepare": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "asets_solver_level": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(_VP)]),
+    "asets_solver_multilevel_stats": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, ctypes.POINTER(ctypes.c_int)]),
+    "asets_solver_set_initial_flows": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
+    "asets_solver_get_spatial_flows": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
     "asets_solver_last_run_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_float),
                                                    ctypes.POINTER(ctypes.c_int)]),
     "asets_batch_create": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
@@ -108,13 +116,12 @@ _SIGS = {
     "asets_wsnet_destroy": (None, [_VP]),
     "asets_wsnet_get_params": (ctypes.c_int, [_VP, _VP]),
     "asets_wsnet_set_params": (ctypes.c_int, [_VP, _VP]),
-    "asets_wsnet_predict": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP,
-                                           _VP, _VP, _VP]),
-    "asets_wsnet_gradients": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP,
-                                             _VP, _VP, _VP, _VP, _VP, ctypes.POINTER(ctypes.c_float)]),
-    "asets_wsnet_train_step": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP,
-                                              _VP, _VP, _VP, _VP, ctypes.c_float,
-                                              ctypes.POINTER(ctypes.c_float)]),
+    "asets_wsnet_predict": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+                            + [_VP] * 8),
+    "asets_wsnet_gradients": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+                              + [_VP] * 9 + [ctypes.POINTER(ctypes.c_float)]),
+    "asets_wsnet_train_step": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+                               + [_VP] * 8 + [ctypes.c_float, ctypes.POINTER(ctypes.c_float)]),
     "asets_binary_mf3d_noalloc": (ctypes.c_int, [_VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int,
                                                  ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                                  ctypes.c_float, ctypes.c_float, _VP, _VP,
@@ -270,11 +277,70 @@ class Solver:
         check(lib().asets_solver_get_cvg(self._h, HOST, _ptr(out) if n else None, n))
         return out
 
-    def get_flows(self) -> tuple[np.ndarray | None, np.ndarray]:
-        ps = None if self.model == "ishikawa" else np.empty(self.n, np.float32)
-        pt = np.empty(self.n * self.pt_labels, np.float32)
-        check(lib().asets_solver_get_flows(self._h, HOST, _ptr(ps), _ptr(pt)))
+    def get_flows(self, ps=None, pt=None, where: int = HOST):
+        """Final (ps, pt); with where=DEVICE, ps/pt are caller-provided device
+        buffers (ps may be None)."""
+        if where == HOST:
+            ps = None if self.model == "ishikawa" else np.empty(self.n, np.float32)
+            pt = np.empty(self.n * self.pt_labels, np.float32)
+        check(lib().asets_solver_get_flows(self._h, where, _ptr(ps), _ptr(pt)))
         return ps, pt
+
+    def run_multilevel(self, levels: int, max_it: int, err_bound: float, cc: float, steps: float,
+                       *, exact: bool = False, tile_config: int = 0, flags: int = 0) -> int:
+        opt = Options(flags=flags | (FLAG_EXACT if exact else 0), tile_config=tile_config)
+        it = ctypes.c_int(0)
+        check(lib().asets_solver_run_multilevel(self._h, ctypes.byref(opt), levels, max_it,
+                                                err_bound, cc, steps, ctypes.byref(it)))
+        self.last_max_it = max_it
+        return it.value
+
+    def multilevel_prepare(self, levels: int) -> int:
+        n = ctypes.c_int(0)
+        check(lib().asets_solver_multilevel_prepare(self._h, levels, ctypes.byref(n)))
+        return n.value
+
+    def level(self, k: int) -> "Solver":
+        """Level k of the multilevel chain (0 = self), a borrowed solver."""
+        h = _VP()
+        check(lib().asets_solver_level(self._h, k, ctypes.byref(h)))
+        if k == 0:
+            return self
+        s = Solver.__new__(Solver)
+        s.ctx, s.model, s.dim, s.nlab = self.ctx, self.model, self.dim, self.nlab
+        ny, nx, nz = self.ny, self.nx, self.nz
+        for _ in range(k):
+            ny, nx = (ny + 1) // 2, (nx + 1) // 2
+            nz = (nz + 1) // 2 if self.dim == 3 else 1
+        s.ny, s.nx, s.nz = ny, nx, nz
+        s._h, s._keep, s.last_max_it, s._borrowed = h.value, [], 0, True
+        return s
+
+    def multilevel_stats(self) -> tuple[list[int], list[float]]:
+        it = (ctypes.c_int * 8)()
+        ms = (ctypes.c_float * 8)()
+        n = ctypes.c_int(0)
+        check(lib().asets_solver_multilevel_stats(self._h, 8, ctypes.cast(it, _VP),
+                                                  ctypes.cast(ms, _VP), ctypes.byref(n)))
+        return list(it[:n.value]), list(ms[:n.value])
+
+    @property
+    def flow_labels(self) -> int:
+        return {"binary": 1, "potts": self.nlab, "ishikawa": self.nlab - 1}[self.model]
+
+    def set_initial_flows(self, bx=None, by=None, bz=None, where: int = HOST) -> None:
+        if where == HOST:
+            bx, by, bz = _host_f32(bx), _host_f32(by), _host_f32(bz)
+        check(lib().asets_solver_set_initial_flows(self._h, where, _ptr(bx), _ptr(by), _ptr(bz)))
+
+    def get_spatial_flows(self, bx=None, by=None, bz=None, where: int = HOST):
+        """(bx, by, bz) after the last run, reference layout (bz None in 2D)."""
+        if where == HOST:
+            m = self.n * self.flow_labels
+            bx, by = np.empty(m, np.float32), np.empty(m, np.float32)
+            bz = np.empty(m, np.float32) if self.dim == 3 else None
+        check(lib().asets_solver_get_spatial_flows(self._h, where, _ptr(bx), _ptr(by), _ptr(bz)))
+        return bx, by, bz
 
     def last_run_stats(self) -> tuple[float, int]:
         ms = ctypes.c_float(0)
@@ -283,9 +349,9 @@ class Solver:
         return ms.value, n.value
 
     def close(self) -> None:
-        if self._h:
+        if self._h and not getattr(self, "_borrowed", False):
             lib().asets_solver_destroy(self._h)
-            self._h = None
+        self._h = None
 
     def __del__(self):
         try:
@@ -343,7 +409,8 @@ class Batch:
 
 class WarmStartNet:
     """The learned warm start (asets_wsnet_*): a 4-layer 3x3x3 convolutional
-    net, (Ct_1..L, alpha) -> (u_1..L, ps, pt_1..L), on the tensor cores.
+    net, (Ct_1..L, alpha) -> (u_1..L, ps, pt_1..L, bx, by, bz), on the tensor
+    cores.
     Array arguments are device pointers / CUDA tensors in Matlab layout
     (label slowest)."""
 
@@ -368,24 +435,26 @@ class WarmStartNet:
         assert p.size == self.num_params()
         check(lib().asets_wsnet_set_params(self._h, p.ctypes.data))
 
-    def predict(self, dims, ct, alpha, u0, ps0, pt0) -> None:
+    def predict(self, dims, ct, alpha, u0, ps0, pt0, bx0=None, by0=None, bz0=None) -> None:
         ny, nx, nz = dims
         check(lib().asets_wsnet_predict(self._h, ny, nx, nz, _ptr(ct), _ptr(alpha), _ptr(u0),
-                                        _ptr(ps0), _ptr(pt0)))
+                                        _ptr(ps0), _ptr(pt0), _ptr(bx0), _ptr(by0), _ptr(bz0)))
 
-    def gradients(self, dims, ct, alpha, u, ps, pt):
+    def gradients(self, dims, ct, alpha, u, ps, pt, bx, by, bz):
         ny, nx, nz = dims
         g = np.empty(self.num_params(), np.float32)
         loss = ctypes.c_float(0)
         check(lib().asets_wsnet_gradients(self._h, ny, nx, nz, _ptr(ct), _ptr(alpha), _ptr(u),
-                                          _ptr(ps), _ptr(pt), g.ctypes.data, ctypes.byref(loss)))
+                                          _ptr(ps), _ptr(pt), _ptr(bx), _ptr(by), _ptr(bz),
+                                          g.ctypes.data, ctypes.byref(loss)))
         return loss.value, g
 
-    def train_step(self, dims, ct, alpha, u, ps, pt, lr: float) -> float:
+    def train_step(self, dims, ct, alpha, u, ps, pt, bx, by, bz, lr: float) -> float:
         ny, nx, nz = dims
         loss = ctypes.c_float(0)
         check(lib().asets_wsnet_train_step(self._h, ny, nx, nz, _ptr(ct), _ptr(alpha), _ptr(u),
-                                           _ptr(ps), _ptr(pt), lr, ctypes.byref(loss)))
+                                           _ptr(ps), _ptr(pt), _ptr(bx), _ptr(by), _ptr(bz), lr,
+                                           ctypes.byref(loss)))
         return loss.value
 
     def close(self) -> None:

@@ -18,9 +18,13 @@ def rng(seed: int) -> np.random.Generator:
 
 def voronoi_labels(shape: tuple[int, ...], ncells: int, g: np.random.Generator) -> np.ndarray:
     """Index of the nearest of `ncells` uniform seeds, per pixel/voxel."""
+    seeds = g.random((ncells, len(shape))) * np.array(shape, dtype=np.float64)
+    return nearest_seed(shape, seeds)
+
+
+def nearest_seed(shape: tuple[int, ...], seeds: np.ndarray) -> np.ndarray:
     from scipy.spatial import cKDTree
 
-    seeds = g.random((ncells, len(shape))) * np.array(shape, dtype=np.float64)
     tree = cKDTree(seeds)
     out = np.empty(int(np.prod(shape)), dtype=np.int32)
     grids = np.meshgrid(*[np.arange(n, dtype=np.float32) for n in shape], indexing="ij")
@@ -110,17 +114,27 @@ def ishikawa2d(seed: int = 0, shape=(1024, 1024), L=8, alpha=0.2, sigma=0.05):
     return ct, a
 
 
-def potts_warmstart(seed: int, shape=(128, 128, 128), L=6):
-    """Warm-start Potts problems: means U[0,1], 30-80 Voronoi cells, noise
-    U[0.05,0.2], alpha U[0.1,0.5]."""
+def potts_warmstart_draws(seed: int, shape=(128, 128, 128), L=6):
+    """The random draws of one warm-start Potts problem, in generator order:
+    label means U[0,1], 30-80 Voronoi cells, noise sigma U[0.05,0.2], alpha
+    U[0.1,0.5], the cell seeds, each cell's mean, the noise field."""
     g = rng(seed)
     means = g.random(L)
     ncells = int(g.integers(30, 81))
     sigma = float(g.uniform(0.05, 0.2))
     alpha = float(g.uniform(0.1, 0.5))
-    lab = voronoi_labels(shape, ncells, g)
+    seeds = g.random((ncells, len(shape))) * np.array(shape, dtype=np.float64)
     cell_mean = means[g.integers(0, L, size=ncells)]
-    img = np.clip(cell_mean[lab] + g.normal(0.0, sigma, size=shape), 0.0, 1.0).astype(np.float32)
+    noise = g.normal(0.0, sigma, size=shape)
+    return means, seeds, cell_mean, alpha, noise
+
+
+def potts_warmstart(seed: int, shape=(128, 128, 128), L=6):
+    """Warm-start Potts problems: means U[0,1], 30-80 Voronoi cells, noise
+    U[0.05,0.2], alpha U[0.1,0.5]; Ct_l=|I-c_l|, alpha on all L slices."""
+    means, seeds, cell_mean, alpha, noise = potts_warmstart_draws(seed, shape, L)
+    lab = nearest_seed(shape, seeds)
+    img = np.clip(cell_mean[lab] + noise, 0.0, 1.0).astype(np.float32)
     ct = np.empty(shape + (L,), dtype=np.float32, order="F")
     for l in range(L):
         ct[..., l] = np.abs(img - np.float32(means[l]))

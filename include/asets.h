@@ -156,6 +156,20 @@ ASETS_API asets_status asets_solver_set_inputs(asets_solver *s, asets_memory whe
 ASETS_API asets_status asets_solver_set_initial(asets_solver *s, asets_memory where,
                                                 const float *u0, const float *ps0,
                                                 const float *pt0);
+/* Spatial flows: initial values and the state after a run (no counterpart in
+ * the reference, whose runMaxFlow keeps bx/by/bz internal and starts them at
+ * zero).  Layout as the reference's arrays: flow_labels*N floats each
+ * (1 binary, L Potts, L-1 Ishikawa), bx(y,x[,z]) the flow across the face
+ * between x-1 and x, by between y-1 and y, bz between z-1 and z (3D only;
+ * pass NULL in 2D).  Border faces (index 0 of their axis) are taken as zero.
+ * Initial flows apply to every later run until cleared with all NULL or by
+ * asets_solver_set_initial(all NULL).  Together with set_initial and
+ * get_u/get_flows this saves and restores the full iteration state. */
+ASETS_API asets_status asets_solver_set_initial_flows(asets_solver *s, asets_memory where,
+                                                      const float *bx, const float *by,
+                                                      const float *bz);
+ASETS_API asets_status asets_solver_get_spatial_flows(asets_solver *s, asets_memory where,
+                                                      float *bx, float *by, float *bz);
 /* Run up to maxIt iterations; itNum as in the one-shot calls. */
 ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_options *opt, int maxIt,
                                         float errBound, float cc, float steps, int *itNum);
@@ -167,6 +181,30 @@ ASETS_API asets_status asets_solver_get_cvg(asets_solver *s, asets_memory where,
  * Potts/Ishikawa N*L). */
 ASETS_API asets_status asets_solver_get_flows(asets_solver *s, asets_memory where, float *ps,
                                               float *pt);
+/* Multilevel (coarse-to-fine) solve (no counterpart in the reference): the
+ * problem is restricted to grids with half the cells per axis (cost terms
+ * 2*mean over each 2x2(x2) block, alpha the block mean), the coarsest grid is
+ * solved first, and each solved state (u, ps, pt and the flows) is prolonged
+ * to the next finer grid as its initial state (u copied, ps/pt halved, flows
+ * interpolated along their axis), down to the original grid, whose run gives
+ * u, erriter and itNum as asets_solver_run does.  Every level runs with the
+ * same maxIt, errBound, cc and steps.  Coarsening stops when an axis would
+ * fall below 4 cells (at most 8 levels).  The coarse levels are solvers
+ * owned by `s`; an initial state set on the coarsest level (through
+ * asets_solver_level) is used by its run, one set on `s` itself is replaced
+ * by the prolonged state.  levels = 1 is asets_solver_run. */
+ASETS_API asets_status asets_solver_run_multilevel(asets_solver *s, const asets_options *opt,
+                                                   int levels, int maxIt, float errBound,
+                                                   float cc, float steps, int *itNum);
+/* Create the coarse levels and restrict the current inputs to them without
+ * solving; *levels_out = the number of levels the grid allows (<= levels). */
+ASETS_API asets_status asets_solver_multilevel_prepare(asets_solver *s, int levels,
+                                                       int *levels_out);
+/* Level `level` (0 = s) of the multilevel chain; owned by s (do not destroy). */
+ASETS_API asets_status asets_solver_level(asets_solver *s, int level, asets_solver **out);
+/* Per-level itNum and device ms of the last multilevel run (level 0 = s). */
+ASETS_API asets_status asets_solver_multilevel_stats(asets_solver *s, int cap, int *iters,
+                                                     float *ms, int *levels_out);
 /* Device time (ms) of the last run's iteration loop, from CUDA events on the
  * launch stream, and the number of kernel launches it made. */
 ASETS_API asets_status asets_solver_last_run_stats(asets_solver *s, float *ms,
@@ -213,37 +251,45 @@ ASETS_API asets_status asets_conv3d_bf16(asets_context *ctx, const void *x, cons
                                          int Nx, int Nz, int relu, int out_fp32, int flip);
 
 /* ------------------------------------------------------------------------
- * Learned warm start for the labelled models (no counterpart in the
- * reference): a network of four 3x3x3 convolutions with 16 channels and ReLU
- * maps (Ct_1..Ct_L, alpha) to an initial (u_1..u_L, ps, pt_1..pt_L) for
- * asets_solver_set_initial.  Forward and input-gradient convolutions run on
- * the tensor cores (BF16, FP32 accumulation), weight gradients in FP32;
- * training is Adam on an MSE loss against solver solutions.  All arrays are
- * device pointers in Matlab layout (label slowest); alpha is one slice.
- * Parameters: 4 x (27*16*16 weights [tap][in][out] + 16 biases), float.
+ * Learned warm start for the Potts model (no counterpart in the reference):
+ * a network of four 3x3x3 convolutional layers with 16 hidden channels and
+ * ReLU maps (Ct_1..Ct_L, alpha) to an initial state for
+ * asets_solver_set_initial / asets_solver_set_initial_flows: u_1..u_L, ps,
+ * pt_1..pt_L and the spatial flows bx, by, bz (L slices each).  Forward and
+ * data-gradient convolutions run on the tensor cores (BF16, FP32
+ * accumulation), weight gradients in FP32; training is Adam on an MSE loss
+ * against solver states (flows relative to alpha).  All arrays are device
+ * pointers in Matlab layout (label slowest); alpha is one slice.
+ * Parameters: 5 blocks x (27*16*16 weights [tap][in][out] + 16 biases),
+ * float; blocks 0-2 are the hidden layers, blocks 3 and 4 the two 16-channel
+ * halves of the 32-channel output layer.
  * ---------------------------------------------------------------------- */
 typedef struct asets_wsnet asets_wsnet;
 
 ASETS_API int asets_wsnet_num_params(void);
-/* nLab <= 7; weights He-initialised from `seed`. */
+/* 1 <= nLab <= 6; weights He-initialised from `seed`. */
 ASETS_API asets_status asets_wsnet_create(asets_context *ctx, int nLab, unsigned long long seed,
                                           asets_wsnet **out);
 ASETS_API void asets_wsnet_destroy(asets_wsnet *n);
 ASETS_API asets_status asets_wsnet_get_params(asets_wsnet *n, float *host_params);
 ASETS_API asets_status asets_wsnet_set_params(asets_wsnet *n, const float *host_params);
-/* u0 (N*L, clamped to [0,1]), ps0 (N), pt0 (N*L) for a Ny x Nx x Nz volume. */
+/* u0 (N*L, clamped to [0,1]), ps0 (N), pt0 (N*L) and optionally the flows
+ * bx0, by0, bz0 (N*L each; all three or none) for a Ny x Nx x Nz volume. */
 ASETS_API asets_status asets_wsnet_predict(asets_wsnet *n, int Ny, int Nx, int Nz,
                                            const float *Ct, const float *alpha, float *u0,
-                                           float *ps0, float *pt0);
-/* Loss and parameter gradients (host) against a solution (u, ps, pt). */
+                                           float *ps0, float *pt0, float *bx0, float *by0,
+                                           float *bz0);
+/* Loss and parameter gradients (host) against a solver state. */
 ASETS_API asets_status asets_wsnet_gradients(asets_wsnet *n, int Ny, int Nx, int Nz,
                                              const float *Ct, const float *alpha, const float *u,
-                                             const float *ps, const float *pt, float *host_grads,
+                                             const float *ps, const float *pt, const float *bx,
+                                             const float *by, const float *bz, float *host_grads,
                                              float *loss);
 /* One Adam step (learning rate lr) on one solved volume; returns the loss. */
 ASETS_API asets_status asets_wsnet_train_step(asets_wsnet *n, int Ny, int Nx, int Nz,
                                               const float *Ct, const float *alpha,
                                               const float *u, const float *ps, const float *pt,
+                                              const float *bx, const float *by, const float *bz,
                                               float lr, float *loss);
 
 /* ------------------------------------------------------------------------

@@ -10,7 +10,7 @@ from __future__ import annotations
 
 import numpy as np
 
-LAYERS = 4
+BLOCKS = 5   # 3 hidden layers + the two 16-channel halves of the output layer
 NW = 27 * 16 * 16
 
 
@@ -24,8 +24,8 @@ def bf16(a: np.ndarray) -> np.ndarray:
 
 def unpack(params: np.ndarray):
     ws, bs = [], []
-    for l in range(LAYERS):
-        base = l * (NW + 16)
+    for b in range(BLOCKS):
+        base = b * (NW + 16)
         ws.append(params[base:base + NW].reshape(27, 16, 16).astype(np.float64))
         bs.append(params[base + NW:base + NW + 16].astype(np.float64))
     return ws, bs
@@ -72,27 +72,36 @@ def wgrad(a, g):
 
 
 def loss_and_grads(params, x, target, L):
-    """x: [nz, nx, ny, 16] network input (BF16 values); target: [.., 16].
-    Returns (loss, flat gradient in the parameter layout)."""
+    """x: [nz, nx, ny, 16] network input (BF16 values); target: [.., 32]
+    (u, ps, pt, flows/alpha).  Returns (loss, flat gradient in the parameter
+    layout, 32-channel output)."""
     ws, bs = unpack(params)
     wq = [bf16(w) for w in ws]
     acts = [bf16(x)]
-    for l in range(LAYERS - 1):
+    for l in range(3):
         acts.append(bf16(np.maximum(conv(acts[-1], wq[l], bs[l]), 0.0)))
-    out = conv(acts[-1], wq[LAYERS - 1], bs[LAYERS - 1])
-    used = 2 * L + 1
+    out = np.concatenate([conv(acts[3], wq[3], bs[3]), conv(acts[3], wq[4], bs[4])], axis=-1)
+    used = 5 * L + 1
     vox = x.shape[0] * x.shape[1] * x.shape[2]
     scale = 1.0 / (vox * used)
     d = np.zeros_like(out)
     d[..., :used] = out[..., :used] - target[..., :used]
     loss = float(np.sum(d * d) * scale)
     g = bf16(2.0 * d * scale)
-    grads = np.zeros(LAYERS * (NW + 16))
-    for l in range(LAYERS - 1, -1, -1):
-        base = l * (NW + 16)
-        grads[base:base + NW] = wgrad(acts[l], g).ravel()
-        grads[base + NW:base + NW + 16] = g.sum(axis=(0, 1, 2))
+    grads = np.zeros(BLOCKS * (NW + 16))
+
+    def put(b, a, gg):
+        base = b * (NW + 16)
+        grads[base:base + NW] = wgrad(a, gg).ravel()
+        grads[base + NW:base + NW + 16] = gg.sum(axis=(0, 1, 2))
+
+    put(3, acts[3], g[..., :16])
+    put(4, acts[3], g[..., 16:])
+    gh = conv_transpose(g[..., :16], wq[3]) + conv_transpose(g[..., 16:], wq[4])
+    gh = bf16(np.where(acts[3] > 0, gh, 0.0))
+    for l in range(2, -1, -1):
+        put(l, acts[l], gh)
         if l == 0:
             break
-        g = bf16(np.where(acts[l] > 0, conv_transpose(g, wq[l]), 0.0))
+        gh = bf16(np.where(acts[l] > 0, conv_transpose(gh, wq[l]), 0.0))
     return loss, grads, out
