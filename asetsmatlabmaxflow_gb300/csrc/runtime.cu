@@ -647,6 +647,27 @@ extern "C" ASETS_API asets_status asets_solver_set_inputs(asets_solver *s, asets
     return ASETS_OK;
 }
 
+extern "C" ASETS_API asets_status asets_solver_get_inputs(asets_solver *s, asets_memory where,
+                                                          float *Cs, float *Ct, float *alpha)
+{
+    if (!s)
+        return fail(ASETS_ERR_INVALID_ARG, "solver is NULL");
+    if (!s->inputs_set)
+        return fail(ASETS_ERR_INVALID_ARG, "inputs not set");
+    if (Cs && s->model != ASETS_BINARY)
+        return fail(ASETS_ERR_INVALID_ARG, "only the binary model has Cs");
+    std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
+    DeviceGuard guard(s->ctx->device);
+    if (Cs)
+        CU_TRY(copy_out(s, Cs, s->cs, 1, where));
+    if (Ct)
+        CU_TRY(copy_out(s, Ct, s->ct, s->ct_labels, where));
+    if (alpha)
+        CU_TRY(copy_out(s, alpha, s->alpha, s->alpha_labels, where));
+    CU_TRY(cudaStreamSynchronize(s->ctx->stream));
+    return ASETS_OK;
+}
+
 extern "C" ASETS_API asets_status asets_solver_set_initial(asets_solver *s, asets_memory where,
                                                            const float *u0, const float *ps0,
                                                            const float *pt0)

@@ -97,6 +97,7 @@ _SIGS = {
     "asets_solver_multilevel_prepare": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "asets_solver_level": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(_VP)]),
     "asets_solver_multilevel_stats": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, ctypes.POINTER(ctypes.c_int)]),
+    "asets_solver_get_inputs": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
     "asets_solver_set_initial_flows": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
     "asets_solver_get_spatial_flows": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
     "asets_solver_last_run_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_float),
@@ -250,6 +251,17 @@ class Solver:
             Ct, alpha, Cs = _host_f32(Ct), _host_f32(alpha), _host_f32(Cs)
             self._keep = [Ct, alpha, Cs]
         check(lib().asets_solver_set_inputs(self._h, where, _ptr(Cs), _ptr(Ct), _ptr(alpha)))
+
+    def get_inputs(self, Cs=None, Ct=None, alpha=None, where: int = HOST):
+        """(Cs, Ct, alpha) as set (restricted, on a coarse level); with
+        where=DEVICE the caller provides the buffers."""
+        if where == HOST:
+            al = {"binary": 1, "potts": self.nlab, "ishikawa": self.nlab - 1}[self.model]
+            Cs = np.empty(self.n, np.float32) if self.model == "binary" else None
+            Ct = np.empty(self.n * (1 if self.model == "binary" else self.nlab), np.float32)
+            alpha = np.empty(self.n * al, np.float32)
+        check(lib().asets_solver_get_inputs(self._h, where, _ptr(Cs), _ptr(Ct), _ptr(alpha)))
+        return Cs, Ct, alpha
 
     def set_initial(self, u0=None, ps0=None, pt0=None, where: int = HOST) -> None:
         if where == HOST:

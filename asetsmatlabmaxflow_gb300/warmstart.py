@@ -2,25 +2,31 @@
 device, solver-generated training pairs, training, and the warm-vs-cold
 evaluation with its cold-start fallback.
 
-The workload is Potts 3D, 128^3 voxels, L = 6 labels (cc = 0.3,
-steps = 0.11): label means U[0,1], a Voronoi partition into 30-80 cells,
-noise sigma U[0.05, 0.2], Ct_l = |I - c_l|, one alpha U[0.1, 0.5] per problem.
-The network (asets_wsnet_*, four 3x3x3 convolutional layers with 16 hidden
-channels) maps (Ct_1..Ct_6, alpha) to an initial solver state: u_1..u_6, ps,
-pt_1..pt_6 and the spatial flows bx, by, bz.  It is trained on the states of
-cold solves run to errBound 1e-5, one pair per seed, generated on the fly (a
-replay buffer of recent pairs stays on the device).  The flows are part of
-the prediction because the solver spends most of its iterations rebuilding
-them: started from the exact converged (u, ps, pt) with zero flows, a solve
-still needs 30-75% of the cold iterations, while noisy flows added to it
-bring that down to about 10%.
+Workload: Potts 3D, 128^3 voxels, L = 6 labels (cc = 0.3, steps = 0.11):
+label means U[0,1], a Voronoi partition into 30-80 cells, noise sigma
+U[0.05, 0.2], Ct_l = |I - c_l|, one alpha U[0.1, 0.5] per problem.
 
-Fallback: the warm solve gets the cold start's calibrated iteration budget
-(the median iterations-to-errBound of cold solves of the training problems);
-if it has not converged by then, the problem is solved again from the cold
-start and that result is used.  The evaluation also solves every held-out
-problem from the cold start, which judges the warm labelling (label
-agreement).
+The network (asets_wsnet_*: four 3x3x3 convolutional layers, 16 hidden
+channels, BF16 on the tensor cores) maps (Ct_1..Ct_6, alpha) to an initial
+solver state: u_1..u_6, ps, pt_1..pt_6 and the spatial flows bx, by, bz.  It
+is trained on states of cold solves run to errBound 1e-5.
+
+Where it is applied.  Measured on this workload, the state of a solve at
+errBound 1e-4 depends on region-scale decisions far outside the network's
+9^3 receptive field: started from the exact converged (u, ps, pt), a solve
+still needs 30-75% of the cold iterations, and the network's prediction of
+the full-resolution state (flows included) does not lower them.  The solve
+therefore runs coarse to fine (asets_solver_run_multilevel, three levels:
+32^3, 64^3, 128^3), and the network predicts the initial state of the
+coarsest level, where the same receptive field covers a quarter of each
+axis.  `level=0` trains and applies it at full resolution instead.
+
+Fallback and judge: the warm solve is accepted when its full-resolution
+iterations stay below the cold start's calibrated budget (the median
+iterations-to-errBound of cold solves of training problems); otherwise the
+problem is solved again from the cold start and that result is used.  The
+evaluation solves every held-out problem from the cold start as well, which
+judges the warm labelling (label agreement).
 """
 from __future__ import annotations
 
@@ -36,6 +42,7 @@ from . import synth
 WEIGHTS = Path(__file__).resolve().parent / "weights" / "potts3d_128_l6.npz"
 SHAPE = (128, 128, 128)
 LABELS = 6
+LEVELS = 3
 CC, STEPS = 0.3, 0.11
 TRAIN_ERR = 1e-5
 EVAL_ERR = 1e-4
@@ -77,133 +84,162 @@ def labels(u, n: int, L: int = LABELS):
     return u.view(L, n).argmax(0)
 
 
-@dataclass
-class Pair:
-    ct: object
-    alpha: object
-    state: tuple  # u, ps, pt, bx, by, bz
+class Level:
+    """Device buffers for one level's inputs and state."""
+
+    def __init__(self, solver: N.Solver, L: int):
+        import torch
+
+        self.s = solver
+        self.shape = (solver.ny, solver.nx, solver.nz)
+        self.n = int(np.prod(self.shape))
+        n = self.n
+        self.ct = torch.empty(n * L, device="cuda")
+        self.alpha_full = torch.empty(n * L, device="cuda")
+        self.state = [torch.empty(n * L, device="cuda"), torch.empty(n, device="cuda")] + \
+            [torch.empty(n * L, device="cuda") for _ in range(4)]  # u, ps, pt, bx, by, bz
+
+    @property
+    def alpha(self):
+        return self.alpha_full[:self.n]
+
+    def read_inputs(self):
+        self.s.get_inputs(None, self.ct, self.alpha_full, where=N.DEVICE)
+
+    def read_state(self):
+        """Final (u, ps, pt, bx, by, bz) of this level's last run."""
+        u, ps, pt, bx, by, bz = self.state
+        self.s.get_u(u, where=N.DEVICE)
+        self.s.get_flows(ps, pt, where=N.DEVICE)
+        self.s.get_spatial_flows(bx, by, bz, where=N.DEVICE)
+        return self.state
+
+    def set_initial(self, st=None):
+        if st is None:
+            self.s.set_initial(None, None, None)
+            return
+        u0, ps0, pt0, bx0, by0, bz0 = st
+        self.s.set_initial(u0, ps0, pt0, where=N.DEVICE)
+        self.s.set_initial_flows(bx0, by0, bz0, where=N.DEVICE)
 
 
 class Runner:
-    """One device-resident Potts solver for the warm-start shape."""
+    """The full-resolution Potts solver and its multilevel chain."""
 
-    def __init__(self, ctx: N.Context | None = None, shape=SHAPE, L: int = LABELS):
-        import torch
-
+    def __init__(self, ctx: N.Context | None = None, shape=SHAPE, L: int = LABELS,
+                 levels: int = LEVELS):
         self.ctx = ctx or N.Context.default()
         self.shape, self.L = shape, L
         self.n = int(np.prod(shape))
         self.s = N.Solver(self.ctx, "potts", shape, L)
-        self.u = torch.empty(self.n * L, device="cuda")
-        self.ps = torch.empty(self.n, device="cuda")
-        self.pt = torch.empty(self.n * L, device="cuda")
-        self.b = [torch.empty(self.n * L, device="cuda") for _ in range(3)]
+        self.levels = levels
+        self.lv: list[Level] = []
 
     def load(self, ct, alpha_full):
         self.s.set_inputs(ct, alpha_full, where=N.DEVICE)
+        got = self.s.multilevel_prepare(self.levels)
+        if not self.lv:
+            self.lv = [Level(self.s.level(k), self.L) for k in range(got)]
+        self.top = self.lv[-1]
+        for lv in self.lv:
+            lv.read_inputs()
 
     def cold(self, err: float, max_it: int = MAX_IT) -> int:
-        self.s.set_initial(None, None, None)
+        self.lv[0].set_initial(None)
         return self.s.run(max_it, err, CC, STEPS)
 
     def warm(self, state, err: float, max_it: int) -> int:
-        u0, ps0, pt0, bx0, by0, bz0 = state
-        self.s.set_initial(u0, ps0, pt0, where=N.DEVICE)
-        self.s.set_initial_flows(bx0, by0, bz0, where=N.DEVICE)
+        """Full-resolution solve from `state`."""
+        self.lv[0].set_initial(state)
         return self.s.run(max_it, err, CC, STEPS)
 
-    @staticmethod
-    def converged(it: int, max_it: int) -> bool:
-        """itNum is the index of the iteration that met errBound, or maxIt
-        when none did."""
-        return it < max_it
-
-    def first_below(self, it: int, err: float) -> int:
-        """itNum a cold run with errBound `err` would have returned (the same
-        trajectory; the Potts stopping rule is erriter <= errBound)."""
-        c = self.s.get_cvg(min(it + 1, self.s.last_max_it))
-        hit = np.nonzero(c <= err)[0]
-        return int(hit[0]) if hit.size else -1
-
-    def state(self):
-        """Final (u, ps, pt, bx, by, bz) of the last run (device buffers)."""
-        self.s.get_u(self.u, where=N.DEVICE)
-        self.s.get_flows(self.ps, self.pt, where=N.DEVICE)
-        self.s.get_spatial_flows(*self.b, where=N.DEVICE)
-        return (self.u, self.ps, self.pt, *self.b)
+    def multilevel(self, err: float, max_it: int = MAX_IT, top_state=None):
+        """Coarse-to-fine solve; the coarsest level starts from `top_state`
+        (or cold).  Returns (full-resolution itNum, per-level itNum)."""
+        self.top.set_initial(top_state)
+        it = self.s.run_multilevel(len(self.lv), max_it, err, CC, STEPS)
+        return it, self.s.multilevel_stats()[0]
 
     def close(self):
         self.s.close()
 
 
-def train(train_seeds, *, steps_per_pair: int = 2, buffer: int = 24, lr: float = 2e-3,
-          lr_final: float = 1e-4, seed: int = 0, log=print):
+def train(train_seeds, *, level: int = LEVELS - 1, epochs: int = 16, lr: float = 2e-3,
+          lr_final: float = 1e-4, calib: int = 50, seed: int = 0, log=print):
     """Train a fresh network on cold solutions (errBound 1e-5) of
-    `train_seeds`.  Returns (net, info) where info holds the calibrated cold
-    iteration budget for errBound 1e-4 and the loss history."""
+    `train_seeds` at multilevel `level` (0 = full resolution; pairs kept on
+    the device).  The first `calib` seeds also get a full-resolution cold
+    solve at errBound 1e-4 for the fallback budget."""
     import torch
 
     run = Runner()
     net = N.WarmStartNet(run.ctx, nlab=LABELS, seed=seed)
-    g = np.random.default_rng(seed)
-    buf: list[Pair] = []
-    cold_iters, losses = [], []
-    total = len(train_seeds) * steps_per_pair
-    k = 0
+    pairs, cold_iters = [], []
     t0 = time.time()
     for i, sd in enumerate(train_seeds):
         ct, a1, af = problem(sd)
         run.load(ct, af)
-        it = run.cold(TRAIN_ERR)
-        cold_iters.append(run.first_below(it, EVAL_ERR))
-        buf.append(Pair(ct, a1, tuple(t.clone() for t in run.state())))
-        if len(buf) > buffer:
-            buf.pop(0)
-        for _ in range(steps_per_pair):
-            p = buf[int(g.integers(len(buf)))]
-            frac = k / max(1, total - 1)
-            lr_k = lr_final + 0.5 * (lr - lr_final) * (1 + np.cos(np.pi * frac))
-            losses.append(net.train_step(run.shape, p.ct, p.alpha, *p.state, lr=lr_k))
-            k += 1
-        if log and (i % 50 == 0 or i == len(train_seeds) - 1):
-            log(f"pair {i + 1}/{len(train_seeds)} seed {sd}: cold it(1e-5)={it} "
-                f"it(1e-4)={cold_iters[-1]} loss={np.mean(losses[-2 * steps_per_pair:]):.5f} "
-                f"{time.time() - t0:.0f}s")
+        lv = run.lv[level]
+        if i < calib:
+            cold_iters.append(run.cold(EVAL_ERR))
+        lv.set_initial(None)
+        lv.s.run(MAX_IT, TRAIN_ERR, CC, STEPS)
+        st = [t.clone() for t in lv.read_state()]
+        pairs.append((lv.ct.clone(), lv.alpha.clone(), st))
+        if log and (i % 250 == 0 or i == len(train_seeds) - 1):
+            log(f"pair {i + 1}/{len(train_seeds)} {time.time() - t0:.0f}s")
+    gen_s = time.time() - t0
+    g = np.random.default_rng(seed)
+    total = epochs * len(pairs)
+    losses = []
+    t1 = time.time()
+    order = None
+    for k in range(total):
+        if k % len(pairs) == 0:
+            order = g.permutation(len(pairs))
+        ct, a1, st = pairs[order[k % len(pairs)]]
+        lr_k = lr_final + 0.5 * (lr - lr_final) * (1 + np.cos(np.pi * k / max(1, total - 1)))
+        losses.append(net.train_step(run.lv[level].shape, ct, a1, *st, lr=lr_k))
+        if log and (k % 2000 == 0 or k == total - 1):
+            log(f"step {k + 1}/{total} loss {np.mean(losses[-200:]):.5f} {time.time() - t1:.0f}s")
     torch.cuda.synchronize()
     run.close()
-    ci = np.array([c for c in cold_iters if c > 0])
-    info = {"cold_budget": int(np.median(ci)), "cold_iters": np.array(cold_iters),
-            "losses": np.array(losses, np.float32), "train_pairs": len(train_seeds),
-            "steps_per_pair": steps_per_pair, "train_seconds": time.time() - t0}
+    info = {"cold_budget": int(np.median(cold_iters)) if cold_iters else MAX_IT,
+            "losses": np.array(losses, np.float32), "train_pairs": len(pairs),
+            "epochs": epochs, "level": level, "gen_seconds": gen_s,
+            "train_seconds": time.time() - t1}
     return net, info
 
 
 def save(net: N.WarmStartNet, info: dict, path: Path = WEIGHTS) -> None:
     path.parent.mkdir(parents=True, exist_ok=True)
     np.savez(path, params=net.get_params(), cold_budget=info["cold_budget"],
-             train_pairs=info["train_pairs"], steps_per_pair=info["steps_per_pair"],
-             final_loss=float(np.mean(info["losses"][-50:])))
+             train_pairs=info["train_pairs"], epochs=info["epochs"], level=info["level"],
+             final_loss=float(np.mean(info["losses"][-200:])))
 
 
 def load(ctx: N.Context | None = None, path: Path = WEIGHTS):
-    """The trained network and its calibrated cold iteration budget."""
+    """(network, cold iteration budget, level it was trained for)."""
     d = np.load(path)
     net = N.WarmStartNet(ctx or N.Context.default(), nlab=LABELS, seed=0)
     net.set_params(d["params"])
-    return net, int(d["cold_budget"])
+    return net, int(d["cold_budget"]), int(d["level"])
 
 
 @dataclass
 class EvalResult:
     seed: int
     cold_it: int
-    cold_ms: float          # wall time of the cold solve (init + iterations)
-    warm_it: int            # iterations of the warm solve (its cap when it fell back)
-    warm_ms: float          # net inference + warm solve (+ the cold solve on fallback)
+    cold_ms: float              # wall time of the cold solve (init + iterations)
+    ml_its: list                # per-level itNum, multilevel with a cold coarsest level
+    ml_ms: float
+    warm_its: list              # per-level itNum with the learned initial state
+    warm_ms: float              # net inference + solve (+ the cold solve on fallback)
     infer_ms: float
     fallback: bool
-    agree_cold: float       # warm labels vs cold labels, both at errBound 1e-4
-    agree_tight: float = float("nan")      # warm labels vs a 1e-5 cold solve
+    agree_cold: float           # warm labels vs cold labels, both at errBound 1e-4
+    agree_ml: float             # multilevel (cold coarsest) labels vs cold labels
+    agree_tight: float = float("nan")       # warm labels vs a 1e-5 cold solve
     cold_agree_tight: float = float("nan")  # cold 1e-4 labels vs the same
     extra: dict = field(default_factory=dict)
 
@@ -218,50 +254,65 @@ def _sync_ms(fn):
     return r, 1e3 * (time.perf_counter() - t)
 
 
-def evaluate(net: N.WarmStartNet, cold_budget: int, seeds, *, tight: bool = True,
-             run: Runner | None = None, log=None) -> list[EvalResult]:
-    """Warm vs cold on held-out seeds, errBound 1e-4.  Each problem is solved
-    cold first (also the judge), then warm with the fallback rule."""
-    import torch
-
+def evaluate(net: N.WarmStartNet, cold_budget: int, seeds, *, level: int = LEVELS - 1,
+             tight: bool = True, run: Runner | None = None, log=None) -> list[EvalResult]:
+    """Cold vs multilevel vs learned warm start on held-out seeds, errBound
+    1e-4.  level = the multilevel level the network predicts (0 = a direct
+    full-resolution warm start without the coarse levels)."""
     own = run is None
     run = run or Runner()
-    n, L = run.n, run.L
-    pred = [torch.empty(n * L, device="cuda"), torch.empty(n, device="cuda")] + \
-        [torch.empty(n * L, device="cuda") for _ in range(4)]
+    n = run.n
     out = []
     for sd in seeds:
         ct, a1, af = problem(sd)
         run.load(ct, af)
+        lv = run.lv[level]
         cold_it, cold_ms = _sync_ms(lambda: run.cold(EVAL_ERR))
-        lab_c = labels(run.state()[0], n).clone()
+        lab_c = labels(run.lv[0].read_state()[0], n).clone()
+        (_, ml_its), ml_ms = _sync_ms(lambda: run.multilevel(EVAL_ERR))
+        lab_m = labels(run.lv[0].read_state()[0], n).clone()
 
         def warm_path():
-            net.predict(run.shape, ct, a1, *pred)
+            net.predict(lv.shape, lv.ct, lv.alpha, *lv.state)
             t_inf = time.perf_counter()
-            it = run.warm(pred, EVAL_ERR, cold_budget)
-            fb = not run.converged(it, cold_budget)
+            if level == 0:
+                it = run.warm(lv.state, EVAL_ERR, cold_budget)
+                its = [it]
+            else:
+                it, its = run.multilevel(EVAL_ERR, MAX_IT, lv.state)
+            fb = it >= cold_budget
             if fb:
                 run.cold(EVAL_ERR)
-            return it, fb, t_inf
+            return its, fb, t_inf
 
         t0 = time.perf_counter()
-        (warm_it, fb, t_inf), warm_ms = _sync_ms(warm_path)
-        infer_ms = 1e3 * (t_inf - t0)
-        lab_w = labels(run.state()[0], n)
-        r = EvalResult(sd, cold_it, cold_ms, warm_it, warm_ms, infer_ms, fb,
-                       float((lab_w == lab_c).float().mean()))
+        (w_its, fb, t_inf), warm_ms = _sync_ms(warm_path)
+        lab_w = labels(run.lv[0].read_state()[0], n)
+        r = EvalResult(sd, cold_it, cold_ms, ml_its, ml_ms, w_its, warm_ms,
+                       1e3 * (t_inf - t0), fb, float((lab_w == lab_c).float().mean()),
+                       float((lab_m == lab_c).float().mean()))
         if tight:
-            run.cold(TRAIN_ERR)
-            lab_t = labels(run.state()[0], n)
+            # both solved to errBound 1e-5 as well: time and label agreement
+            it_t, ms_t = _sync_ms(lambda: run.cold(TRAIN_ERR))
+            lab_t = labels(run.lv[0].read_state()[0], n).clone()
             r.agree_tight = float((lab_w == lab_t).float().mean())
             r.cold_agree_tight = float((lab_c == lab_t).float().mean())
+            r.extra["ml_agree_tight"] = float((lab_m == lab_t).float().mean())
+            if level > 0:
+                def warm_tight():
+                    net.predict(lv.shape, lv.ct, lv.alpha, *lv.state)
+                    return run.multilevel(TRAIN_ERR, MAX_IT, lv.state)
+                (_, its5), ms5 = _sync_ms(warm_tight)
+                lab5 = labels(run.lv[0].read_state()[0], n)
+                r.extra.update(cold5_it=it_t, cold5_ms=ms_t, warm5_its=its5, warm5_ms=ms5,
+                               agree5=float((lab5 == lab_t).float().mean()))
         out.append(r)
         if log:
-            log(f"seed {sd}: cold {cold_it} it {cold_ms:.1f} ms | warm {warm_it} it "
-                f"{warm_ms:.1f} ms (net {infer_ms:.1f} ms){' FALLBACK' if fb else ''} | "
-                f"agree cold {r.agree_cold:.5f} tight {r.agree_tight:.5f} "
-                f"(cold vs tight {r.cold_agree_tight:.5f})")
+            log(f"seed {sd}: cold {cold_it} it {cold_ms:.1f} ms | multilevel {ml_its} "
+                f"{ml_ms:.1f} ms | learned {w_its} {warm_ms:.1f} ms (net {r.infer_ms:.1f} ms)"
+                f"{' FALLBACK' if fb else ''} | agree cold {r.agree_cold:.4f} "
+                f"(multilevel {r.agree_ml:.4f}) tight {r.agree_tight:.4f} "
+                f"(cold {r.cold_agree_tight:.4f})")
     if own:
         run.close()
     return out
@@ -269,23 +320,51 @@ def evaluate(net: N.WarmStartNet, cold_budget: int, seeds, *, tight: bool = True
 
 def summarize(res: list[EvalResult]) -> dict:
     c_it = np.array([r.cold_it for r in res], float)
-    w_it = np.array([r.warm_it if not r.fallback else r.warm_it + r.cold_it for r in res], float)
+    w_it = np.array([r.warm_its[0] + (r.cold_it if r.fallback else 0) for r in res], float)
+    m_it = np.array([r.ml_its[0] for r in res], float)
     c_ms = np.array([r.cold_ms for r in res])
     w_ms = np.array([r.warm_ms for r in res])
+    m_ms = np.array([r.ml_ms for r in res])
+    top_m = np.array([r.ml_its[-1] for r in res], float)
+    top_w = np.array([r.warm_its[-1] for r in res], float)
     return {
         "problems": len(res),
-        "cold_iters_mean": float(c_it.mean()), "warm_iters_mean": float(w_it.mean()),
-        "cold_ms_mean": float(c_ms.mean()), "warm_ms_mean": float(w_ms.mean()),
+        "cold_iters_mean": float(c_it.mean()),
+        "multilevel_iters_mean": float(m_it.mean()),
+        "warm_iters_mean": float(w_it.mean()),
+        "coarsest_iters_cold_start_mean": float(top_m.mean()),
+        "coarsest_iters_learned_mean": float(top_w.mean()),
+        "cold_ms_mean": float(c_ms.mean()), "multilevel_ms_mean": float(m_ms.mean()),
+        "warm_ms_mean": float(w_ms.mean()),
         "infer_ms_mean": float(np.mean([r.infer_ms for r in res])),
-        "iters_ratio": float(c_it.sum() / w_it.sum()),
-        "wall_ratio": float(c_ms.sum() / w_ms.sum()),
+        "wall_ratio_cold_over_warm": float(c_ms.sum() / w_ms.sum()),
+        "wall_ratio_cold_over_multilevel": float(c_ms.sum() / m_ms.sum()),
+        "wall_ratio_multilevel_over_warm": float(m_ms.sum() / w_ms.sum()),
         "fallbacks": int(sum(r.fallback for r in res)),
-        "regressions": int(sum((not r.fallback) and r.warm_it >= r.cold_it for r in res)),
-        "agree_cold_min": float(min(r.agree_cold for r in res)),
+        "regressions": int(sum((not r.fallback) and r.warm_its[0] >= r.cold_it for r in res)),
         "agree_cold_mean": float(np.mean([r.agree_cold for r in res])),
+        "agree_cold_min": float(min(r.agree_cold for r in res)),
+        "agree_cold_ge_999": int(sum(r.agree_cold >= 0.999 for r in res)),
+        "agree_ml_mean": float(np.mean([r.agree_ml for r in res])),
         "agree_tight_mean": float(np.nanmean([r.agree_tight for r in res])),
         "cold_agree_tight_mean": float(np.nanmean([r.cold_agree_tight for r in res])),
+        **_summary_1e5(res),
     }
+
+
+def _summary_1e5(res) -> dict:
+    ex = [r.extra for r in res if "warm5_ms" in r.extra]
+    if not ex:
+        return {}
+    c = np.array([e["cold5_ms"] for e in ex])
+    w = np.array([e["warm5_ms"] for e in ex])
+    return {"err1e5_cold_ms_mean": float(c.mean()), "err1e5_warm_ms_mean": float(w.mean()),
+            "err1e5_cold_iters_mean": float(np.mean([e["cold5_it"] for e in ex])),
+            "err1e5_warm_iters_mean": float(np.mean([e["warm5_its"][0] for e in ex])),
+            "err1e5_wall_ratio": float(c.sum() / w.sum()),
+            "err1e5_agree_mean": float(np.mean([e["agree5"] for e in ex])),
+            "err1e5_agree_min": float(min(e["agree5"] for e in ex)),
+            "err1e5_agree_ge_999": int(sum(e["agree5"] >= 0.999 for e in ex))}
 
 
 def main(argv=None):
@@ -296,24 +375,33 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", type=int, default=2000, help="training pairs (seeds 0..N-1)")
     ap.add_argument("--eval", type=int, default=200, help="held-out seeds")
-    ap.add_argument("--steps-per-pair", type=int, default=2)
+    ap.add_argument("--level", type=int, default=LEVELS - 1)
+    ap.add_argument("--epochs", type=int, default=16)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--out", type=Path, default=WEIGHTS)
     ap.add_argument("--no-tight", action="store_true")
     ap.add_argument("--eval-only", action="store_true")
+    ap.add_argument("--results", type=Path, default=None, help="per-seed results (JSON)")
     a = ap.parse_args(argv)
     if a.eval_only:
-        net, budget = load(path=a.out)
+        net, budget, level = load(path=a.out)
     else:
-        net, info = train(range(a.train), steps_per_pair=a.steps_per_pair, lr=a.lr)
+        net, info = train(range(a.train), level=a.level, epochs=a.epochs, lr=a.lr)
         save(net, info, a.out)
-        budget = info["cold_budget"]
-        print(json.dumps({"train_pairs": a.train, "cold_budget": budget,
+        budget, level = info["cold_budget"], a.level
+        print(json.dumps({"train_pairs": a.train, "level": level, "cold_budget": budget,
+                          "gen_seconds": round(info["gen_seconds"], 1),
                           "train_seconds": round(info["train_seconds"], 1),
-                          "final_loss": float(np.mean(info["losses"][-50:]))}), flush=True)
-    res = evaluate(net, budget, range(HELDOUT_SEED0, HELDOUT_SEED0 + a.eval),
+                          "final_loss": float(np.mean(info["losses"][-200:]))}), flush=True)
+    res = evaluate(net, budget, range(HELDOUT_SEED0, HELDOUT_SEED0 + a.eval), level=level,
                    tight=not a.no_tight, log=print)
-    print(json.dumps(summarize(res)), flush=True)
+    summary = summarize(res)
+    print(json.dumps(summary), flush=True)
+    if a.results:
+        from dataclasses import asdict
+
+        a.results.write_text(json.dumps({"summary": summary,
+                                         "per_seed": [asdict(r) for r in res]}, indent=1))
 
 
 if __name__ == "__main__":

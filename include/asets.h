@@ -149,6 +149,10 @@ ASETS_API void asets_solver_destroy(asets_solver *s);
 ASETS_API asets_status asets_solver_set_inputs(asets_solver *s, asets_memory where,
                                                const float *Cs, const float *Ct,
                                                const float *alpha);
+/* Copy the current inputs out (any pointer may be NULL); on a coarse level
+ * of a multilevel chain these are the restricted inputs. */
+ASETS_API asets_status asets_solver_get_inputs(asets_solver *s, asets_memory where, float *Cs,
+                                               float *Ct, float *alpha);
 /* Warm start: initial u/ps/pt instead of the reference's init (the flows
  * still start at zero, as calloc'd in runMaxFlow).  Shapes: binary u,ps,pt N;
  * Potts u N*L, ps N, pt N*L; Ishikawa u N*(L-1), pt N*L (ps NULL).  Pass all

@@ -65,6 +65,9 @@ def test_two_level_solve_equals_oracle_transfer(model, dims, L):
     fine.run(k, 0.0, cc, steps, exact=True)
     assert np.array_equal(bits(ml.get_u()), bits(fine.get_u()))
     assert np.array_equal(bits(ml.get_cvg(k)), bits(fine.get_cvg(k)))
+    _, ct_c, al_c = ml.level(1).get_inputs()
+    assert np.array_equal(bits(ct_c), bits(rs(inp["Ct"], 2.0)))
+    assert np.array_equal(bits(al_c), bits(rs(inp["alpha"], 1.0)))
     # the coarse level's own result is the oracle-restricted problem's
     assert np.array_equal(bits(ml.level(1).get_u()), bits(u))
     for s in (ml, co, fine):

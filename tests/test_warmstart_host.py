@@ -17,9 +17,11 @@ def test_device_problem_generator_equals_synth():
 
 def test_summary_counts_fallback_iterations():
     R = warmstart.EvalResult
-    res = [R(1, 300, 120.0, 100, 50.0, 2.0, False, 0.999),
-           R(2, 300, 120.0, 300, 250.0, 2.0, True, 1.0)]
+    res = [R(1, 300, 120.0, [40, 60, 200], 30.0, [38, 50, 90], 25.0, 1.0, False, 0.99, 0.98),
+           R(2, 300, 120.0, [40, 60, 200], 30.0, [310, 50, 90], 250.0, 1.0, True, 1.0, 0.97)]
     s = warmstart.summarize(res)
-    assert s["fallbacks"] == 1
-    assert s["warm_iters_mean"] == (100 + 600) / 2
-    assert abs(s["wall_ratio"] - 240 / 300) < 1e-12
+    assert s["fallbacks"] == 1 and s["regressions"] == 0
+    assert s["warm_iters_mean"] == (38 + 310 + 300) / 2
+    assert s["coarsest_iters_learned_mean"] == 90 and s["coarsest_iters_cold_start_mean"] == 200
+    assert abs(s["wall_ratio_cold_over_warm"] - 240 / 275) < 1e-12
+    assert abs(s["wall_ratio_cold_over_multilevel"] - 4.0) < 1e-12
