@@ -346,10 +346,17 @@ def summarize(res: list[EvalResult]) -> dict:
         "agree_cold_min": float(min(r.agree_cold for r in res)),
         "agree_cold_ge_999": int(sum(r.agree_cold >= 0.999 for r in res)),
         "agree_ml_mean": float(np.mean([r.agree_ml for r in res])),
-        "agree_tight_mean": float(np.nanmean([r.agree_tight for r in res])),
-        "cold_agree_tight_mean": float(np.nanmean([r.cold_agree_tight for r in res])),
+        **_summary_tight(res),
         **_summary_1e5(res),
     }
+
+
+def _summary_tight(res) -> dict:
+    t = [r for r in res if np.isfinite(r.agree_tight)]
+    if not t:
+        return {}
+    return {"agree_tight_mean": float(np.mean([r.agree_tight for r in t])),
+            "cold_agree_tight_mean": float(np.mean([r.cold_agree_tight for r in t]))}
 
 
 def _summary_1e5(res) -> dict:

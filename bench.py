@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solver measurement")
+    ap.add_argument("--warm-seeds", type=int, default=4,
+                    help="held-out Potts problems for the warm-start comparison (0: skip)")
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="run one solve of N iterations of the workload and exit (for ncu)")
     ap.add_argument("--shape", default="256,256,256", help="volume for --profile-iters")
@@ -211,6 +213,27 @@ def batch_run(ctx) -> dict:
     return out
 
 
+def warm_start_run(ctx, nseeds: int) -> dict:
+    """Potts 3D 128^3, L = 6, errBound 1e-4 on held-out seeds: cold start vs
+    the multilevel solve vs the multilevel solve whose coarsest level starts
+    from the trained network (committed weights)."""
+    from asetsmatlabmaxflow_gb300 import warmstart as W
+
+    net, budget, level = W.load(ctx)
+    run = W.Runner(ctx)
+    W.evaluate(net, budget, [W.HELDOUT_SEED0 + 900], level=level, tight=False, run=run)  # warm-up
+    res = W.evaluate(net, budget, range(W.HELDOUT_SEED0, W.HELDOUT_SEED0 + nseeds), level=level,
+                     tight=False, run=run)
+    run.close()
+    net.close()
+    out = W.summarize(res)
+    out["workload"] = ("Potts 3D 128^3 L=6 (means U[0,1], Voronoi 30-80 cells, noise U[.05,.2], "
+                       "alpha U[.1,.5]), cc 0.3, steps 0.11, errBound 1e-4, held-out seeds "
+                       f"{W.HELDOUT_SEED0}..{W.HELDOUT_SEED0 + nseeds - 1}; wall ms per solve")
+    out["levels"] = W.LEVELS
+    return out
+
+
 def cpu_baseline_sample(cs, ct, alpha, iters: int) -> dict:
     """Single-core oracle solve of the same volume for `iters` iterations
     (init included, as the reference's timet)."""
@@ -315,11 +338,23 @@ def main():
     achieved = BYTES_PER_VOXEL_ITER * nvox / (per_launch_ms * 1e-3) / 1e9
     traffic = traffic_per_launch()
 
-    # ---- time to errBound 1e-4 (convergence run)
+    # ---- time to errBound 1e-4 (convergence run): cold start, and the
+    # multilevel (coarse-to-fine) solve; wall time of the synchronous call
+    def timed(fn):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, 1e3 * (time.perf_counter() - t)
+
     s.run(2000, 1e-4, CC, STEPS)
-    conv_ms, conv_launches = s.last_run_stats()
-    conv_it = s.run(2000, 1e-4, CC, STEPS)
+    conv_it, conv_wall = timed(lambda: s.run(2000, 1e-4, CC, STEPS))
     conv_ms, _ = s.last_run_stats()
+    u_cold = s.get_u()
+    s.run_multilevel(3, 2000, 1e-4, CC, STEPS)
+    ml_it, ml_wall = timed(lambda: s.run_multilevel(3, 2000, 1e-4, CC, STEPS))
+    ml_its, ml_dev = s.multilevel_stats()
+    ml_agree = float(np.mean((s.get_u() > 0.5) == (u_cold > 0.5)))
     s.close()
 
     # ---- e2e: the C ABI one-shot call from pinned host buffers
@@ -352,6 +387,7 @@ def main():
     ok = bool(np.isfinite(h_u.numpy()).all())
 
     batch = None if args.no_batch else batch_run(ctx)
+    warm = warm_start_run(ctx, args.warm_seeds) if (rank == 0 and args.warm_seeds > 0) else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -375,7 +411,12 @@ def main():
                          "peak_kind": peak_kind, "kernel": "stencil_col_kernel<3, 16 warps, 4 stages, binary, fast>",
                          "bytes_per_voxel_iter": BYTES_PER_VOXEL_ITER,
                          "launch_ms": per_launch_ms},
-            "time_to_errbound": {"err_bound": 1e-4, "iterations": conv_it, "ms": conv_ms},
+            "time_to_errbound": {"err_bound": 1e-4, "iterations": conv_it, "ms": conv_ms,
+                                 "wall_ms": conv_wall,
+                                 "multilevel": {"levels": len(ml_its), "iterations": ml_its,
+                                                "device_ms": ml_dev, "wall_ms": ml_wall,
+                                                "label_agreement_with_cold": ml_agree}},
+            "warm_start": warm,
             "clocks": clk.summary(),
             "gpu_launches": launches,
             "batch": batch,
