@@ -41,7 +41,6 @@ CU_SOURCES = (
     "flow3d.cu",
     "flow2d.cu",
     "label_kernels.cu",
-    "batch.cu",
     "noalloc.cu",
     "conv_tc.cu",
     "warmstart.cu",

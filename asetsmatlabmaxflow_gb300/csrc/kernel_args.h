@@ -46,26 +46,6 @@ enum Epilogue : int {
     EPI_DIV = 1,     // multi-label models: write the new flow and its divergence
 };
 
-struct StencilArgs {
-    CUtensorMap map[2][NUM_SLOTS];  // [parity of the source buffers][slot]
-    float *dst_b[2][3];             // [source parity][SL_BC, SL_BR, SL_BS]
-    float *dst_s[2][3];             // binary: ps, pt, u; EPI_DIV: [.][0] = divergence
-    const float *cs;                // binary source/sink capacities (padded layout)
-    const float *ct;
-    IterControl *ctl;
-    double *partials;               // one per block
-    float *cvg;
-    long long pitch;                // padded row pitch (elements)
-    long long plane_stride;         // pitch * nc
-    long long label_stride;         // plane_stride * ns
-    long long total_work;           // labels * tiles * ns tile-planes
-    int nr, nc, ns;                 // rows, columns (1 in 2D), stream length
-    int nlab_items;                 // labels swept by this launch
-    int tiles_r, tiles_c;
-    int lab_mul[NUM_SLOTS];         // label coordinate of slot = k*mul + add
-    int lab_add[NUM_SLOTS];
-    float cc, inv_cc, steps;
-};
 
 // Arguments of the column-per-thread iteration kernel (stencil2_kernel.cuh).
 // Halo slots are SL_BC..SL_ALPHA at the step's plane; tile slots carry the
