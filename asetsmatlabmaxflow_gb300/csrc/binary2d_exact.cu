@@ -1,0 +1,19 @@
+// Compiled instances of the fused iteration kernel for the binary model (ps/pt/u
+// epilogue), 2D tiles 224-row, 56-row; EXACT projection, built with the reference's
+// float arithmetic (no FMA contraction, no flush to zero).
+#include "variants.cuh"
+
+namespace asets {
+
+static const StencilVariant kVariants[] = {
+    make_variant<2, 8, 4, EPI_BINARY, true>(),
+    make_variant<2, 2, 4, EPI_BINARY, true>(),
+};
+
+const StencilVariant *binary2d_exact_variants(int *count)
+{
+    *count = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
+    return kVariants;
+}
+
+}  // namespace asets

@@ -1,0 +1,19 @@
+// Compiled instances of the fused iteration kernel for the labelled models (divergence
+// epilogue), 2D tiles 224-row, 56-row; fast projection, built with FMA contraction and
+// flush to zero (held to the parity tolerance, not bit-exactness).
+#include "variants.cuh"
+
+namespace asets {
+
+static const StencilVariant kVariants[] = {
+    make_variant<2, 8, 4, EPI_DIV, false>(),
+    make_variant<2, 2, 4, EPI_DIV, false>(),
+};
+
+const StencilVariant *flow2d_fast_variants(int *count)
+{
+    *count = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
+    return kVariants;
+}
+
+}  // namespace asets

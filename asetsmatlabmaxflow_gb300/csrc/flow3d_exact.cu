@@ -1,17 +1,16 @@
-// Compiled instances of the fused iteration kernel: 3D tiles of 28 x 12 (16 warps) and 28 x 8 (12 warps),
-// fast and EXACT projection.
+// Compiled instances of the fused iteration kernel for the labelled models (divergence
+// epilogue), 3D tiles 28 x 12, 28 x 8; EXACT projection, built with the reference's
+// float arithmetic (no FMA contraction, no flush to zero).
 #include "variants.cuh"
 
 namespace asets {
 
 static const StencilVariant kVariants[] = {
-    make_variant<3, 16, 4, EPI_DIV, false>(),
     make_variant<3, 16, 4, EPI_DIV, true>(),
-    make_variant<3, 12, 4, EPI_DIV, false>(),
     make_variant<3, 12, 4, EPI_DIV, true>(),
 };
 
-const StencilVariant *flow3d_variants(int *count)
+const StencilVariant *flow3d_exact_variants(int *count)
 {
     *count = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
     return kVariants;

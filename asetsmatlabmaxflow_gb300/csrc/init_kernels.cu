@@ -126,4 +126,28 @@ cudaError_t launch_validate_alpha(const InitArgs &a, int num_sms, cudaStream_t s
     return cudaGetLastError();
 }
 
+// Self-check of the bounded wait: one thread arms an mbarrier for 16 bytes
+// of transaction that no copy will deliver and waits on it with the solver
+// kernels' bounded wait, which must give up after its budget and report
+// DEV_ERR_TIMEOUT.  Nothing is in flight when the kernel returns.
+__global__ void wait_selftest_kernel(int *err)
+{
+    __shared__ uint64_t bar;
+    __shared__ int abort_flag;
+    if (threadIdx.x == 0) {
+        abort_flag = 0;
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+        mbar_arrive_expect_tx(&bar, 16);
+        if (!mbar_wait_bounded(&bar, 0, &abort_flag))
+            atomicOr(err, DEV_ERR_TIMEOUT);
+    }
+}
+
+cudaError_t launch_wait_selftest(int *d_err, cudaStream_t st)
+{
+    wait_selftest_kernel<<<1, 32, 0, st>>>(d_err);
+    return cudaGetLastError();
+}
+
 }  // namespace asets

@@ -55,10 +55,24 @@ int choose_zchunks(const StencilProblem &p, const StencilVariant &v, long long s
 int problem_items(const StencilProblem &p, const StencilVariant &v, int zchunks);
 
 // Variant tables, one per translation unit.
-const StencilVariant *binary3d_variants(int *count);
-const StencilVariant *binary2d_variants(int *count);
-const StencilVariant *flow3d_variants(int *count);
-const StencilVariant *flow2d_variants(int *count);
+const StencilVariant *binary3d_fast_variants(int *count);
+const StencilVariant *binary3d_exact_variants(int *count);
+const StencilVariant *binary2d_fast_variants(int *count);
+const StencilVariant *binary2d_exact_variants(int *count);
+const StencilVariant *flow3d_fast_variants(int *count);
+const StencilVariant *flow3d_exact_variants(int *count);
+const StencilVariant *flow2d_fast_variants(int *count);
+const StencilVariant *flow2d_exact_variants(int *count);
+// The compiled variants of one kind (dimension, epilogue, EXACT or fast);
+// tile_config k >= 1 selects entry k-1.
+inline const StencilVariant *stencil_variants(int dim, int epi, int exact, int *count)
+{
+    if (dim == 3)
+        return epi == EPI_BINARY ? (exact ? binary3d_exact_variants(count) : binary3d_fast_variants(count))
+                                 : (exact ? flow3d_exact_variants(count) : flow3d_fast_variants(count));
+    return epi == EPI_BINARY ? (exact ? binary2d_exact_variants(count) : binary2d_fast_variants(count))
+                             : (exact ? flow2d_exact_variants(count) : flow2d_fast_variants(count));
+}
 
 // ---------------------------------------------------------------- labels
 struct LabelArgs {
@@ -95,6 +109,7 @@ struct InitArgs {
 
 cudaError_t launch_init(int model, const InitArgs &a, int num_sms, cudaStream_t st);
 cudaError_t launch_validate_alpha(const InitArgs &a, int num_sms, cudaStream_t st);
+cudaError_t launch_wait_selftest(int *d_err, cudaStream_t st);
 
 // Message returned by asets_last_error() on the calling thread.
 void set_last_error(const char *msg);

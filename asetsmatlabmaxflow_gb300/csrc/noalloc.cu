@@ -237,11 +237,8 @@ extern "C" ASETS_API asets_status asets_binary_mf3d_noalloc(
     // kernel variant and arguments (the same fused kernel as the other entry points)
     const int exact = (flags & ASETS_FLAG_EXACT) ? 1 : 0;
     int nv = 0;
-    const StencilVariant *tab = binary3d_variants(&nv);
-    const StencilVariant *v = nullptr;
-    for (int i = 0; i < nv && !v; ++i)
-        if (tab[i].exact == exact)
-            v = &tab[i];
+    const StencilVariant *tab = stencil_variants(3, EPI_BINARY, exact, &nv);
+    const StencilVariant *v = nv > 0 ? &tab[0] : nullptr;
     if (!v)
         return na_fail(ASETS_ERR_UNSUPPORTED, "no kernel variant");
     StencilProblem p;

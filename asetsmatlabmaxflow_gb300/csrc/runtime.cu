@@ -262,6 +262,30 @@ extern "C" ASETS_API asets_status asets_default_context(asets_context **out)
     return ASETS_OK;
 }
 
+extern "C" ASETS_API asets_status asets_selftest_wait_timeout(asets_context *ctx)
+{
+    if (!ctx)
+        return fail(ASETS_ERR_INVALID_ARG, "ctx is NULL");
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    DeviceGuard guard(ctx->device);
+    int *d_err = nullptr;
+    CU_TRY(cudaMallocAsync(&d_err, sizeof(int), ctx->stream));
+    int h_err = 0;
+    cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream);
+    if (e == cudaSuccess)
+        e = launch_wait_selftest(d_err, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaFreeAsync(d_err, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess)
+        return cuda_fail(e, "wait self-test");
+    if (h_err & DEV_ERR_TIMEOUT)
+        return fail(ASETS_ERR_TIMEOUT, "a device-side wait timed out (self-test)");
+    return fail(ASETS_ERR_CUDA, "the self-test wait did not time out");
+}
+
 extern "C" ASETS_API asets_status asets_context_set_stream(asets_context *ctx, void *stream)
 {
     if (!ctx)
@@ -315,16 +339,11 @@ static long long round_pitch(int nr)
 static const StencilVariant *pick_variant(const asets_solver *s, int exact, int tile_config)
 {
     int n = 0;
-    const StencilVariant *tab;
-    const bool binary = (s->model == ASETS_BINARY);
-    if (s->dim == 3)
-        tab = binary ? binary3d_variants(&n) : flow3d_variants(&n);
-    else
-        tab = binary ? binary2d_variants(&n) : flow2d_variants(&n);
+    const StencilVariant *tab = stencil_variants(s->dim, s->model == ASETS_BINARY ? EPI_BINARY : EPI_DIV,
+                                                 exact, &n);
     std::vector<const StencilVariant *> match;
     for (int i = 0; i < n; ++i)
-        if (tab[i].exact == exact)
-            match.push_back(&tab[i]);
+        match.push_back(&tab[i]);
     if (match.empty())
         return nullptr;
     if (tile_config > 0 && tile_config <= (int)match.size())
@@ -1502,13 +1521,10 @@ static asets_status batch_autotune(asets_batch *b, int flags, float cc, float st
                 continue;
         }
         int n = 0;
-        if (gi == 1)
-            binary3d_variants(&n);
-        else
-            binary2d_variants(&n);
+        stencil_variants(gi == 1 ? 3 : 2, EPI_BINARY, (flags & ASETS_FLAG_EXACT) ? 1 : 0, &n);
         int best = 1;
         float best_ms = 1e30f;
-        for (int cand = 1; cand <= n / 2; ++cand) {
+        for (int cand = 1; cand <= n; ++cand) {
             int tc[2] = {tile_config[0], tile_config[1]};
             tc[gi] = cand;
             asets_status st = batch_prepare(b, flags, tc, kGraphIters, 0.0f, cc, steps);

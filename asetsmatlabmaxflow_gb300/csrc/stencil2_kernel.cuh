@@ -316,29 +316,55 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         float gkprev = 0.f, bsprev = 0.f, g2prev = 1.f, alpha_prev = 1.f;
         float br_prev = 0.f, bc_prev = 0.f, bss_cur = 0.f, bss_old = 0.f, dvp = 0.f;
 
-        for (int t = 0; t < n_steps; ++t) {
-            const int s = p_first + t;
-            const int st_cur = (q0 + t) % NSTAGE, st_nxt = (q0 + t + 1) % NSTAGE;
+        // A wait gave up: drain this item's loads [first, issued) (bounded),
+        // record the error and leave the item.
+        auto abort_item = [&](int first, int issued) {
+            if (producer) {
+                s_abort = 0;
+                for (int j = first; j < issued; ++j) {
+                    const unsigned int q = q0 + j;
+                    mbar_wait_bounded(&bars[q % NSTAGE], (q / NSTAGE) & 1, &s_abort);
+                }
+                atomicOr(&ctl->error, DEV_ERR_TIMEOUT);
+            }
+            __syncthreads();
+        };
+        // Step t reads the stages of planes t and t+1.  Labelled models
+        // (kEarly): the stage is not read after X, so step t refills its own
+        // slot with plane t+NSTAGE, the first two stages arrive here and every
+        // later one before the Y barrier two steps ahead (two barriers per
+        // step).  Binary: Z reads the stage's tile boxes, so step t refills the
+        // slot of plane t-1 and waits for its stages at the top (three).
+        constexpr bool kEarly = (EPI == EPI_DIV);
+        constexpr int kLead = kEarly ? NSTAGE : NSTAGE - 1;
+        if constexpr (kEarly) {
             bool ok = true;
             if (producer) {
-                ok = mbar_wait_bounded(&bars[st_cur], ((q0 + t) / NSTAGE) & 1, &s_abort);
-                ok = ok && mbar_wait_bounded(&bars[st_nxt], ((q0 + t + 1) / NSTAGE) & 1, &s_abort);
+                ok = mbar_wait_bounded(&bars[q0 % NSTAGE], (q0 / NSTAGE) & 1, &s_abort);
+                ok = ok && mbar_wait_bounded(&bars[(q0 + 1) % NSTAGE], ((q0 + 1) / NSTAGE) & 1, &s_abort);
             }
-            // the barrier publishes the completed stages to every thread
             if (__syncthreads_or(!ok)) {
                 aborted = true;
+                abort_item(0, min(NSTAGE, n_loads));
+            }
+        }
+
+        for (int t = 0; t < n_steps && !aborted; ++t) {
+            const int s = p_first + t;
+            const int st_cur = (q0 + t) % NSTAGE, st_nxt = (q0 + t + 1) % NSTAGE;
+            if constexpr (!kEarly) {
+                bool ok = true;
                 if (producer) {
-                    s_abort = 0;
-                    // loads issued so far: the prologue, then one per step from t = 1
-                    const int issued = min(n_loads, (t >= 1) ? t + NSTAGE - 1 : NSTAGE);
-                    for (int j = t; j < issued; ++j) {
-                        const unsigned int q = q0 + j;
-                        mbar_wait_bounded(&bars[q % NSTAGE], (q / NSTAGE) & 1, &s_abort);
-                    }
-                    atomicOr(&ctl->error, DEV_ERR_TIMEOUT);
+                    ok = mbar_wait_bounded(&bars[st_cur], ((q0 + t) / NSTAGE) & 1, &s_abort);
+                    ok = ok && mbar_wait_bounded(&bars[st_nxt], ((q0 + t + 1) / NSTAGE) & 1, &s_abort);
                 }
-                __syncthreads();
-                break;
+                // the barrier publishes the completed stages to every thread
+                if (__syncthreads_or(!ok)) {
+                    aborted = true;
+                    // loads issued: the prologue, then one per step from t = 1
+                    abort_item(t, min(n_loads, (t >= 1) ? t + NSTAGE - 1 : NSTAGE));
+                    break;
+                }
             }
             const bool s_in = (s >= 0 && s < ns);
             const bool sb_in = (s >= 1 && s < ns);          // stream face s is interior
@@ -372,9 +398,9 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             }
             __syncthreads();
 
-            // refill the slot of plane s-1 (its last readers finished before the barrier)
-            if (producer && t >= 1 && t + NSTAGE - 1 < n_loads)
-                issue_load(t + NSTAGE - 1);
+            // refill a slot whose last readers finished before the barrier
+            if (producer && (kEarly || t >= 1) && t + kLead < n_loads)
+                issue_load(t + kLead);
 
             // ---- Y: gradient step b'(s), projection g2(s-1), stream faces b''(s-1)
             const float gk_up = __shfl_up_sync(0xffffffffu, gk, 1);
@@ -407,7 +433,23 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             g2prev = g2;
             bsprev = bsn;
             alpha_prev = alpha_cur;
-            __syncthreads();
+            if constexpr (kEarly) {
+                // the stage of plane s+2 (read by the next step's X) arrives
+                // before this barrier, which also publishes Y's shared planes
+                bool ok = true;
+                if (producer && t + 2 < n_loads) {
+                    const unsigned int q = q0 + t + 2;
+                    ok = mbar_wait_bounded(&bars[q % NSTAGE], (q / NSTAGE) & 1, &s_abort);
+                }
+                if (__syncthreads_or(!ok)) {
+                    aborted = true;
+                    // loads issued: the prologue, then one per step
+                    abort_item(t + 2, min(n_loads, t + NSTAGE + 1));
+                    break;
+                }
+            } else {
+                __syncthreads();
+            }
 
             // ---- Z: row/column faces of plane s-1 and the output of plane s-2
             {

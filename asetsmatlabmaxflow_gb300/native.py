@@ -97,6 +97,7 @@ _SIGS = {
     "asets_solver_multilevel_prepare": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "asets_solver_level": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(_VP)]),
     "asets_solver_multilevel_stats": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, ctypes.POINTER(ctypes.c_int)]),
+    "asets_selftest_wait_timeout": (ctypes.c_int, [_VP]),
     "asets_solver_get_inputs": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
     "asets_solver_set_initial_flows": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
     "asets_solver_get_spatial_flows": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),

@@ -84,6 +84,12 @@ ASETS_API asets_status asets_default_context(asets_context **out);
 /* Launch on this CUDA stream (a cudaStream_t passed as void*, or NULL for the
  * context's own stream). */
 ASETS_API asets_status asets_context_set_stream(asets_context *ctx, void *stream);
+/* Failure-detection self-check (no counterpart in the reference): runs one
+ * kernel whose bounded device-side wait (the kind every solver kernel uses on
+ * its TMA and tensor-core completions) waits on a barrier that nothing
+ * completes.  Expected result: ASETS_ERR_TIMEOUT after about one second, with
+ * the context still usable. */
+ASETS_API asets_status asets_selftest_wait_timeout(asets_context *ctx);
 
 /* ------------------------------------------------------------------------
  * One-shot solvers with host pointers: the runMaxFlow() of each mex file,

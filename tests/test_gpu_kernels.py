@@ -30,3 +30,30 @@ def test_reciprocal_division_is_correctly_rounded_for_all_dividends(div_lib, d):
     f = ctypes.c_uint(0)
     assert div_lib.div_check(d, ctypes.byref(m), ctypes.byref(f)) == 0
     assert m.value == 0, f"{m.value} mismatches, first dividend bits {f.value:#010x}"
+
+
+def test_bounded_wait_times_out_and_context_survives():
+    """A device-side wait on a barrier that nothing completes gives up after
+    its budget, the host gets ASETS_ERR_TIMEOUT, and the next solve on the
+    same context runs normally."""
+    import time
+
+    import numpy as np
+
+    from asetsmatlabmaxflow_gb300 import native as N
+
+    ctx = N.Context.default()
+    t0 = time.perf_counter()
+    st = N.lib().asets_selftest_wait_timeout(ctx.handle)
+    dt = time.perf_counter() - t0
+    assert st == N.ASETS_ERR_TIMEOUT, N.lib().asets_last_error()
+    assert 0.9 < dt < 10.0
+    g = np.random.default_rng(0)
+    n = 24 * 20 * 8
+    img = g.random(n).astype(np.float32)
+    s = N.Solver(ctx, "binary", (24, 20, 8))
+    s.set_inputs(np.abs(img - 0.8).astype(np.float32), np.full(n, 0.3, np.float32),
+                 np.abs(img - 0.2).astype(np.float32))
+    it = s.run(50, 1e-4, 0.35, 0.11)
+    assert 0 < it <= 50 and np.all(np.isfinite(s.get_u()))
+    s.close()
