@@ -86,8 +86,10 @@ struct LabelArgs {
     float *cvg;
     long long cells;         // padded cells per label
     long long label_stride;  // == cells
+    unsigned int rows;       // padded rows per label (cells / pitch)
     int pitch, nr, nlab;
     float cc, inv_cc, inv_cc_l;  // 1/cc and 1/(cc*L) as the reference rounds them
+    int exact;               // 1: the reference's divisions; 0: reciprocal multiplies
 };
 
 int label_kernel_grid(long long cells, int num_sms);

@@ -826,6 +826,8 @@ static LabelArgs label_args(asets_solver *s)
     a.inv_cc = s->desc.inv_cc;
     // `1/(cc*nLab)` of updatePSU: cc*nLab rounded to float, then divided
     a.inv_cc_l = 1.0f / (s->desc.cc * (float)s->nlab);
+    a.rows = (unsigned int)(s->cells / s->pitch);
+    a.exact = s->variant ? s->variant->exact : 1;
     return a;
 }
 
