@@ -20,8 +20,9 @@
 //   Z: b''_r, b''_c of plane s-1; ps/pt/u (or div) of s-2    tile
 // with two block barriers per step.  Old-state planes come through a ring of
 // 4D TMA tiled loads; a stage holds the halo boxes of its plane and, for the
-// binary model, tile boxes of ps/pt/u/Cs/Ct two planes behind, which is the
-// plane the step writes.  Out-of-grid elements load as 0: the zero-flux
+// binary model, tile boxes of ps/pt/u/Cs/Ct three planes behind: step t reads
+// them from the stage of plane s+1 (the plane s-2 it writes), which stays
+// resident until the next step's X.  Out-of-grid elements load as 0: the zero-flux
 // border of the reference.
 //
 // Work split: each problem's (label, stream chunk, tile) items, ordered
@@ -283,7 +284,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             if constexpr (EPI == EPI_BINARY) {
 #pragma unroll
                 for (int ts = 0; ts < NUM_TILE_SLOTS; ++ts)
-                    tma_load_4d(tile_slot(st, ts), &tmaps[ts], r0, c0, plane - 2, 0, &bars[st]);
+                    tma_load_4d(tile_slot(st, ts), &tmaps[ts], r0, c0, plane - 3, 0, &bars[st]);
             }
         };
         if (producer)
@@ -329,14 +330,15 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             }
             __syncthreads();
         };
-        // Step t reads the stages of planes t and t+1.  Labelled models
-        // (kEarly): the stage is not read after X, so step t refills its own
-        // slot with plane t+NSTAGE, the first two stages arrive here and every
-        // later one before the Y barrier two steps ahead (two barriers per
-        // step).  Binary: Z reads the stage's tile boxes, so step t refills the
-        // slot of plane t-1 and waits for its stages at the top (three).
-        constexpr bool kEarly = (EPI == EPI_DIV);
-        constexpr int kLead = kEarly ? NSTAGE : NSTAGE - 1;
+        // Step t reads the stages of planes t and t+1 (X; the binary Z also
+        // reads the tile boxes of stage t+1), so after the X barrier no one
+        // reads stage t any more and step t refills its slot with plane
+        // t+NSTAGE.  Labelled models (kEarly): the first two stages arrive
+        // here and every later one before the Y barrier two steps ahead (two
+        // barriers per step).  Binary: its larger stages are waited for at the
+        // top of the step that first reads them (three barriers per step).
+        constexpr bool kEarly = (EPI == EPI_DIV);   // wait before the Y barrier
+        constexpr int kLead = NSTAGE;                // refill the slot read by this X
         if constexpr (kEarly) {
             bool ok = true;
             if (producer) {
@@ -361,8 +363,8 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                 // the barrier publishes the completed stages to every thread
                 if (__syncthreads_or(!ok)) {
                     aborted = true;
-                    // loads issued: the prologue, then one per step from t = 1
-                    abort_item(t, min(n_loads, (t >= 1) ? t + NSTAGE - 1 : NSTAGE));
+                    // loads issued: the prologue, then one per earlier step
+                    abort_item(t, min(n_loads, t + NSTAGE));
                     break;
                 }
             }
@@ -399,7 +401,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             __syncthreads();
 
             // refill a slot whose last readers finished before the barrier
-            if (producer && (kEarly || t >= 1) && t + kLead < n_loads)
+            if (producer && t + kLead < n_loads)
                 issue_load(t + kLead);
 
             // ---- Y: gradient step b'(s), projection g2(s-1), stream faces b''(s-1)
@@ -480,7 +482,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                         dv = dv - bss_old;
                         const unsigned int o = col_off + (unsigned int)so * plane_stride;
                         if constexpr (EPI == EPI_BINARY) {
-                            const float *T = stages + st_cur * (SB / 4) + OFF_T0 + ti;
+                            const float *T = stages + st_nxt * (SB / 4) + OFF_T0 + ti;
                             const float pt = T[TS_S1 * TSZ];
                             const float u = T[TS_S2 * TSZ];
                             const float csv = T[TS_CS * TSZ];
