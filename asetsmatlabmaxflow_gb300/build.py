@@ -54,6 +54,7 @@ CU_SOURCES = (
     "conv_tc.cu",
     "warmstart.cu",
     "multilevel.cu",
+    "costs.cu",
 )
 
 MEX_SOLVERS = (

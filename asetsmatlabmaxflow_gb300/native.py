@@ -98,6 +98,16 @@ _SIGS = {
     "asets_solver_level": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(_VP)]),
     "asets_solver_multilevel_stats": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, ctypes.POINTER(ctypes.c_int)]),
     "asets_selftest_wait_timeout": (ctypes.c_int, [_VP]),
+    "asets_cost_l1": (ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.c_longlong, _VP, ctypes.c_int,
+                                     ctypes.c_int, _VP]),
+    "asets_cost_neglog": (ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.c_longlong, ctypes.c_int,
+                                         ctypes.c_float, _VP]),
+    "asets_cost_histogram_ll": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, ctypes.c_longlong,
+                                               ctypes.c_int, ctypes.c_double, _VP, _VP]),
+    "asets_alpha_contrast": (ctypes.c_int, [_VP, ctypes.c_int, _VP, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                            ctypes.c_float, ctypes.c_float, ctypes.c_int,
+                                            ctypes.c_int, _VP]),
     "asets_solver_get_inputs": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
     "asets_solver_set_initial_flows": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
     "asets_solver_get_spatial_flows": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),

@@ -303,6 +303,43 @@ ASETS_API asets_status asets_wsnet_train_step(asets_wsnet *n, int Ny, int Nx, in
                                               float lr, float *loss);
 
 /* ------------------------------------------------------------------------
+ * Cost terms and regularisation weights on the GPU: the step before the
+ * solvers in the reference's applications (applications/*.m; no counterpart
+ * in its C code).  Arrays in Matlab layout, label slowest; `where` says
+ * whether the pointers are host or device memory.  Normalisation divides by
+ * the volume's own range, (I - min I) / (max I - min I), in float32.
+ * ---------------------------------------------------------------------- */
+/* L1 intensity cost (L1IntensitySegmentation2D.m:32-45): Ct_l = |I' - m_l|,
+ * I' the normalised image (normalize != 0) or I itself; 1 <= L <= 32. */
+ASETS_API asets_status asets_cost_l1(asets_context *ctx, asets_memory where, const float *img,
+                                     long long n, const float *models, int L, int normalize,
+                                     float *Ct);
+/* -log probability cost (atlasProbabilityMapsRegularization3D.m:45-53):
+ * Ct = -log(p + eps) for N*L probabilities. */
+ASETS_API asets_status asets_cost_neglog(asets_context *ctx, asets_memory where,
+                                         const float *prob, long long n, int L, float eps,
+                                         float *Ct);
+/* Histogram log-likelihood cost (interactiveGraphCutSegmentation3D.m:104-122):
+ * x = I' * 255; for each label l = 1..L the 256-bin histogram of x over the
+ * voxels with scribbles == l (bin k holds k <= x < k+1, the last also
+ * x == 255, as histc on 0:255), normalised to probabilities P_l; then
+ * Ct_l = -log10(P_l[round(x)] + eps) (round half away from zero, as
+ * uint16()).  hist_out (host, L*256, may be NULL) receives the counts. */
+ASETS_API asets_status asets_cost_histogram_ll(asets_context *ctx, asets_memory where,
+                                               const float *img, const int *scribbles,
+                                               long long n, int L, double eps, float *Ct,
+                                               unsigned int *hist_out);
+/* Contrast-sensitive regularisation weight (smoothManualSegmentations2D.m:82-91;
+ * the binary 3D workload's alpha): alpha = a + b*exp(-c*|grad I'|^p), p = 2
+ * if squared else 1, gradient as Matlab's gradient (central differences
+ * inside, one-sided at the border, 2D when Nz == 1), replicated over L
+ * slices. */
+ASETS_API asets_status asets_alpha_contrast(asets_context *ctx, asets_memory where,
+                                            const float *img, int Ny, int Nx, int Nz,
+                                            int normalize, float a, float b, float c, int squared,
+                                            int L, float *alpha);
+
+/* ------------------------------------------------------------------------
  * Allocation-free binary 3D solve.  No counterpart in the reference: it
  * exists for callers that cannot allocate device memory while they run -- a
  * host whose GPU memory is owned by another allocator (a framework's caching
