@@ -55,6 +55,7 @@ CU_SOURCES = (
     "warmstart.cu",
     "multilevel.cu",
     "costs.cu",
+    "starshape.cu",
 )
 
 MEX_SOLVERS = (

@@ -303,6 +303,23 @@ ASETS_API asets_status asets_wsnet_train_step(asets_wsnet *n, int Ny, int Nx, in
                                               float lr, float *loss);
 
 /* ------------------------------------------------------------------------
+ * Star-shape Potts 2D (maxflow/asetsPotts2D_starShape.m, a Matlab solver:
+ * no counterpart in the reference's C code).  Same arguments as the .m
+ * function, computed in double precision as Matlab does: Ct, alpha
+ * rows x cols x nlab (host, Matlab layout); init_points nlab x 2 of 1-based
+ * (column, row) seed points (ss_initPoints); pars = [rows, cols, nlab,
+ * iterNum, beta, cc, steps, stepv].  Outputs u (rows*cols*nlab), erriter
+ * (iterNum, zero after the break), itNum = the 1-based iteration of the
+ * break (erriter < beta) or iterNum, seconds = wall time.
+ * ---------------------------------------------------------------------- */
+ASETS_API asets_status asets_potts2d_starshape(asets_context *ctx, const double *Ct,
+                                               const double *alpha, int rows, int cols,
+                                               int nlab, int iterNum, double beta, double cc,
+                                               double steps, double stepv,
+                                               const int *init_points, double *u,
+                                               double *erriter, int *itNum, float *seconds);
+
+/* ------------------------------------------------------------------------
  * Cost terms and regularisation weights on the GPU: the step before the
  * solvers in the reference's applications (applications/*.m; no counterpart
  * in its C code).  Arrays in Matlab layout, label slowest; `where` says
