@@ -56,6 +56,7 @@ CU_SOURCES = (
     "multilevel.cu",
     "costs.cu",
     "starshape.cu",
+    "hmf.cu",
 )
 
 MEX_SOLVERS = (

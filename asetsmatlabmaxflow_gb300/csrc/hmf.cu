@@ -1,0 +1,505 @@
+// Hierarchical max-flow (HMF), full-flow iteration, 2D and 3D: the GPU form
+// of maxflow/asetsHMF2D.m / asetsHMF3D.m (MaxFullFlow), a Matlab class in
+// the reference computing in the class of its cost terms (single or double),
+// here templated on that type with the .m files' evaluation order.
+//
+// The label hierarchy is a tree of nodes listed in pre-order (every parent
+// before its children, children in their order).  Per iteration:
+//   K1 per pixel, all nodes: sink flows children-first (UpdateSinkFlows),
+//      then the labels (UpdateLabels), then g = steps*(div + pt - P.pt - u/cc)
+//      of every non-root node (the first line of UpdateSpatialFlows) -- all
+//      per-pixel, so one pass;
+//   K2 gradient step of the spatial flows, K3 flow magnitude and projection
+//   factor, K4 flow rescale, K5 divergence (the rest of UpdateSpatialFlows).
+// Costs (CalculateCostsFullFlow) are summed on the device in double.
+// Not built: the anisotropic lx/ly branch and MaxPseudoFlow.
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "asets.h"
+#include "internal.h"
+
+using namespace asets;
+
+namespace {
+
+constexpr int kThreads = 256;
+
+template <class T>
+struct NodeDev {
+    const T *ct;     // leaves
+    const T *alpha;  // per-pixel alpha or null
+    T alpha_s;       // scalar alpha
+    int parent, child_begin, nchild;
+};
+
+template <class T>
+struct HArgs {
+    int dim, d1, d2, d3, m;
+    long long n, f1, f2, f3;  // cells and face counts per node
+    T cc, steps, inv_cc;      // inv_cc: 1/cc formed in double (the root's 1/cc .* ones)
+    const NodeDev<T> *nodes;
+    const int *children;
+    T *pt, *u, *div, *g, *p1, *p2, *p3;
+    double *cost;  // [m][2]: sum u*Ct (leaves), sum u*div (non-root)
+};
+
+template <class T> __device__ __forceinline__ T add(T a, T b);
+template <class T> __device__ __forceinline__ T sub(T a, T b);
+template <class T> __device__ __forceinline__ T mul(T a, T b);
+template <class T> __device__ __forceinline__ T dvd(T a, T b);
+template <class T> __device__ __forceinline__ T sqr(T a);
+template <> __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+template <> __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+template <> __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+template <> __device__ __forceinline__ float dvd(float a, float b) { return __fdiv_rn(a, b); }
+template <> __device__ __forceinline__ float sqr(float a) { return __fsqrt_rn(a); }
+template <> __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+template <> __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+template <> __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+template <> __device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+template <> __device__ __forceinline__ double sqr(double a) { return __dsqrt_rn(a); }
+
+// pixel c = (z*d2 + x)*d1 + y; face arrays: p1 (d1-1) x d2 x d3, p2
+// d1 x (d2-1) x d3, p3 d1 x d2 x (d3-1), each face indexed by the pixel
+// before it along its axis.
+template <class T>
+struct Pix {
+    int y, x, z;
+    long long c;
+    __device__ Pix(const HArgs<T> &A, long long c_) : c(c_)
+    {
+        y = (int)(c % A.d1);
+        const long long q = c / A.d1;
+        x = (int)(q % A.d2);
+        z = (int)(q / A.d2);
+    }
+};
+template <class T>
+__device__ __forceinline__ long long i1(const HArgs<T> &A, int y, int x, int z)
+{
+    return ((long long)z * A.d2 + x) * (A.d1 - 1) + y;
+}
+template <class T>
+__device__ __forceinline__ long long i2(const HArgs<T> &A, int y, int x, int z)
+{
+    return ((long long)z * (A.d2 - 1) + x) * A.d1 + y;
+}
+template <class T>
+__device__ __forceinline__ long long i3(const HArgs<T> &A, int y, int x, int z)
+{
+    return ((long long)z * A.d2 + x) * A.d1 + y;
+}
+
+#define H_LOOP(total)                                                                  \
+    for (long long t = blockIdx.x * (long long)kThreads + threadIdx.x; t < (total);    \
+         t += (long long)gridDim.x * kThreads)
+
+template <class T>
+__global__ void k1_pointwise(const HArgs<T> A)
+{
+    H_LOOP(A.n)
+    {
+        const long long c = t;
+        // sink flows, children before parents (pre-order reversed); a node
+        // reads its parent's pt before the parent is updated
+        for (int i = A.m - 1; i >= 0; --i) {
+            const NodeDev<T> nd = A.nodes[i];
+            const long long o = (long long)i * A.n + c;
+            T acc;
+            if (nd.parent >= 0)
+                acc = add(sub(A.pt[(long long)nd.parent * A.n + c], A.div[o]), dvd(A.u[o], A.cc));
+            else
+                acc = A.inv_cc;
+            if (nd.nchild == 0) {
+                const T ct = nd.ct[c];
+                A.pt[o] = (ct <= acc || ct != ct) ? ct : acc;
+                continue;
+            }
+            for (int j = 0; j < nd.nchild; ++j) {
+                const long long oc = (long long)A.children[nd.child_begin + j] * A.n + c;
+                acc = sub(add(add(acc, A.pt[oc]), A.div[oc]), dvd(A.u[oc], A.cc));
+            }
+            A.pt[o] = dvd(acc, (T)(nd.parent >= 0 ? 1 + nd.nchild : nd.nchild));
+        }
+        // labels, then the flow-gradient input g of every non-root node
+        for (int i = 1; i < A.m; ++i) {
+            const long long o = (long long)i * A.n + c;
+            const T ptp = A.pt[(long long)A.nodes[i].parent * A.n + c];
+            const T dv = A.div[o], pt = A.pt[o];
+            const T u = add(A.u[o], mul(A.cc, sub(sub(ptp, dv), pt)));
+            A.u[o] = u;
+            A.g[o] = mul(A.steps, sub(sub(add(dv, pt), ptp), dvd(u, A.cc)));
+        }
+    }
+}
+
+template <class T>
+__global__ void k2_gradient(const HArgs<T> A)
+{
+    H_LOOP(A.n * (A.m - 1))
+    {
+        const int i = 1 + (int)(t / A.n);
+        const Pix<T> p(A, t - (long long)(i - 1) * A.n);
+        const T *g = A.g + (long long)i * A.n;
+        const T gc = g[p.c];
+        // 2D: p + (g(k+1) - g(k)); 3D: (p + g(k+1)) - g(k)
+        auto step = [&](T pv, T gn) { return A.dim == 2 ? add(pv, sub(gn, gc)) : sub(add(pv, gn), gc); };
+        if (p.y + 1 < A.d1) {
+            T *f = A.p1 + (long long)i * A.f1 + i1(A, p.y, p.x, p.z);
+            *f = step(*f, g[p.c + 1]);
+        }
+        if (p.x + 1 < A.d2) {
+            T *f = A.p2 + (long long)i * A.f2 + i2(A, p.y, p.x, p.z);
+            *f = step(*f, g[p.c + A.d1]);
+        }
+        if (A.dim == 3 && p.z + 1 < A.d3) {
+            T *f = A.p3 + (long long)i * A.f3 + i3(A, p.y, p.x, p.z);
+            *f = step(*f, g[p.c + (long long)A.d1 * A.d2]);
+        }
+    }
+}
+
+template <class T>
+__global__ void k3_projection(const HArgs<T> A)
+{
+    H_LOOP(A.n * (A.m - 1))
+    {
+        const int i = 1 + (int)(t / A.n);
+        const Pix<T> p(A, t - (long long)(i - 1) * A.n);
+        const T *f1 = A.p1 + (long long)i * A.f1;
+        const T *f2 = A.p2 + (long long)i * A.f2;
+        const T *f3 = A.p3 + (long long)i * A.f3;
+        // sum of the squares of the cell's faces, in the .m files' order
+        T s = (T)0;
+        if (p.y + 1 < A.d1) {
+            const T v = f1[i1(A, p.y, p.x, p.z)];
+            s = add(s, mul(v, v));
+        }
+        if (p.y >= 1) {
+            const T v = f1[i1(A, p.y - 1, p.x, p.z)];
+            s = add(s, mul(v, v));
+        }
+        if (p.x + 1 < A.d2) {
+            const T v = f2[i2(A, p.y, p.x, p.z)];
+            s = add(s, mul(v, v));
+        }
+        if (p.x >= 1) {
+            const T v = f2[i2(A, p.y, p.x - 1, p.z)];
+            s = add(s, mul(v, v));
+        }
+        if (A.dim == 3) {
+            if (p.z + 1 < A.d3) {
+                const T v = f3[i3(A, p.y, p.x, p.z)];
+                s = add(s, mul(v, v));
+            }
+            if (p.z >= 1) {
+                const T v = f3[i3(A, p.y, p.x, p.z - 1)];
+                s = add(s, mul(v, v));
+            }
+        }
+        const T mag = sqr(s);
+        const NodeDev<T> &nd = A.nodes[i];
+        const T al = nd.alpha ? nd.alpha[p.c] : nd.alpha_s;
+        A.g[(long long)i * A.n + p.c] = (mag <= al) ? (T)1 : dvd(al, mag);
+    }
+}
+
+template <class T>
+__global__ void k4_rescale(const HArgs<T> A)
+{
+    H_LOOP(A.n * (A.m - 1))
+    {
+        const int i = 1 + (int)(t / A.n);
+        const Pix<T> p(A, t - (long long)(i - 1) * A.n);
+        const T *g = A.g + (long long)i * A.n;
+        const T gc = g[p.c];
+        auto scale = [&](T *f, T gn) { *f = mul(mul((T)0.5, *f), add(gn, gc)); };
+        if (p.y + 1 < A.d1)
+            scale(A.p1 + (long long)i * A.f1 + i1(A, p.y, p.x, p.z), g[p.c + 1]);
+        if (p.x + 1 < A.d2)
+            scale(A.p2 + (long long)i * A.f2 + i2(A, p.y, p.x, p.z), g[p.c + A.d1]);
+        if (A.dim == 3 && p.z + 1 < A.d3)
+            scale(A.p3 + (long long)i * A.f3 + i3(A, p.y, p.x, p.z), g[p.c + (long long)A.d1 * A.d2]);
+    }
+}
+
+template <class T>
+__global__ void k5_divergence(const HArgs<T> A)
+{
+    H_LOOP(A.n * (A.m - 1))
+    {
+        const int i = 1 + (int)(t / A.n);
+        const Pix<T> p(A, t - (long long)(i - 1) * A.n);
+        const T *f1 = A.p1 + (long long)i * A.f1;
+        const T *f2 = A.p2 + (long long)i * A.f2;
+        const T *f3 = A.p3 + (long long)i * A.f3;
+        T d = (p.y + 1 < A.d1) ? f1[i1(A, p.y, p.x, p.z)] : (T)0;
+        if (p.y >= 1)
+            d = sub(d, f1[i1(A, p.y - 1, p.x, p.z)]);
+        if (p.x + 1 < A.d2)
+            d = add(d, f2[i2(A, p.y, p.x, p.z)]);
+        if (p.x >= 1)
+            d = sub(d, f2[i2(A, p.y, p.x - 1, p.z)]);
+        if (A.dim == 3) {
+            if (p.z + 1 < A.d3)
+                d = add(d, f3[i3(A, p.y, p.x, p.z)]);
+            if (p.z >= 1)
+                d = sub(d, f3[i3(A, p.y, p.x, p.z - 1)]);
+        }
+        A.div[(long long)i * A.n + p.c] = d;
+    }
+}
+
+template <class T>
+__global__ void k_costs(const HArgs<T> A)
+{
+    H_LOOP(A.n * A.m)
+    {
+        const int i = (int)(t / A.n);
+        const long long c = t - (long long)i * A.n;
+        const NodeDev<T> &nd = A.nodes[i];
+        const double u = (double)A.u[t];
+        if (nd.nchild == 0)
+            atomicAdd(&A.cost[2 * i], u * (double)nd.ct[c]);
+        if (nd.parent >= 0)
+            atomicAdd(&A.cost[2 * i + 1], u * (double)A.div[t]);
+    }
+}
+
+int h_grid(long long n, int sms)
+{
+    long long b = (n + kThreads - 1) / kThreads;
+    const long long cap = (long long)sms * 8;
+    return (int)(b < 1 ? 1 : (b < cap ? b : cap));
+}
+
+template <class T>
+asets_status run_hmf(asets_context *ctx, int dim, int d1, int d2, int d3, int m, const int *parent,
+                     const void *const *Ct, const void *const *alpha_arr, const double *alpha_s,
+                     int its, double steps, double cc, void *const *u_out, void *const *pt_out,
+                     void *const *div_out, void *const *g_out, void *const *p_out[3],
+                     double *data_cost, double *regu_cost)
+{
+    cudaStream_t st = context_stream(ctx);
+    const int sms = context_num_sms(ctx);
+    const long long n = (long long)d1 * d2 * d3;
+    const long long f1 = (long long)(d1 - 1) * d2 * d3, f2 = (long long)d1 * (d2 - 1) * d3,
+                    f3 = dim == 3 ? (long long)d1 * d2 * (d3 - 1) : 0;
+    // tree tables (children of each node in index order)
+    std::vector<int> nchild(m, 0), begin(m, 0), kids;
+    for (int i = 1; i < m; ++i)
+        ++nchild[parent[i]];
+    for (int i = 0, acc = 0; i < m; ++i) {
+        begin[i] = acc;
+        acc += nchild[i];
+    }
+    kids.assign(m > 1 ? m - 1 : 1, 0);
+    {
+        std::vector<int> fill(begin);
+        for (int i = 1; i < m; ++i)
+            kids[fill[parent[i]]++] = i;
+    }
+    std::vector<void *> bufs;
+    asets_status status = ASETS_OK;
+    auto get = [&](void **p, size_t bytes) {
+        if (cudaMallocAsync(p, bytes ? bytes : 8, st) != cudaSuccess)
+            return false;
+        bufs.push_back(*p);
+        return true;
+    };
+    HArgs<T> A;
+    memset(&A, 0, sizeof A);
+    A.dim = dim;
+    A.d1 = d1;
+    A.d2 = d2;
+    A.d3 = d3;
+    A.m = m;
+    A.n = n;
+    A.f1 = f1;
+    A.f2 = f2;
+    A.f3 = f3;
+    A.cc = (T)cc;
+    A.steps = (T)steps;
+    A.inv_cc = (T)(1.0 / cc);
+    std::vector<NodeDev<T>> nodes(m);
+    void *vp = nullptr;
+    cudaError_t e = cudaSuccess;
+    bool ok = get(&vp, sizeof(T) * n * m * 4);
+    if (ok) {
+        T *base = static_cast<T *>(vp);
+        A.pt = base;
+        A.u = base + n * m;
+        A.div = base + 2 * n * m;
+        A.g = base + 3 * n * m;
+        e = cudaMemsetAsync(vp, 0, sizeof(T) * n * m * 4, st);
+    }
+    const long long fsum = (f1 + f2 + f3) * m;
+    ok = ok && get(&vp, sizeof(T) * fsum);
+    if (ok) {
+        A.p1 = static_cast<T *>(vp);
+        A.p2 = A.p1 + f1 * m;
+        A.p3 = A.p2 + f2 * m;
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(vp, 0, sizeof(T) * fsum, st);
+    }
+    ok = ok && get(&vp, sizeof(double) * 2 * m);
+    if (ok) {
+        A.cost = static_cast<double *>(vp);
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(vp, 0, sizeof(double) * 2 * m, st);
+    }
+    for (int i = 0; ok && i < m; ++i) {
+        NodeDev<T> &nd = nodes[i];
+        nd.parent = parent[i];
+        nd.child_begin = begin[i];
+        nd.nchild = nchild[i];
+        nd.alpha_s = (T)(alpha_s ? alpha_s[i] : 0.0);
+        nd.ct = nullptr;
+        nd.alpha = nullptr;
+        if (nchild[i] == 0 && e == cudaSuccess) {
+            ok = get(&vp, sizeof(T) * n);
+            if (ok) {
+                e = cudaMemcpyAsync(vp, Ct[i], sizeof(T) * n, cudaMemcpyHostToDevice, st);
+                nd.ct = static_cast<const T *>(vp);
+            }
+        }
+        if (ok && alpha_arr && alpha_arr[i] && e == cudaSuccess) {
+            ok = get(&vp, sizeof(T) * n);
+            if (ok) {
+                e = cudaMemcpyAsync(vp, alpha_arr[i], sizeof(T) * n, cudaMemcpyHostToDevice, st);
+                nd.alpha = static_cast<const T *>(vp);
+            }
+        }
+    }
+    ok = ok && get(&vp, sizeof(NodeDev<T>) * m);
+    if (ok && e == cudaSuccess) {
+        e = cudaMemcpyAsync(vp, nodes.data(), sizeof(NodeDev<T>) * m, cudaMemcpyHostToDevice, st);
+        A.nodes = static_cast<const NodeDev<T> *>(vp);
+    }
+    ok = ok && get(&vp, sizeof(int) * kids.size());
+    if (ok && e == cudaSuccess) {
+        e = cudaMemcpyAsync(vp, kids.data(), sizeof(int) * kids.size(), cudaMemcpyHostToDevice, st);
+        A.children = static_cast<const int *>(vp);
+    }
+    if (!ok) {
+        status = ASETS_ERR_OUT_OF_MEMORY;
+        set_last_error("asets_hmf_full_flow: out of device memory");
+    } else if (e == cudaSuccess) {
+        const int gp = h_grid(n, sms), gn = h_grid(n * (m - 1), sms);
+        for (int it = 0; it < its && e == cudaSuccess; ++it) {
+            k1_pointwise<T><<<gp, kThreads, 0, st>>>(A);
+            if (m > 1) {
+                k2_gradient<T><<<gn, kThreads, 0, st>>>(A);
+                k3_projection<T><<<gn, kThreads, 0, st>>>(A);
+                k4_rescale<T><<<gn, kThreads, 0, st>>>(A);
+                k5_divergence<T><<<gn, kThreads, 0, st>>>(A);
+            }
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) {
+            k_costs<T><<<h_grid(n * m, sms), kThreads, 0, st>>>(A);
+            e = cudaGetLastError();
+        }
+        std::vector<double> cost(2 * m, 0.0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(cost.data(), A.cost, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost, st);
+        for (int i = 0; i < m && e == cudaSuccess; ++i) {
+            const size_t nb = sizeof(T) * n;
+            if (u_out && u_out[i])
+                e = cudaMemcpyAsync(u_out[i], A.u + (long long)i * n, nb, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess && pt_out && pt_out[i])
+                e = cudaMemcpyAsync(pt_out[i], A.pt + (long long)i * n, nb, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess && div_out && div_out[i])
+                e = cudaMemcpyAsync(div_out[i], A.div + (long long)i * n, nb, cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess && g_out && g_out[i])
+                e = cudaMemcpyAsync(g_out[i], A.g + (long long)i * n, nb, cudaMemcpyDeviceToHost, st);
+            const T *fp[3] = {A.p1 + f1 * i, A.p2 + f2 * i, A.p3 + f3 * i};
+            const long long fn[3] = {f1, f2, f3};
+            for (int k = 0; k < dim && e == cudaSuccess; ++k)
+                if (p_out[k] && p_out[k][i] && fn[k] > 0)
+                    e = cudaMemcpyAsync(p_out[k][i], fp[k], sizeof(T) * fn[k], cudaMemcpyDeviceToHost, st);
+        }
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) {
+            // CalculateCostsFullFlow: each node adds its children's costs
+            std::vector<double> dc(m), rc(m);
+            for (int i = m - 1; i >= 0; --i) {
+                dc[i] = cost[2 * i];
+                rc[i] = cost[2 * i + 1];
+                for (int j = 0; j < nchild[i]; ++j) {
+                    dc[i] += dc[kids[begin[i] + j]];
+                    rc[i] += rc[kids[begin[i] + j]];
+                }
+            }
+            for (int i = 0; i < m; ++i) {
+                if (data_cost)
+                    data_cost[i] = dc[i];
+                if (regu_cost)
+                    regu_cost[i] = rc[i];
+            }
+        }
+    }
+    if (status == ASETS_OK && e != cudaSuccess) {
+        cudaGetLastError();
+        status = ASETS_ERR_CUDA;
+        set_last_error((std::string("asets_hmf_full_flow: ") + cudaGetErrorString(e)).c_str());
+    }
+    for (void *p : bufs)
+        cudaFreeAsync(p, st);
+    cudaStreamSynchronize(st);
+    return status;
+}
+
+}  // namespace
+
+extern "C" ASETS_API asets_status asets_hmf_full_flow(
+    asets_context *ctx, int precision, int dim, int D1, int D2, int D3, int num_nodes,
+    const int *parent, const void *const *Ct, const void *const *alpha_arrays,
+    const double *alpha_scalars, int numIts, double steps, double cc, void *const *u,
+    void *const *pt, void *const *div, void *const *g, void *const *p1, void *const *p2,
+    void *const *p3, double *data_cost, double *regu_cost)
+{
+    if (!ctx || !parent || !Ct || (precision != 4 && precision != 8) || (dim != 2 && dim != 3) ||
+        D1 < 1 || D2 < 1 || D3 < 1 || (dim == 2 && D3 != 1) || num_nodes < 1 || numIts < 0) {
+        set_last_error("asets_hmf_full_flow: bad arguments");
+        return ASETS_ERR_INVALID_ARG;
+    }
+    if (parent[0] != -1) {
+        set_last_error("asets_hmf_full_flow: node 0 must be the root (parent -1)");
+        return ASETS_ERR_INVALID_ARG;
+    }
+    std::vector<int> nch(num_nodes, 0);
+    for (int i = 1; i < num_nodes; ++i) {
+        if (parent[i] < 0 || parent[i] >= i) {
+            set_last_error("asets_hmf_full_flow: nodes must be in pre-order (parent index < node index)");
+            return ASETS_ERR_INVALID_ARG;
+        }
+        ++nch[parent[i]];
+    }
+    for (int i = 0; i < num_nodes; ++i)
+        if (nch[i] == 0 && !Ct[i]) {
+            set_last_error("asets_hmf_full_flow: every leaf needs its Ct");
+            return ASETS_ERR_INVALID_ARG;
+        }
+    if (num_nodes == 1 || nch[0] == 0) {
+        set_last_error("asets_hmf_full_flow: the root needs children");
+        return ASETS_ERR_INVALID_ARG;
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(context_device(ctx));
+    void *const *p_out[3] = {p1, p2, p3};
+    const asets_status s =
+        precision == 8
+            ? run_hmf<double>(ctx, dim, D1, D2, D3, num_nodes, parent, Ct, alpha_arrays,
+                              alpha_scalars, numIts, steps, cc, u, pt, div, g, p_out, data_cost,
+                              regu_cost)
+            : run_hmf<float>(ctx, dim, D1, D2, D3, num_nodes, parent, Ct, alpha_arrays,
+                             alpha_scalars, numIts, steps, cc, u, pt, div, g, p_out, data_cost,
+                             regu_cost);
+    cudaSetDevice(prev);
+    return s;
+}

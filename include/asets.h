@@ -320,6 +320,31 @@ ASETS_API asets_status asets_potts2d_starshape(asets_context *ctx, const double 
                                                double *erriter, int *itNum, float *seconds);
 
 /* ------------------------------------------------------------------------
+ * Hierarchical max-flow, full-flow iteration (maxflow/asetsHMF2D.m and
+ * asetsHMF3D.m, MaxFullFlow; Matlab classes with no counterpart in the
+ * reference's C code).  precision 4 (float) or 8 (double), as the class of
+ * the cost terms.  The tree: num_nodes nodes in pre-order, parent[0] = -1
+ * (the root), parent[i] < i, children of a node in index order.  Ct[i]:
+ * D1*D2*D3 costs of leaf i (Matlab layout; NULL for inner nodes);
+ * alpha_arrays[i] a per-pixel alpha or NULL, then alpha_scalars[i] is used.
+ * Runs numIts iterations (UpdateSinkFlows, UpdateLabels,
+ * UpdateSpatialFlows; isotropic flows only) and copies out any non-NULL
+ * per-node result: u, pt, div, g (D1*D2*D3), the spatial flows p1
+ * ((D1-1)*D2*D3, the class's px), p2 (D1*(D2-1)*D3, py), p3
+ * (D1*D2*(D3-1), pz, 3D only), and CalculateCostsFullFlow's dataCost and
+ * reguCost per node (each including its subtree).  All host memory.
+ * ---------------------------------------------------------------------- */
+ASETS_API asets_status asets_hmf_full_flow(asets_context *ctx, int precision, int dim, int D1,
+                                           int D2, int D3, int num_nodes, const int *parent,
+                                           const void *const *Ct,
+                                           const void *const *alpha_arrays,
+                                           const double *alpha_scalars, int numIts,
+                                           double steps, double cc, void *const *u,
+                                           void *const *pt, void *const *div, void *const *g,
+                                           void *const *p1, void *const *p2, void *const *p3,
+                                           double *data_cost, double *regu_cost);
+
+/* ------------------------------------------------------------------------
  * Cost terms and regularisation weights on the GPU: the step before the
  * solvers in the reference's applications (applications/*.m; no counterpart
  * in its C code).  Arrays in Matlab layout, label slowest; `where` says
