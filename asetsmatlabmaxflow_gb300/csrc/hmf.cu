@@ -12,6 +12,11 @@
 //   K2 gradient step of the spatial flows, K3 flow magnitude and projection
 //   factor, K4 flow rescale, K5 divergence (the rest of UpdateSpatialFlows).
 // Costs (CalculateCostsFullFlow) are summed on the device in double.
+//
+// The DAG solver (maxflow/asetsDAGMF2D.m / 3D, nodes may have several
+// parents, each child weighted 1/(its number of parents)) shares the spatial
+// passes; its iteration is spatial flows first, then one per-pixel pass for
+// PushDownFlows (top-down list), PushCapacityUp (bottom-up) and the labels.
 // Not built: the anisotropic lx/ly branch and MaxPseudoFlow.
 #include <cstring>
 #include <string>
@@ -32,15 +37,21 @@ struct NodeDev {
     const T *alpha;  // per-pixel alpha or null
     T alpha_s;       // scalar alpha
     int parent, child_begin, nchild;
+    int nparent;     // DAG: number of parents (parent = the first)
+    T wdiv;          // DAG: sum of the children's weights squared (+1 below the root)
 };
 
 template <class T>
 struct HArgs {
     int dim, d1, d2, d3, m;
+    int paren;  // gradient step p + (g1 - g0) (asetsHMF2D.m) instead of (p + g1) - g0
     long long n, f1, f2, f3;  // cells and face counts per node
     T cc, steps, inv_cc;      // inv_cc: 1/cc formed in double (the root's 1/cc .* ones)
     const NodeDev<T> *nodes;
     const int *children;
+    const T *wchild;    // DAG: weight of each child edge
+    const int *order;   // DAG: the top-down node list
+    T *pn;              // DAG: pushed-down flow of multi-parent nodes
     T *pt, *u, *div, *g, *p1, *p2, *p3;
     double *cost;  // [m][2]: sum u*Ct (leaves), sum u*div (non-root)
 };
@@ -145,7 +156,7 @@ __global__ void k2_gradient(const HArgs<T> A)
         const T *g = A.g + (long long)i * A.n;
         const T gc = g[p.c];
         // 2D: p + (g(k+1) - g(k)); 3D: (p + g(k+1)) - g(k)
-        auto step = [&](T pv, T gn) { return A.dim == 2 ? add(pv, sub(gn, gc)) : sub(add(pv, gn), gc); };
+        auto step = [&](T pv, T gn) { return A.paren ? add(pv, sub(gn, gc)) : sub(add(pv, gn), gc); };
         if (p.y + 1 < A.d1) {
             T *f = A.p1 + (long long)i * A.f1 + i1(A, p.y, p.x, p.z);
             *f = step(*f, g[p.c + 1]);
@@ -268,6 +279,118 @@ __global__ void k_costs(const HArgs<T> A)
     }
 }
 
+// ---------------------------------------------------------------- DAG
+template <class T>
+__device__ __forceinline__ T dag_in(const HArgs<T> &A, const NodeDev<T> &nd, int i, long long c)
+{
+    return nd.nparent > 1 ? A.pn[(long long)i * A.n + c] : A.pt[(long long)nd.parent * A.n + c];
+}
+
+// InitializeFullFlow: pt = Ct (leaves) or max(0, pt of the first child);
+// pn = pt (2D) or 0 (3D) for nodes with several parents.
+template <class T>
+__global__ void k_dag_init(const HArgs<T> A)
+{
+    H_LOOP(A.n)
+    {
+        for (int j = A.m - 1; j >= 0; --j) {
+            const int i = A.order[j];
+            const NodeDev<T> nd = A.nodes[i];
+            const long long o = (long long)i * A.n + t;
+            T pt;
+            if (nd.nchild == 0) {
+                pt = nd.ct[t];
+            } else {
+                const T x = A.pt[(long long)A.children[nd.child_begin] * A.n + t];
+                const T z = (T)0;
+                pt = (z >= x) ? z : x;
+            }
+            A.pt[o] = pt;
+            if (nd.nparent > 1)
+                A.pn[o] = A.dim == 2 ? pt : (T)0;
+        }
+    }
+}
+
+// UpdateSpatialFlows' first line: g = steps*(div + pt - in - u/cc)
+template <class T>
+__global__ void k_dag_g(const HArgs<T> A)
+{
+    H_LOOP(A.n * (A.m - 1))
+    {
+        const int i = 1 + (int)(t / A.n);
+        const long long c = t - (long long)(i - 1) * A.n;
+        const long long o = (long long)i * A.n + c;
+        const T in = dag_in(A, A.nodes[i], i, c);
+        A.g[o] = mul(A.steps, sub(sub(add(A.div[o], A.pt[o]), in), dvd(A.u[o], A.cc)));
+    }
+}
+
+// pn reset, PushDownFlows (top-down), PushCapacityUp (bottom-up), labels.
+template <class T>
+__global__ void k_dag_point(const HArgs<T> A)
+{
+    H_LOOP(A.n)
+    {
+        const long long c = t;
+        for (int i = 0; i < A.m; ++i)
+            if (A.nodes[i].nparent > 1)
+                A.pn[(long long)i * A.n + c] = (T)0;
+        for (int j = 0; j < A.m; ++j) {
+            const int i = A.order[j];
+            const NodeDev<T> nd = A.nodes[i];
+            const long long o = (long long)i * A.n + c;
+            const T pt = A.pt[o];
+            for (int k = 0; k < nd.nchild; ++k) {
+                const int ch = A.children[nd.child_begin + k];
+                if (A.nodes[ch].nparent > 1) {
+                    T *pn = A.pn + (long long)ch * A.n + c;
+                    *pn = add(*pn, mul(A.wchild[nd.child_begin + k], pt));
+                }
+            }
+            if (nd.nparent > 0 && nd.nchild > 0)
+                A.g[o] = add(sub(dag_in(A, nd, i, c), A.div[o]), dvd(A.u[o], A.cc));
+            else if (nd.nparent == 0)
+                A.g[o] = A.inv_cc;
+        }
+        for (int j = A.m - 1; j >= 0; --j) {
+            const int i = A.order[j];
+            const NodeDev<T> nd = A.nodes[i];
+            const long long o = (long long)i * A.n + c;
+            if (nd.nchild == 0) {
+                const T x = add(sub(dag_in(A, nd, i, c), A.div[o]), dvd(A.u[o], A.cc));
+                const T ct = nd.ct[c];
+                A.pt[o] = (ct <= x || ct != ct) ? ct : x;
+                continue;
+            }
+            const T pto = A.pt[o];
+            T g = A.g[o];
+            for (int k = 0; k < nd.nchild; ++k) {
+                const int ch = A.children[nd.child_begin + k];
+                const long long oc = (long long)ch * A.n + c;
+                const T uc = dvd(A.u[oc], A.cc);
+                if (A.nodes[ch].nparent > 1) {
+                    const T w = A.wchild[nd.child_begin + k];
+                    const T e = sub(sub(add(add(A.div[oc], A.pt[oc]), mul(w, pto)), A.pn[oc]), uc);
+                    g = add(g, mul(w, e));
+                } else {
+                    g = sub(add(add(g, A.div[oc]), A.pt[oc]), uc);
+                }
+            }
+            A.g[o] = g;
+            A.pt[o] = dvd(g, nd.wdiv);
+        }
+        for (int j = 0; j < A.m; ++j) {
+            const int i = A.order[j];
+            const NodeDev<T> nd = A.nodes[i];
+            if (nd.nparent == 0)
+                continue;
+            const long long o = (long long)i * A.n + c;
+            A.u[o] = add(A.u[o], mul(A.cc, sub(sub(dag_in(A, nd, i, c), A.div[o]), A.pt[o])));
+        }
+    }
+}
+
 int h_grid(long long n, int sms)
 {
     long long b = (n + kThreads - 1) / kThreads;
@@ -323,6 +446,7 @@ asets_status run_hmf(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
     A.cc = (T)cc;
     A.steps = (T)steps;
     A.inv_cc = (T)(1.0 / cc);
+    A.paren = (dim == 2) ? 1 : 0;  // asetsHMF2D.m parenthesises the gradient step
     std::vector<NodeDev<T>> nodes(m);
     void *vp = nullptr;
     cudaError_t e = cudaSuccess;
@@ -453,7 +577,245 @@ asets_status run_hmf(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
     return status;
 }
 
+template <class T>
+asets_status run_dag(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
+                     const std::vector<int> &nchild, const std::vector<int> &begin,
+                     const std::vector<int> &kids, const std::vector<int> &nparent,
+                     const std::vector<int> &parent0, const std::vector<int> &order,
+                     const void *const *Ct, const void *const *alpha_arr, const double *alpha_s,
+                     int its, double steps, double cc, void *const *outs[5],
+                     void *const *p_out[3])
+{
+    cudaStream_t st = context_stream(ctx);
+    const int sms = context_num_sms(ctx);
+    const long long n = (long long)d1 * d2 * d3;
+    const long long f1 = (long long)(d1 - 1) * d2 * d3, f2 = (long long)d1 * (d2 - 1) * d3,
+                    f3 = dim == 3 ? (long long)d1 * d2 * (d3 - 1) : 0;
+    std::vector<void *> bufs;
+    auto get = [&](void **p, size_t bytes) {
+        if (cudaMallocAsync(p, bytes ? bytes : 8, st) != cudaSuccess)
+            return false;
+        bufs.push_back(*p);
+        return true;
+    };
+    HArgs<T> A;
+    memset(&A, 0, sizeof A);
+    A.dim = dim;
+    A.d1 = d1;
+    A.d2 = d2;
+    A.d3 = d3;
+    A.m = m;
+    A.n = n;
+    A.f1 = f1;
+    A.f2 = f2;
+    A.f3 = f3;
+    A.cc = (T)cc;
+    A.steps = (T)steps;
+    A.inv_cc = (T)(1.0 / cc);
+    A.paren = 0;  // both DAG files: (p + g(k+1)) - g(k)
+    // child weights 1/(parents of the child); per node the sum of their squares
+    std::vector<T> w(kids.size());
+    std::vector<NodeDev<T>> nodes(m);
+    for (int i = 0; i < m; ++i) {
+        double s2 = 0.0;
+        for (int k = 0; k < nchild[i]; ++k) {
+            const double wk = 1.0 / (double)nparent[kids[begin[i] + k]];
+            w[begin[i] + k] = (T)wk;
+            s2 += wk * wk;
+        }
+        NodeDev<T> &nd = nodes[i];
+        nd.parent = parent0[i];
+        nd.nparent = nparent[i];
+        nd.child_begin = begin[i];
+        nd.nchild = nchild[i];
+        nd.wdiv = (T)(nparent[i] == 0 ? s2 : 1.0 + s2);
+        nd.alpha_s = (T)(alpha_s ? alpha_s[i] : 0.0);
+        nd.ct = nullptr;
+        nd.alpha = nullptr;
+    }
+    cudaError_t e = cudaSuccess;
+    void *vp = nullptr;
+    bool ok = get(&vp, sizeof(T) * n * m * 5);
+    if (ok) {
+        T *base = static_cast<T *>(vp);
+        A.pt = base;
+        A.u = base + n * m;
+        A.div = base + 2 * n * m;
+        A.g = base + 3 * n * m;
+        A.pn = base + 4 * n * m;
+        e = cudaMemsetAsync(vp, 0, sizeof(T) * n * m * 5, st);
+    }
+    const long long fsum = (f1 + f2 + f3) * m;
+    ok = ok && get(&vp, sizeof(T) * fsum);
+    if (ok) {
+        A.p1 = static_cast<T *>(vp);
+        A.p2 = A.p1 + f1 * m;
+        A.p3 = A.p2 + f2 * m;
+        if (e == cudaSuccess)
+            e = cudaMemsetAsync(vp, 0, sizeof(T) * fsum, st);
+    }
+    for (int i = 0; ok && i < m && e == cudaSuccess; ++i) {
+        if (nchild[i] == 0) {
+            ok = get(&vp, sizeof(T) * n);
+            if (ok) {
+                e = cudaMemcpyAsync(vp, Ct[i], sizeof(T) * n, cudaMemcpyHostToDevice, st);
+                nodes[i].ct = static_cast<const T *>(vp);
+            }
+        }
+        if (ok && e == cudaSuccess && alpha_arr && alpha_arr[i]) {
+            ok = get(&vp, sizeof(T) * n);
+            if (ok) {
+                e = cudaMemcpyAsync(vp, alpha_arr[i], sizeof(T) * n, cudaMemcpyHostToDevice, st);
+                nodes[i].alpha = static_cast<const T *>(vp);
+            }
+        }
+    }
+    struct Up {
+        const void *src;
+        size_t bytes;
+        const void **dst;
+    } ups[] = {{nodes.data(), sizeof(NodeDev<T>) * m, reinterpret_cast<const void **>(&A.nodes)},
+               {kids.data(), sizeof(int) * kids.size(), reinterpret_cast<const void **>(&A.children)},
+               {w.data(), sizeof(T) * w.size(), reinterpret_cast<const void **>(&A.wchild)},
+               {order.data(), sizeof(int) * order.size(), reinterpret_cast<const void **>(&A.order)}};
+    for (auto &u : ups) {
+        ok = ok && get(&vp, u.bytes);
+        if (ok && e == cudaSuccess) {
+            e = cudaMemcpyAsync(vp, u.src, u.bytes, cudaMemcpyHostToDevice, st);
+            *u.dst = vp;
+        }
+    }
+    asets_status status = ASETS_OK;
+    if (!ok) {
+        status = ASETS_ERR_OUT_OF_MEMORY;
+        set_last_error("asets_dag_full_flow: out of device memory");
+    } else if (e == cudaSuccess) {
+        const int gp = h_grid(n, sms), gn = h_grid(n * (m - 1), sms);
+        k_dag_init<T><<<gp, kThreads, 0, st>>>(A);
+        for (int it = 0; it < its && e == cudaSuccess; ++it) {
+            k_dag_g<T><<<gn, kThreads, 0, st>>>(A);
+            k2_gradient<T><<<gn, kThreads, 0, st>>>(A);
+            k3_projection<T><<<gn, kThreads, 0, st>>>(A);
+            k4_rescale<T><<<gn, kThreads, 0, st>>>(A);
+            k5_divergence<T><<<gn, kThreads, 0, st>>>(A);
+            k_dag_point<T><<<gp, kThreads, 0, st>>>(A);
+            e = cudaGetLastError();
+        }
+        T *const srcs[5] = {A.u, A.pt, A.pn, A.div, A.g};
+        for (int i = 0; i < m && e == cudaSuccess; ++i) {
+            for (int k = 0; k < 5 && e == cudaSuccess; ++k)
+                if (outs[k] && outs[k][i])
+                    e = cudaMemcpyAsync(outs[k][i], srcs[k] + (long long)i * n, sizeof(T) * n,
+                                        cudaMemcpyDeviceToHost, st);
+            const T *fp[3] = {A.p1 + f1 * i, A.p2 + f2 * i, A.p3 + f3 * i};
+            const long long fn[3] = {f1, f2, f3};
+            for (int k = 0; k < dim && e == cudaSuccess; ++k)
+                if (p_out[k] && p_out[k][i] && fn[k] > 0)
+                    e = cudaMemcpyAsync(p_out[k][i], fp[k], sizeof(T) * fn[k], cudaMemcpyDeviceToHost, st);
+        }
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(st);
+    }
+    if (status == ASETS_OK && e != cudaSuccess) {
+        cudaGetLastError();
+        status = ASETS_ERR_CUDA;
+        set_last_error((std::string("asets_dag_full_flow: ") + cudaGetErrorString(e)).c_str());
+    }
+    for (void *p : bufs)
+        cudaFreeAsync(p, st);
+    cudaStreamSynchronize(st);
+    return status;
+}
+
 }  // namespace
+
+extern "C" ASETS_API asets_status asets_dag_full_flow(
+    asets_context *ctx, int precision, int dim, int D1, int D2, int D3, int num_nodes,
+    const int *nchild_in, const int *children, const void *const *Ct,
+    const void *const *alpha_arrays, const double *alpha_scalars, int numIts, double steps,
+    double cc, void *const *u, void *const *pt, void *const *pn, void *const *div,
+    void *const *g, void *const *p1, void *const *p2, void *const *p3)
+{
+    if (!ctx || !nchild_in || !Ct || (precision != 4 && precision != 8) || (dim != 2 && dim != 3) ||
+        D1 < 1 || D2 < 1 || D3 < 1 || (dim == 2 && D3 != 1) || num_nodes < 2 || numIts < 0) {
+        set_last_error("asets_dag_full_flow: bad arguments");
+        return ASETS_ERR_INVALID_ARG;
+    }
+    const int m = num_nodes;
+    std::vector<int> nchild(nchild_in, nchild_in + m), begin(m, 0), nparent(m, 0), parent0(m, -1);
+    int total = 0;
+    for (int i = 0; i < m; ++i) {
+        if (nchild[i] < 0 || nchild[i] == 1) {
+            set_last_error("asets_dag_full_flow: an inner node needs two or more children");
+            return ASETS_ERR_INVALID_ARG;
+        }
+        begin[i] = total;
+        total += nchild[i];
+    }
+    std::vector<int> kids(children ? children : nullptr, children ? children + total : nullptr);
+    if ((int)kids.size() != total) {
+        set_last_error("asets_dag_full_flow: children missing");
+        return ASETS_ERR_INVALID_ARG;
+    }
+    for (int i = 0; i < m; ++i)
+        for (int k = 0; k < nchild[i]; ++k) {
+            const int c = kids[begin[i] + k];
+            if (c <= 0 || c >= m) {
+                set_last_error("asets_dag_full_flow: bad child index (node 0 is the root)");
+                return ASETS_ERR_INVALID_ARG;
+            }
+            if (nparent[c]++ == 0)
+                parent0[c] = i;
+        }
+    if (nparent[0] != 0 || nchild[0] == 0) {
+        set_last_error("asets_dag_full_flow: node 0 must be the root, with children");
+        return ASETS_ERR_INVALID_ARG;
+    }
+    for (int i = 0; i < m; ++i)
+        if (nchild[i] == 0 && !Ct[i]) {
+            set_last_error("asets_dag_full_flow: every leaf needs its Ct");
+            return ASETS_ERR_INVALID_ARG;
+        }
+    // the top-down list of MaxFullFlow: depth-first from the root, a node
+    // entering the stack once all its parents are listed
+    std::vector<int> order, stack{0};
+    std::vector<char> listed(m, 0);
+    while (!stack.empty()) {
+        const int q = stack.back();
+        stack.pop_back();
+        order.push_back(q);
+        listed[q] = 1;
+        for (int k = 0; k < nchild[q]; ++k) {
+            const int r = kids[begin[q] + k];
+            bool all = true;
+            for (int i = 0; i < m && all; ++i)
+                for (int j = 0; j < nchild[i]; ++j)
+                    if (kids[begin[i] + j] == r && !listed[i]) {
+                        all = false;
+                        break;
+                    }
+            if (all)
+                stack.push_back(r);
+        }
+    }
+    if ((int)order.size() != m) {
+        set_last_error("asets_dag_full_flow: the graph has nodes not reachable from the root, or a cycle");
+        return ASETS_ERR_INVALID_ARG;
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(context_device(ctx));
+    void *const *outs[5] = {u, pt, pn, div, g};
+    void *const *p_out[3] = {p1, p2, p3};
+    const asets_status s =
+        precision == 8
+            ? run_dag<double>(ctx, dim, D1, D2, D3, m, nchild, begin, kids, nparent, parent0, order,
+                              Ct, alpha_arrays, alpha_scalars, numIts, steps, cc, outs, p_out)
+            : run_dag<float>(ctx, dim, D1, D2, D3, m, nchild, begin, kids, nparent, parent0, order,
+                             Ct, alpha_arrays, alpha_scalars, numIts, steps, cc, outs, p_out);
+    cudaSetDevice(prev);
+    return s;
+}
 
 extern "C" ASETS_API asets_status asets_hmf_full_flow(
     asets_context *ctx, int precision, int dim, int D1, int D2, int D3, int num_nodes,

@@ -344,6 +344,26 @@ ASETS_API asets_status asets_hmf_full_flow(asets_context *ctx, int precision, in
                                            void *const *p1, void *const *p2, void *const *p3,
                                            double *data_cost, double *regu_cost);
 
+/* DAG max-flow, full-flow iteration (maxflow/asetsDAGMF2D.m and
+ * asetsDAGMF3D.m, MaxFullFlow; Matlab classes with no counterpart in the
+ * reference's C code): as asets_hmf_full_flow, but a node may have several
+ * parents.  The graph: node 0 is the root; nchild[i] children of node i,
+ * listed in order in the flattened `children` (inner nodes need two or
+ * more, as the reference's initialisation does).  Each child is weighted
+ * 1/(its number of parents); nodes are visited in the class's own top-down
+ * list (depth-first, a node once all its parents are listed).  Outputs as
+ * asets_hmf_full_flow plus pn (the flow pushed down to nodes with several
+ * parents); no costs. */
+ASETS_API asets_status asets_dag_full_flow(asets_context *ctx, int precision, int dim, int D1,
+                                           int D2, int D3, int num_nodes, const int *nchild,
+                                           const int *children, const void *const *Ct,
+                                           const void *const *alpha_arrays,
+                                           const double *alpha_scalars, int numIts,
+                                           double steps, double cc, void *const *u,
+                                           void *const *pt, void *const *pn, void *const *div,
+                                           void *const *g, void *const *p1, void *const *p2,
+                                           void *const *p3);
+
 /* ------------------------------------------------------------------------
  * Cost terms and regularisation weights on the GPU: the step before the
  * solvers in the reference's applications (applications/*.m; no counterpart
