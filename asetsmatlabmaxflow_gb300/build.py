@@ -57,6 +57,7 @@ CU_SOURCES = (
     "costs.cu",
     "starshape.cu",
     "hmf.cu",
+    "mtwin.cu",
 )
 
 MEX_SOLVERS = (

@@ -1,0 +1,542 @@
+// Matlab-semantics solvers: the GPU form of the reference's Matlab twins of
+// the six mex solvers (maxflow/asetsBinaryMF2D.m, asetsBinaryMF3D.m,
+// asetsPotts2D.m, asetsPotts3D.m, asetsIshikawa2D.m, asetsIshikawa3D.m),
+// the path its tutorials use with gpuArray (tutorials/t03_usingCUDA.m).
+// They differ from the mex files: they compute in the class of Ct (single
+// or double), break on erriter < beta, initialise Potts/Ishikawa from the
+// argmin of Ct, and use Matlab's own expression orders, all kept here;
+// the kernels are templated on the element type and follow each .m line's
+// evaluation order (IEEE operations, no contraction), so u matches a numpy
+// restatement in the same precision bit for bit.
+//
+// Per iteration, four passes over every flow label (binary 1, Potts L,
+// Ishikawa L-1):
+//   1 gradient step of the face flows from ud = divp - ((A - B) + u/cc),
+//     (A, B) = (ps, pt) binary, (ps, pt_k) Potts, (pt_k, pt_k+1) Ishikawa
+//   2 projection factor gk = 1/max(1, |p|/alpha) per cell
+//   3 face flows *= 0.5 (gk + gk of the cell below)
+//   4 per cell: divp of every label, then the model's sink/source flows and
+//     multipliers, and erriter; the last block records erriter and the break.
+#include <chrono>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "asets.h"
+#include "internal.h"
+
+using namespace asets;
+
+namespace {
+
+constexpr int kThreads = 256;
+enum { MT_BINARY = 0, MT_POTTS = 1, MT_ISHIKAWA = 2 };
+
+struct MTCtl {
+    int iter, done, it_num;
+    unsigned int ticket;
+    int max_it;
+    double beta, vol;
+};
+
+template <class T>
+struct MTArgs {
+    int rows, cols, slices, nlab, nflow;
+    long long n, f1, f2, f3;  // cells and faces per flow label
+    T cc, steps, half, one_over_cc, one_over_ccl, beta;
+    const T *cs, *ct, *alpha;
+    T *u, *pt, *ps, *divp, *gk, *p1, *p2, *p3;
+    double *partials;
+    T *erriter;
+    MTCtl *ctl;
+};
+
+template <class T> __device__ __forceinline__ T add(T a, T b);
+template <class T> __device__ __forceinline__ T sub(T a, T b);
+template <class T> __device__ __forceinline__ T mul(T a, T b);
+template <class T> __device__ __forceinline__ T dvd(T a, T b);
+template <class T> __device__ __forceinline__ T sqr(T a);
+template <> __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+template <> __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+template <> __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+template <> __device__ __forceinline__ float dvd(float a, float b) { return __fdiv_rn(a, b); }
+template <> __device__ __forceinline__ float sqr(float a) { return __fsqrt_rn(a); }
+template <> __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+template <> __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+template <> __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+template <> __device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+template <> __device__ __forceinline__ double sqr(double a) { return __dsqrt_rn(a); }
+
+// Matlab's min(a, b) for ordered values; a NaN a is kept (as the restatement)
+template <class T>
+__device__ __forceinline__ T mn(T a, T b)
+{
+    return (a <= b || a != a) ? a : b;
+}
+
+template <class T>
+struct Cell {
+    int y, x, z;
+    long long g;
+    __device__ Cell(const MTArgs<T> &A, long long g_) : g(g_)
+    {
+        y = (int)(g % A.rows);
+        const long long q = g / A.rows;
+        x = (int)(q % A.cols);
+        z = (int)(q / A.cols);
+    }
+};
+// face arrays: p1 rows x (cols+1) x slices (along columns), p2 (rows+1) x
+// cols x slices (along rows), p3 rows x cols x (slices+1) (along slices)
+template <class T>
+__device__ __forceinline__ long long j1(const MTArgs<T> &A, int y, int x, int z)
+{
+    return ((long long)z * (A.cols + 1) + x) * A.rows + y;
+}
+template <class T>
+__device__ __forceinline__ long long j2(const MTArgs<T> &A, int y, int x, int z)
+{
+    return ((long long)z * A.cols + x) * (A.rows + 1) + y;
+}
+template <class T>
+__device__ __forceinline__ long long j3(const MTArgs<T> &A, int y, int x, int z)
+{
+    return ((long long)z * A.cols + x) * A.rows + y;
+}
+
+template <class T>
+__device__ __forceinline__ bool finished(const MTArgs<T> &A)
+{
+    return *(volatile int *)&A.ctl->done != 0;
+}
+
+#define MT_LOOP(total)                                                                 \
+    for (long long t = blockIdx.x * (long long)kThreads + threadIdx.x; t < (total);    \
+         t += (long long)gridDim.x * kThreads)
+
+// ud of flow label k at cell g: divp - ((A - B) + u/cc)
+template <class T, int M>
+__device__ __forceinline__ T ud(const MTArgs<T> &A, int k, long long g)
+{
+    const long long o = (long long)k * A.n + g;
+    T a, b;
+    if (M == MT_BINARY) {
+        a = A.ps[g];
+        b = A.pt[g];
+    } else if (M == MT_POTTS) {
+        a = A.ps[g];
+        b = A.pt[o];
+    } else {
+        a = A.pt[o];
+        b = A.pt[o + A.n];
+    }
+    return sub(A.divp[o], add(sub(a, b), dvd(A.u[o], A.cc)));
+}
+
+template <class T, int M, int D>
+__global__ void mt_step(const MTArgs<T> A)
+{
+    if (finished(A))
+        return;
+    MT_LOOP(A.n * A.nflow)
+    {
+        const int k = (int)(t / A.n);
+        const Cell<T> c(A, t - (long long)k * A.n);
+        const T u0 = ud<T, M>(A, k, c.g);
+        // binary: pp + steps*(d); Potts/Ishikawa: steps*(d) + pp
+        auto upd = [&](T *f, T nb) {
+            const T s = mul(A.steps, sub(u0, nb));
+            *f = (M == MT_BINARY) ? add(*f, s) : add(s, *f);
+        };
+        if (c.x >= 1)
+            upd(A.p1 + (long long)k * A.f1 + j1(A, c.y, c.x, c.z), ud<T, M>(A, k, c.g - A.rows));
+        if (c.y >= 1)
+            upd(A.p2 + (long long)k * A.f2 + j2(A, c.y, c.x, c.z), ud<T, M>(A, k, c.g - 1));
+        if (D == 3 && c.z >= 1)
+            upd(A.p3 + (long long)k * A.f3 + j3(A, c.y, c.x, c.z),
+                ud<T, M>(A, k, c.g - (long long)A.rows * A.cols));
+    }
+}
+
+template <class T, int M, int D>
+__global__ void mt_gk(const MTArgs<T> A)
+{
+    if (finished(A))
+        return;
+    MT_LOOP(A.n * A.nflow)
+    {
+        const int k = (int)(t / A.n);
+        const Cell<T> c(A, t - (long long)k * A.n);
+        const T *f1 = A.p1 + (long long)k * A.f1, *f2 = A.p2 + (long long)k * A.f2;
+        const T a = f1[j1(A, c.y, c.x, c.z)], b = f1[j1(A, c.y, c.x + 1, c.z)];
+        const T d = A.p2[(long long)k * A.f2 + j2(A, c.y, c.x, c.z)], e = f2[j2(A, c.y + 1, c.x, c.z)];
+        T s = add(mul(a, a), mul(b, b));
+        s = add(s, mul(d, d));
+        s = add(s, mul(e, e));
+        if (D == 3) {
+            const T *f3 = A.p3 + (long long)k * A.f3;
+            const T p = f3[j3(A, c.y, c.x, c.z)], q = f3[j3(A, c.y, c.x, c.z + 1)];
+            s = add(s, mul(p, p));
+            s = add(s, mul(q, q));
+        }
+        const T g = sqr(mul(s, A.half));
+        const T al = A.alpha[t];
+        const T r = (g <= al) ? (T)1 : dvd(g, al);
+        A.gk[t] = dvd((T)1, r);
+    }
+}
+
+template <class T, int M, int D>
+__global__ void mt_rescale(const MTArgs<T> A)
+{
+    if (finished(A))
+        return;
+    MT_LOOP(A.n * A.nflow)
+    {
+        const int k = (int)(t / A.n);
+        const Cell<T> c(A, t - (long long)k * A.n);
+        const T g0 = A.gk[t];
+        auto sc = [&](T *f, T gnb) { *f = mul(mul(A.half, add(g0, gnb)), *f); };
+        if (c.x >= 1)
+            sc(A.p1 + (long long)k * A.f1 + j1(A, c.y, c.x, c.z), A.gk[t - A.rows]);
+        if (c.y >= 1)
+            sc(A.p2 + (long long)k * A.f2 + j2(A, c.y, c.x, c.z), A.gk[t - 1]);
+        if (D == 3 && c.z >= 1)
+            sc(A.p3 + (long long)k * A.f3 + j3(A, c.y, c.x, c.z), A.gk[t - (long long)A.rows * A.cols]);
+    }
+}
+
+template <class T, int D>
+__device__ __forceinline__ T divergence(const MTArgs<T> &A, int k, const Cell<T> &c)
+{
+    const T *f1 = A.p1 + (long long)k * A.f1, *f2 = A.p2 + (long long)k * A.f2;
+    T d = sub(f1[j1(A, c.y, c.x + 1, c.z)], f1[j1(A, c.y, c.x, c.z)]);
+    d = add(d, f2[j2(A, c.y + 1, c.x, c.z)]);
+    d = sub(d, f2[j2(A, c.y, c.x, c.z)]);
+    if (D == 3) {
+        const T *f3 = A.p3 + (long long)k * A.f3;
+        d = add(d, f3[j3(A, c.y, c.x, c.z + 1)]);
+        d = sub(d, f3[j3(A, c.y, c.x, c.z)]);
+    }
+    return d;
+}
+
+template <class T, int M, int D>
+__global__ void mt_cell(const MTArgs<T> A)
+{
+    __shared__ double s_red[kThreads / 32];
+    __shared__ int s_last;
+    if (finished(A))
+        return;
+    const int it = *(volatile int *)&A.ctl->iter;
+    double err = 0.0;
+    MT_LOOP(A.n)
+    {
+        const Cell<T> c(A, t);
+        const long long g = t, n = A.n;
+        for (int k = 0; k < A.nflow; ++k)
+            A.divp[(long long)k * n + g] = divergence<T, D>(A, k, c);
+        if (M == MT_BINARY) {
+            const T dv = A.divp[g], u = A.u[g], uc = dvd(u, A.cc);
+            const T ps = mn(add(sub(add(dv, A.pt[g]), uc), A.one_over_cc), A.cs[g]);
+            const T pt = mn(add(add(-dv, ps), uc), A.ct[g]);
+            const T e = mul(A.cc, sub(add(dv, pt), ps));
+            A.ps[g] = ps;
+            A.pt[g] = pt;
+            A.u[g] = sub(u, e);
+            err += fabs((double)e);
+        } else if (M == MT_POTTS) {
+            const T ps = A.ps[g];
+            T pd = (T)0;
+            for (int k = 0; k < A.nlab; ++k) {
+                const long long o = (long long)k * n + g;
+                const T dv = A.divp[o], uc = dvd(A.u[o], A.cc);
+                const T pt = mn(add(add(-dv, ps), uc), A.ct[o]);
+                A.pt[o] = pt;
+                pd = add(pd, sub(add(dv, pt), uc));
+            }
+            const T psn = add(dvd(pd, (T)A.nlab), A.one_over_ccl);
+            A.ps[g] = psn;
+            for (int k = 0; k < A.nlab; ++k) {
+                const long long o = (long long)k * n + g;
+                const T e = mul(A.cc, sub(add(A.divp[o], A.pt[o]), psn));
+                A.u[o] = sub(A.u[o], e);
+                err += fabs((double)e);
+            }
+        } else {
+            const int L = A.nlab;
+            for (int k = 0; k < L; ++k) {
+                const long long o = (long long)k * n + g;
+                T v;
+                if (k == 0) {
+                    v = add(sub(add(A.divp[g], A.pt[g + n]), dvd(A.u[g], A.cc)), A.one_over_cc);
+                } else {
+                    const long long ob = o - n;  // label k-1: its pt is the new one
+                    v = add(add(-A.divp[ob], A.pt[ob]), dvd(A.u[ob], A.cc));
+                    if (k < L - 1) {
+                        v = sub(add(add(v, A.divp[o]), A.pt[o + n]), dvd(A.u[o], A.cc));
+                        v = dvd(v, (T)2);
+                    }
+                }
+                A.pt[o] = mn(v, A.ct[o]);
+            }
+            for (int k = 0; k < L - 1; ++k) {
+                const long long o = (long long)k * n + g;
+                const T e = mul(A.cc, sub(add(A.divp[o], A.pt[o + n]), A.pt[o]));
+                A.u[o] = sub(A.u[o], e);
+                err += fabs((double)e);
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+        err += __shfl_xor_sync(0xffffffffu, err, o);
+    if ((threadIdx.x & 31) == 0)
+        s_red[threadIdx.x >> 5] = err;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w)
+            b += s_red[w];
+        A.partials[blockIdx.x] = b;
+        __threadfence();
+        s_last = (atomicAdd(&A.ctl->ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        __threadfence();
+        double tot = 0.0;
+        for (unsigned int b = 0; b < gridDim.x; ++b)
+            tot += __ldcg(A.partials + b);
+        const T e = (T)(tot / A.ctl->vol);
+        A.erriter[it] = e;
+        if (e < A.beta) {
+            A.ctl->done = 1;
+            A.ctl->it_num = it + 1;
+        } else if (it + 1 >= A.ctl->max_it) {
+            A.ctl->done = 1;
+            A.ctl->it_num = A.ctl->max_it;
+        }
+        A.ctl->ticket = 0;
+        A.ctl->iter = it + 1;
+        __threadfence();
+    }
+}
+
+// initial state (the .m files before their loop)
+template <class T, int M>
+__global__ void mt_init(const MTArgs<T> A)
+{
+    MT_LOOP(A.n)
+    {
+        const long long g = t, n = A.n;
+        if (M == MT_BINARY) {
+            const T cs = A.cs[g], ct = A.ct[g];
+            A.u[g] = (sub(cs, ct) >= (T)0) ? (T)1 : (T)0;
+            const T ps = mn(cs, ct);
+            A.ps[g] = ps;
+            A.pt[g] = ps;
+            continue;
+        }
+        // [m, I] = min(Ct, [], labels): the first minimum
+        T m = A.ct[g];
+        int I = 0;
+        for (int k = 1; k < A.nlab; ++k) {
+            const T v = A.ct[(long long)k * n + g];
+            if (v < m) {
+                m = v;
+                I = k;
+            }
+        }
+        for (int k = 0; k < A.nlab; ++k)
+            A.pt[(long long)k * n + g] = m;
+        if (M == MT_POTTS) {
+            A.ps[g] = m;
+            for (int k = 0; k < A.nlab; ++k)
+                A.u[(long long)k * n + g] = (I == k) ? (T)1 : (T)0;
+        } else {
+            for (int k = 0; k < A.nlab - 1; ++k)  // u(:,:,k) = init > k, 1-based
+                A.u[(long long)k * n + g] = (I > k) ? (T)1 : (T)0;
+        }
+    }
+}
+
+int mt_grid(long long n, int sms)
+{
+    long long b = (n + kThreads - 1) / kThreads;
+    const long long cap = (long long)sms * 8;
+    return (int)(b < 1 ? 1 : (b < cap ? b : cap));
+}
+
+template <class T, int M, int D>
+asets_status mt_run(asets_context *ctx, int rows, int cols, int slices, int nlab,
+                    const void *Cs, const void *Ct, const void *alpha, int iterNum, double beta,
+                    double cc, double steps, void *u_out, void *err_out, int *itNum)
+{
+    cudaStream_t st = context_stream(ctx);
+    const int sms = context_num_sms(ctx);
+    MTArgs<T> A;
+    memset(&A, 0, sizeof A);
+    A.rows = rows;
+    A.cols = cols;
+    A.slices = slices;
+    A.nlab = (M == MT_BINARY) ? 1 : nlab;
+    A.nflow = (M == MT_ISHIKAWA) ? nlab - 1 : A.nlab;
+    const long long n = (long long)rows * cols * slices;
+    A.n = n;
+    A.f1 = (long long)rows * (cols + 1) * slices;
+    A.f2 = (long long)(rows + 1) * cols * slices;
+    A.f3 = D == 3 ? (long long)rows * cols * (slices + 1) : 0;
+    // scalars rounded to the class of Ct, as Matlab combines them
+    A.cc = (T)cc;
+    A.steps = (T)steps;
+    A.half = (T)0.5;
+    A.one_over_cc = (T)(1.0 / cc);
+    A.one_over_ccl = (T)(1.0 / (cc * A.nlab));
+    A.beta = (T)beta;
+    const int nct = A.nlab, nu = (M == MT_ISHIKAWA) ? nlab - 1 : A.nlab;
+    const int npt = A.nlab;
+    std::vector<void *> bufs;
+    auto get = [&](T **p, long long count) {
+        void *v = nullptr;
+        if (cudaMallocAsync(&v, (size_t)(count < 1 ? 1 : count) * sizeof(T), st) != cudaSuccess)
+            return false;
+        bufs.push_back(v);
+        *p = static_cast<T *>(v);
+        return true;
+    };
+    T *cs = nullptr, *ct = nullptr, *al = nullptr;
+    asets_status status = ASETS_OK;
+    const int grid = mt_grid(n * A.nflow, sms), gcell = mt_grid(n, sms);
+    bool ok = get(&ct, n * nct) && get(&al, n * A.nflow) && get(&A.u, n * nu) &&
+              get(&A.pt, n * npt) && get(&A.ps, n) && get(&A.divp, n * A.nflow) &&
+              get(&A.gk, n * A.nflow) && get(&A.p1, A.f1 * A.nflow) && get(&A.p2, A.f2 * A.nflow) &&
+              get(&A.p3, A.f3 * A.nflow) && get(&A.erriter, iterNum) &&
+              (M != MT_BINARY || get(&cs, n));
+    void *pv = nullptr;
+    ok = ok && cudaMallocAsync(&pv, sizeof(MTCtl) + (size_t)gcell * sizeof(double), st) == cudaSuccess;
+    if (ok) {
+        bufs.push_back(pv);
+        A.ctl = static_cast<MTCtl *>(pv);
+        A.partials = reinterpret_cast<double *>(static_cast<char *>(pv) + sizeof(MTCtl));
+    }
+    cudaError_t e = cudaSuccess;
+    MTCtl c0;
+    memset(&c0, 0, sizeof c0);
+    c0.max_it = iterNum;
+    c0.beta = beta;
+    c0.vol = (M == MT_BINARY)    ? (double)n
+             : (M == MT_POTTS)   ? (double)(n * nlab)
+                                 : (double)(n * nlab - 1);  // rows*cols*nlab-1, as the .m files
+    if (!ok) {
+        status = ASETS_ERR_OUT_OF_MEMORY;
+        set_last_error("Matlab-semantics solver: out of device memory");
+    } else {
+        e = cudaMemcpyAsync(ct, Ct, sizeof(T) * n * nct, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(al, alpha, sizeof(T) * n * A.nflow, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && M == MT_BINARY)
+            e = cudaMemcpyAsync(cs, Cs, sizeof(T) * n, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(A.ctl, &c0, sizeof c0, cudaMemcpyHostToDevice, st);
+        T *zero[] = {A.divp, A.p1, A.p2, A.p3, A.erriter};
+        const long long zn[] = {n * A.nflow, A.f1 * A.nflow, A.f2 * A.nflow, A.f3 * A.nflow,
+                                (long long)iterNum};
+        for (int i = 0; i < 5 && e == cudaSuccess; ++i)
+            if (zn[i] > 0)
+                e = cudaMemsetAsync(zero[i], 0, sizeof(T) * zn[i], st);
+        A.cs = cs;
+        A.ct = ct;
+        A.alpha = al;
+        if (e == cudaSuccess) {
+            mt_init<T, M><<<gcell, kThreads, 0, st>>>(A);
+            e = cudaGetLastError();
+        }
+        constexpr int kChunk = 16;
+        int h_done = 0;
+        for (int done_it = 0; e == cudaSuccess && done_it < iterNum; done_it += kChunk) {
+            for (int i = 0; i < kChunk && done_it + i < iterNum; ++i) {
+                mt_step<T, M, D><<<grid, kThreads, 0, st>>>(A);
+                mt_gk<T, M, D><<<grid, kThreads, 0, st>>>(A);
+                mt_rescale<T, M, D><<<grid, kThreads, 0, st>>>(A);
+                mt_cell<T, M, D><<<gcell, kThreads, 0, st>>>(A);
+            }
+            e = cudaGetLastError();
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(&h_done, &A.ctl->done, sizeof(int), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess)
+                e = cudaStreamSynchronize(st);
+            if (h_done)
+                break;
+        }
+        MTCtl out;
+        memset(&out, 0, sizeof out);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&out, A.ctl, sizeof out, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(u_out, A.u, sizeof(T) * n * nu, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && err_out)
+            e = cudaMemcpyAsync(err_out, A.erriter, sizeof(T) * iterNum, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess && itNum)
+            *itNum = out.it_num;
+    }
+    if (status == ASETS_OK && e != cudaSuccess) {
+        cudaGetLastError();
+        status = ASETS_ERR_CUDA;
+        set_last_error((std::string("Matlab-semantics solver: ") + cudaGetErrorString(e)).c_str());
+    }
+    for (void *p : bufs)
+        cudaFreeAsync(p, st);
+    cudaStreamSynchronize(st);
+    return status;
+}
+
+template <class T>
+asets_status mt_dispatch(int model, int dim, asets_context *ctx, int rows, int cols, int slices,
+                         int nlab, const void *Cs, const void *Ct, const void *alpha, int iterNum,
+                         double beta, double cc, double steps, void *u, void *err, int *itNum)
+{
+#define MT_CASE(M, D)                                                                       \
+    if (model == M && dim == D)                                                             \
+        return mt_run<T, M, D>(ctx, rows, cols, slices, nlab, Cs, Ct, alpha, iterNum, beta, \
+                               cc, steps, u, err, itNum);
+    MT_CASE(MT_BINARY, 2)
+    MT_CASE(MT_BINARY, 3)
+    MT_CASE(MT_POTTS, 2)
+    MT_CASE(MT_POTTS, 3)
+    MT_CASE(MT_ISHIKAWA, 2)
+    MT_CASE(MT_ISHIKAWA, 3)
+#undef MT_CASE
+    set_last_error("Matlab-semantics solver: bad model or dimension");
+    return ASETS_ERR_INVALID_ARG;
+}
+
+}  // namespace
+
+extern "C" ASETS_API asets_status asets_matlab_solve(
+    asets_context *ctx, int model, int precision, int dim, int rows, int cols, int slices,
+    int nlab, const void *Cs, const void *Ct, const void *alpha, int iterNum, double beta,
+    double cc, double steps, void *u, void *erriter, int *itNum, float *seconds)
+{
+    if (!ctx || !Ct || !alpha || !u || iterNum < 1 || rows < 1 || cols < 1 || slices < 1 ||
+        (dim != 2 && dim != 3) || (dim == 2 && slices != 1) || (precision != 4 && precision != 8) ||
+        (model == MT_BINARY && !Cs) || (model == MT_POTTS && nlab < 1) ||
+        (model == MT_ISHIKAWA && nlab < 2) || model < 0 || model > 2) {
+        set_last_error("asets_matlab_solve: bad arguments");
+        return ASETS_ERR_INVALID_ARG;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(context_device(ctx));
+    const asets_status s =
+        precision == 8 ? mt_dispatch<double>(model, dim, ctx, rows, cols, slices, nlab, Cs, Ct,
+                                             alpha, iterNum, beta, cc, steps, u, erriter, itNum)
+                       : mt_dispatch<float>(model, dim, ctx, rows, cols, slices, nlab, Cs, Ct,
+                                            alpha, iterNum, beta, cc, steps, u, erriter, itNum);
+    cudaSetDevice(prev);
+    if (seconds)
+        *seconds = std::chrono::duration<float>(std::chrono::steady_clock::now() - t0).count();
+    return s;
+}

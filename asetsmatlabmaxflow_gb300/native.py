@@ -98,6 +98,12 @@ _SIGS = {
     "asets_solver_level": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.POINTER(_VP)]),
     "asets_solver_multilevel_stats": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, ctypes.POINTER(ctypes.c_int)]),
     "asets_selftest_wait_timeout": (ctypes.c_int, [_VP]),
+    "asets_matlab_solve": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          _VP, _VP, _VP, ctypes.c_int, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_double, _VP, _VP,
+                                          ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_float)]),
     "asets_dag_full_flow": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP,
                                            _VP, _VP, _VP, ctypes.c_int, ctypes.c_double,

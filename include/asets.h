@@ -365,6 +365,24 @@ ASETS_API asets_status asets_dag_full_flow(asets_context *ctx, int precision, in
                                            void *const *p3);
 
 /* ------------------------------------------------------------------------
+ * Matlab-semantics solvers: the reference's Matlab twins of the six solvers
+ * (maxflow/asets{BinaryMF,Potts,Ishikawa}{2D,3D}.m, the path its tutorials
+ * run with gpuArray), computed in the class of Ct (precision 4 or 8) with
+ * the .m files' initialisation, expression order and `<` break rule.
+ * model: 0 binary (Cs needed), 1 Potts, 2 Ishikawa; Ct rows*cols*slices*L
+ * (binary L = 1); alpha per flow label (binary 1, Potts L, Ishikawa L-1
+ * slices); host arrays of that precision.  Outputs u (binary N, Potts N*L,
+ * Ishikawa N*(L-1)), erriter (iterNum, zero after the break; Ishikawa's
+ * denominator is N*L-1 as in the .m files), itNum = the 1-based iteration
+ * of the break or iterNum, seconds = wall time.
+ * ---------------------------------------------------------------------- */
+ASETS_API asets_status asets_matlab_solve(asets_context *ctx, int model, int precision, int dim,
+                                          int rows, int cols, int slices, int nlab,
+                                          const void *Cs, const void *Ct, const void *alpha,
+                                          int iterNum, double beta, double cc, double steps,
+                                          void *u, void *erriter, int *itNum, float *seconds);
+
+/* ------------------------------------------------------------------------
  * Cost terms and regularisation weights on the GPU: the step before the
  * solvers in the reference's applications (applications/*.m; no counterpart
  * in its C code).  Arrays in Matlab layout, label slowest; `where` says
