@@ -53,7 +53,32 @@ def parse():
                     help="run one solve of N iterations of the workload and exit (for ncu)")
     ap.add_argument("--shape", default="256,256,256", help="volume for --profile-iters")
     ap.add_argument("--tile-config", type=int, default=0, help="kernel variant for --profile-iters")
+    ap.add_argument("--profile-model", default="binary", choices=["binary", "potts"],
+                    help="model for --profile-iters (potts: the warm-start workload, seed 1000000)")
+    ap.add_argument("--profile-conv", type=int, default=0,
+                    help="run the warm-start network's forward pass on an S^3 volume and exit")
     return ap.parse_args()
+
+
+def profile_conv(args):
+    """Five forward passes of the warm-start network (committed weights) on
+    an S^3 volume of 6 labels, for profilers."""
+    import torch
+
+    from asetsmatlabmaxflow_gb300 import warmstart as W
+
+    net, _, _ = W.load()
+    n = args.profile_conv ** 3
+    dims = (args.profile_conv,) * 3
+    g = torch.Generator(device="cuda").manual_seed(0)
+    ct = torch.rand(n * 6, device="cuda", generator=g)
+    a = torch.full((n,), 0.3, device="cuda")
+    outs = [torch.empty(n * 6, device="cuda"), torch.empty(n, device="cuda")] + \
+        [torch.empty(n * 6, device="cuda") for _ in range(4)]
+    for _ in range(5):
+        net.predict(dims, ct, a, *outs)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_conv": list(dims), "launches": 5 * 5}))
 
 
 def profile_run(args):
@@ -61,6 +86,17 @@ def profile_run(args):
     from asetsmatlabmaxflow_gb300 import native as N
     from asetsmatlabmaxflow_gb300 import synth
 
+    if args.profile_model == "potts":
+        from asetsmatlabmaxflow_gb300 import warmstart as W
+
+        run = W.Runner()
+        ct6, a1, af = W.problem(W.HELDOUT_SEED0)
+        run.load(ct6, af)
+        it = run.s.run(args.profile_iters, 0.0, W.CC, W.STEPS, tile_config=args.tile_config)
+        ms, n = run.s.last_run_stats()
+        print(json.dumps({"profile_run": "potts 128^3 L=6", "iterations": it,
+                          "ms_per_iteration": ms / max(args.profile_iters, 1)}))
+        return
     shape = tuple(int(x) for x in args.shape.split(","))
     cs, ct, alpha = synth.binary3d(seed=0, shape=shape)
     s = N.Solver(N.Context.default(), "binary", shape)
@@ -292,6 +328,9 @@ def main():
     args = parse()
     if args.profile_iters:
         profile_run(args)
+        return
+    if args.profile_conv:
+        profile_conv(args)
         return
     world, rank, local, pg = dist_setup()
     if args.impl == "reference":
