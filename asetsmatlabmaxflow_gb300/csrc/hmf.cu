@@ -17,7 +17,19 @@
 // parents, each child weighted 1/(its number of parents)) shares the spatial
 // passes; its iteration is spatial flows first, then one per-pixel pass for
 // PushDownFlows (top-down list), PushCapacityUp (bottom-up) and the labels.
-// Not built: the anisotropic lx/ly branch and MaxPseudoFlow.
+//
+// Geodesic branch (nodes with direction fields lx, ly (, lz); asetsHMF2D.m
+// :228-247, asetsHMF3D.m:215-236, asetsDAGMF2D.m:275-294): the fields are
+// normalised once at initialisation (k_norm_dirs); after the gradient step
+// k_exempt_a forms per cell the exemption amount a (into g) and
+// k_exempt_e per face the exempt flow e, taken off the flow before the
+// projection and added back in the rescale.
+//
+// Pseudo-flow (asetsHMF2D.m / 3D MaxPseudoFlow): one per-pixel pass for the
+// capacity reset, push-down, the labels u*exp(-g/cc) normalised over the
+// leaves and the push-up of capacity requests, then the same spatial passes
+// on steps*g; at the end each inner node's u is the sum of its children's.
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -39,6 +51,8 @@ struct NodeDev {
     int parent, child_begin, nchild;
     int nparent;     // DAG: number of parents (parent = the first)
     T wdiv;          // DAG: sum of the children's weights squared (+1 below the root)
+    T *l[3];         // direction fields (normalised in place) or null
+    int nnorm;       // normalisations at initialisation (DAG: paths from the root)
 };
 
 template <class T>
@@ -53,6 +67,7 @@ struct HArgs {
     const int *order;   // DAG: the top-down node list
     T *pn;              // DAG: pushed-down flow of multi-parent nodes
     T *pt, *u, *div, *g, *p1, *p2, *p3;
+    T *e1, *e2, *e3;  // exempt flow per face (nodes with direction fields)
     double *cost;  // [m][2]: sum u*Ct (leaves), sum u*div (non-root)
 };
 
@@ -71,6 +86,9 @@ template <> __device__ __forceinline__ double sub(double a, double b) { return _
 template <> __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
 template <> __device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
 template <> __device__ __forceinline__ double sqr(double a) { return __dsqrt_rn(a); }
+template <class T> __device__ __forceinline__ T expo(T a);
+template <> __device__ __forceinline__ float expo(float a) { return expf(a); }
+template <> __device__ __forceinline__ double expo(double a) { return exp(a); }
 
 // pixel c = (z*d2 + x)*d1 + y; face arrays: p1 (d1-1) x d2 x d3, p2
 // d1 x (d2-1) x d3, p3 d1 x d2 x (d3-1), each face indexed by the pixel
@@ -226,13 +244,21 @@ __global__ void k4_rescale(const HArgs<T> A)
         const Pix<T> p(A, t - (long long)(i - 1) * A.n);
         const T *g = A.g + (long long)i * A.n;
         const T gc = g[p.c];
-        auto scale = [&](T *f, T gn) { *f = mul(mul((T)0.5, *f), add(gn, gc)); };
+        const bool ex = A.nodes[i].l[0] != nullptr;
+        // p = 0.5 p (g(k+1) + g(k)), or e + that with direction fields
+        auto scale = [&](T *f, const T *e, T gn) {
+            const T r = mul(mul((T)0.5, *f), add(gn, gc));
+            *f = ex ? add(*e, r) : r;
+        };
+        long long o = (long long)i * A.f1 + i1(A, p.y, p.x, p.z);
         if (p.y + 1 < A.d1)
-            scale(A.p1 + (long long)i * A.f1 + i1(A, p.y, p.x, p.z), g[p.c + 1]);
+            scale(A.p1 + o, A.e1 + o, g[p.c + 1]);
+        o = (long long)i * A.f2 + i2(A, p.y, p.x, p.z);
         if (p.x + 1 < A.d2)
-            scale(A.p2 + (long long)i * A.f2 + i2(A, p.y, p.x, p.z), g[p.c + A.d1]);
+            scale(A.p2 + o, A.e2 + o, g[p.c + A.d1]);
+        o = (long long)i * A.f3 + i3(A, p.y, p.x, p.z);
         if (A.dim == 3 && p.z + 1 < A.d3)
-            scale(A.p3 + (long long)i * A.f3 + i3(A, p.y, p.x, p.z), g[p.c + (long long)A.d1 * A.d2]);
+            scale(A.p3 + o, A.e3 + o, g[p.c + (long long)A.d1 * A.d2]);
     }
 }
 
@@ -260,6 +286,201 @@ __global__ void k5_divergence(const HArgs<T> A)
                 d = sub(d, f3[i3(A, p.y, p.x, p.z - 1)]);
         }
         A.div[(long long)i * A.n + p.c] = d;
+    }
+}
+
+// InitializeFullFlow / InitializePseudoFlow: unit direction vectors, 0 where
+// sqrt(lx^2 + ly^2 (+ lz^2)) is at most 0.001 (compared in T).  The DAG
+// classes initialise a node once per path from the root (each parent
+// recurses into it), and the normalisation is repeated as often.
+template <class T>
+__global__ void k_norm_dirs(const HArgs<T> A)
+{
+    H_LOOP(A.n * A.m)
+    {
+        const int i = (int)(t / A.n);
+        const long long c = t - (long long)i * A.n;
+        const NodeDev<T> &nd = A.nodes[i];
+        T *const *l = nd.l;
+        if (!l[0])
+            continue;
+        T v[3] = {l[0][c], l[1][c], A.dim == 3 ? l[2][c] : (T)0};
+        for (int r = 0; r < nd.nnorm; ++r) {
+            T s = mul(v[0], v[0]);
+            for (int k = 1; k < A.dim; ++k)
+                s = add(s, mul(v[k], v[k]));
+            const T den = sqr(s);
+            const bool keep = den > (T)0.001;
+            for (int k = 0; k < A.dim; ++k)
+                v[k] = keep ? dvd(v[k], den) : (T)0;
+        }
+        for (int k = 0; k < A.dim; ++k)
+            l[k][c] = v[k];
+    }
+}
+
+// max((m).*v.*l, 0): x for x > 0, else +0 (NaN gives 0)
+template <class T>
+__device__ __forceinline__ T pos_part(bool m, T v, T l)
+{
+    const T x = mul(mul(m ? (T)1 : (T)0, v), l);
+    return x > (T)0 ? x : (T)0;
+}
+
+// exemption amount a per cell (into g): first axis backward then forward
+// (one addition, either order), then each further axis forward, backward
+template <class T>
+__global__ void k_exempt_a(const HArgs<T> A)
+{
+    H_LOOP(A.n * (A.m - 1))
+    {
+        const int i = 1 + (int)(t / A.n);
+        T *const *l = A.nodes[i].l;
+        if (!l[0])
+            continue;
+        const Pix<T> p(A, t - (long long)(i - 1) * A.n);
+        const T *f1 = A.p1 + (long long)i * A.f1;
+        const T *f2 = A.p2 + (long long)i * A.f2;
+        const T *f3 = A.p3 + (long long)i * A.f3;
+        T a = (T)0;
+        if (p.y >= 1) {
+            const T v = f1[i1(A, p.y - 1, p.x, p.z)];
+            a = add(a, pos_part(v < (T)0, v, l[0][p.c]));
+        }
+        if (p.y + 1 < A.d1) {
+            const T v = f1[i1(A, p.y, p.x, p.z)];
+            a = add(a, pos_part(v > (T)0, v, l[0][p.c]));
+        }
+        if (p.x + 1 < A.d2) {
+            const T v = f2[i2(A, p.y, p.x, p.z)];
+            a = add(a, pos_part(v > (T)0, v, l[1][p.c]));
+        }
+        if (p.x >= 1) {
+            const T v = f2[i2(A, p.y, p.x - 1, p.z)];
+            a = add(a, pos_part(v < (T)0, v, l[1][p.c]));
+        }
+        if (A.dim == 3) {
+            if (p.z + 1 < A.d3) {
+                const T v = f3[i3(A, p.y, p.x, p.z)];
+                a = add(a, pos_part(v > (T)0, v, l[2][p.c]));
+            }
+            if (p.z >= 1) {
+                const T v = f3[i3(A, p.y, p.x, p.z - 1)];
+                a = add(a, pos_part(v < (T)0, v, l[2][p.c]));
+            }
+        }
+        A.g[(long long)i * A.n + p.c] = a;
+    }
+}
+
+// exempt flow of each forward face: the part along the direction of the cell
+// it leaves, e = (p>0 & l(k)>0) l(k) a(k) + (p<0 & l(k+1)<0) l(k+1) a(k+1);
+// the flow keeps p - e until the rescale adds e back
+template <class T>
+__global__ void k_exempt_e(const HArgs<T> A)
+{
+    H_LOOP(A.n * (A.m - 1))
+    {
+        const int i = 1 + (int)(t / A.n);
+        T *const *l = A.nodes[i].l;
+        if (!l[0])
+            continue;
+        const Pix<T> p(A, t - (long long)(i - 1) * A.n);
+        const T *a = A.g + (long long)i * A.n;
+        auto face = [&](T *f, T *e, const T *lk, long long step) {
+            const T v = *f;
+            const T llo = lk[p.c], lhi = lk[p.c + step];
+            T x = mul(mul((v > (T)0 && llo > (T)0) ? (T)1 : (T)0, llo), a[p.c]);
+            x = add(x, mul(mul((v < (T)0 && lhi < (T)0) ? (T)1 : (T)0, lhi), a[p.c + step]));
+            *e = x;
+            *f = sub(v, x);
+        };
+        long long o = (long long)i * A.f1 + i1(A, p.y, p.x, p.z);
+        if (p.y + 1 < A.d1)
+            face(A.p1 + o, A.e1 + o, l[0], 1);
+        o = (long long)i * A.f2 + i2(A, p.y, p.x, p.z);
+        if (p.x + 1 < A.d2)
+            face(A.p2 + o, A.e2 + o, l[1], A.d1);
+        o = (long long)i * A.f3 + i3(A, p.y, p.x, p.z);
+        if (A.dim == 3 && p.z + 1 < A.d3)
+            face(A.p3 + o, A.e3 + o, l[2], (long long)A.d1 * A.d2);
+    }
+}
+
+// MaxPseudoFlow, per pixel: ResetPseudoFlowCapacity, PushDownPseudoFlows,
+// UpdatePseudoFlowLabels (the root's g sums the leaves' labels),
+// NormalizePseudoFlowLabels, PushUpCapacityReqs, and steps*g of every
+// non-root node (UpdateSpatialPseudoFlows' first line).
+template <class T>
+__global__ void k_pseudo_point(const HArgs<T> A)
+{
+    H_LOOP(A.n)
+    {
+        const long long c = t;
+        T *g = A.g + c;
+        T *u = A.u + c;
+        const long long n = A.n;
+        for (int i = 0; i < A.m; ++i) {
+            const NodeDev<T> &nd = A.nodes[i];
+            g[i * n] = nd.nchild == 0 ? add(A.div[i * n + c], nd.ct[c]) : (T)0;
+        }
+        for (int i = 0; i < A.m; ++i) {
+            const NodeDev<T> &nd = A.nodes[i];
+            for (int j = 0; j < nd.nchild; ++j) {
+                const long long oc = (long long)A.children[nd.child_begin + j] * n;
+                g[oc] = add(g[oc], g[i * n]);
+            }
+        }
+        T acc = (T)0;
+        for (int i = 0; i < A.m; ++i) {
+            if (A.nodes[i].nchild != 0)
+                continue;
+            const T v = mul(u[i * n], expo(dvd(-g[i * n], A.cc)));
+            u[i * n] = v;
+            g[i * n] = v;
+            acc = add(acc, v);
+        }
+        for (int i = 0; i < A.m; ++i) {
+            if (A.nodes[i].nchild != 0)
+                continue;
+            T v = dvd(u[i * n], acc);
+            if (v > (T)1)
+                v = (T)1;
+            if (v < (T)0)
+                v = (T)0;
+            u[i * n] = v;
+        }
+        for (int i = A.m - 1; i >= 1; --i) {
+            const NodeDev<T> &nd = A.nodes[i];
+            if (nd.nchild == 0)
+                continue;
+            T s = (T)0;
+            for (int j = 0; j < nd.nchild; ++j)
+                s = add(s, g[(long long)A.children[nd.child_begin + j] * n]);
+            g[i * n] = s;
+        }
+        g[0] = (T)0;
+        for (int i = 1; i < A.m; ++i)
+            g[i * n] = mul(A.steps, g[i * n]);
+    }
+}
+
+// DeInitializePseudoFlow: an inner node's u is the sum of its children's
+template <class T>
+__global__ void k_pseudo_final(const HArgs<T> A)
+{
+    H_LOOP(A.n)
+    {
+        T *u = A.u + t;
+        for (int i = A.m - 1; i >= 0; --i) {
+            const NodeDev<T> &nd = A.nodes[i];
+            if (nd.nchild == 0)
+                continue;
+            T s = u[(long long)A.children[nd.child_begin] * A.n];
+            for (int j = 1; j < nd.nchild; ++j)
+                s = add(s, u[(long long)A.children[nd.child_begin + j] * A.n]);
+            u[(long long)i * A.n] = s;
+        }
     }
 }
 
@@ -398,13 +619,73 @@ int h_grid(long long n, int sms)
     return (int)(b < 1 ? 1 : (b < cap ? b : cap));
 }
 
+// gradient step on g, the geodesic exemption (nodes with direction fields),
+// flow magnitude and projection factor, rescale, divergence
 template <class T>
-asets_status run_hmf(asets_context *ctx, int dim, int d1, int d2, int d3, int m, const int *parent,
-                     const void *const *Ct, const void *const *alpha_arr, const double *alpha_s,
-                     int its, double steps, double cc, void *const *u_out, void *const *pt_out,
-                     void *const *div_out, void *const *g_out, void *const *p_out[3],
-                     double *data_cost, double *regu_cost)
+void spatial_passes(const HArgs<T> &A, int gn, cudaStream_t st, bool dirs)
 {
+    k2_gradient<T><<<gn, kThreads, 0, st>>>(A);
+    if (dirs) {
+        k_exempt_a<T><<<gn, kThreads, 0, st>>>(A);
+        k_exempt_e<T><<<gn, kThreads, 0, st>>>(A);
+    }
+    k3_projection<T><<<gn, kThreads, 0, st>>>(A);
+    k4_rescale<T><<<gn, kThreads, 0, st>>>(A);
+    k5_divergence<T><<<gn, kThreads, 0, st>>>(A);
+}
+
+// Device copies of the nodes' direction fields (ld[k][i], host, null for a
+// node without) and the exempt-flow buffers; false when out of memory.
+template <class T, class Get>
+bool setup_dirs(Get &get, cudaStream_t st, int dim, int m, void *const *const ld[3],
+                std::vector<NodeDev<T>> &nodes, HArgs<T> &A, cudaError_t &e, bool &any)
+{
+    any = false;
+    for (int i = 0; i < m; ++i) {
+        if (!ld[0] || !ld[0][i])
+            continue;
+        any = true;
+        void *vp = nullptr;
+        if (!get(&vp, sizeof(T) * A.n * dim))
+            return false;
+        for (int k = 0; k < dim; ++k) {
+            nodes[i].l[k] = static_cast<T *>(vp) + A.n * k;
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(nodes[i].l[k], ld[k][i], sizeof(T) * A.n, cudaMemcpyHostToDevice, st);
+        }
+    }
+    if (any) {
+        void *vp = nullptr;
+        if (!get(&vp, sizeof(T) * (A.f1 + A.f2 + A.f3) * m))
+            return false;
+        A.e1 = static_cast<T *>(vp);
+        A.e2 = A.e1 + A.f1 * m;
+        A.e3 = A.e2 + A.f2 * m;
+    }
+    return true;
+}
+
+// the normalised direction fields back into the caller's arrays
+template <class T>
+cudaError_t download_dirs(cudaStream_t st, int dim, int m, long long n, void *const *const ld[3],
+                          const std::vector<NodeDev<T>> &nodes)
+{
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < m && e == cudaSuccess; ++i)
+        for (int k = 0; k < dim && e == cudaSuccess && nodes[i].l[0]; ++k)
+            e = cudaMemcpyAsync(ld[k][i], nodes[i].l[k], sizeof(T) * n, cudaMemcpyDeviceToHost, st);
+    return e;
+}
+
+template <class T>
+asets_status run_hmf(asets_context *ctx, int algo, int dim, int d1, int d2, int d3, int m,
+                     const int *parent, const void *const *Ct, const void *const *alpha_arr,
+                     const double *alpha_s, void *const *const ld[3], int its, double steps,
+                     double cc, void *const *u_out, void *const *pt_out, void *const *div_out,
+                     void *const *g_out, void *const *p_out[3], double *data_cost,
+                     double *regu_cost)
+{
+    const bool pseudo = (algo == ASETS_HMF_PSEUDO_FLOW);
     cudaStream_t st = context_stream(ctx);
     const int sms = context_num_sms(ctx);
     const long long n = (long long)d1 * d2 * d3;
@@ -446,7 +727,8 @@ asets_status run_hmf(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
     A.cc = (T)cc;
     A.steps = (T)steps;
     A.inv_cc = (T)(1.0 / cc);
-    A.paren = (dim == 2) ? 1 : 0;  // asetsHMF2D.m parenthesises the gradient step
+    // asetsHMF2D.m parenthesises the full-flow gradient step, not the pseudo-flow one
+    A.paren = (dim == 2 && !pseudo) ? 1 : 0;
     std::vector<NodeDev<T>> nodes(m);
     void *vp = nullptr;
     cudaError_t e = cudaSuccess;
@@ -482,6 +764,7 @@ asets_status run_hmf(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
         nd.alpha_s = (T)(alpha_s ? alpha_s[i] : 0.0);
         nd.ct = nullptr;
         nd.alpha = nullptr;
+        nd.nnorm = 1;
         if (nchild[i] == 0 && e == cudaSuccess) {
             ok = get(&vp, sizeof(T) * n);
             if (ok) {
@@ -496,7 +779,12 @@ asets_status run_hmf(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
                 nd.alpha = static_cast<const T *>(vp);
             }
         }
+        // pseudo-flow starts from the leaves' labels
+        if (ok && pseudo && nchild[i] == 0 && e == cudaSuccess)
+            e = cudaMemcpyAsync(A.u + (long long)i * n, u_out[i], sizeof(T) * n, cudaMemcpyHostToDevice, st);
     }
+    bool dirs = false;
+    ok = ok && setup_dirs<T>(get, st, dim, m, ld, nodes, A, e, dirs);
     ok = ok && get(&vp, sizeof(NodeDev<T>) * m);
     if (ok && e == cudaSuccess) {
         e = cudaMemcpyAsync(vp, nodes.data(), sizeof(NodeDev<T>) * m, cudaMemcpyHostToDevice, st);
@@ -512,20 +800,25 @@ asets_status run_hmf(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
         set_last_error("asets_hmf_full_flow: out of device memory");
     } else if (e == cudaSuccess) {
         const int gp = h_grid(n, sms), gn = h_grid(n * (m - 1), sms);
+        if (dirs)
+            k_norm_dirs<T><<<h_grid(n * m, sms), kThreads, 0, st>>>(A);
         for (int it = 0; it < its && e == cudaSuccess; ++it) {
-            k1_pointwise<T><<<gp, kThreads, 0, st>>>(A);
-            if (m > 1) {
-                k2_gradient<T><<<gn, kThreads, 0, st>>>(A);
-                k3_projection<T><<<gn, kThreads, 0, st>>>(A);
-                k4_rescale<T><<<gn, kThreads, 0, st>>>(A);
-                k5_divergence<T><<<gn, kThreads, 0, st>>>(A);
-            }
+            if (pseudo)
+                k_pseudo_point<T><<<gp, kThreads, 0, st>>>(A);
+            else
+                k1_pointwise<T><<<gp, kThreads, 0, st>>>(A);
+            spatial_passes(A, gn, st, dirs);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) {
-            k_costs<T><<<h_grid(n * m, sms), kThreads, 0, st>>>(A);
+            if (pseudo)
+                k_pseudo_final<T><<<gp, kThreads, 0, st>>>(A);
+            else
+                k_costs<T><<<h_grid(n * m, sms), kThreads, 0, st>>>(A);
             e = cudaGetLastError();
         }
+        if (e == cudaSuccess && dirs)
+            e = download_dirs<T>(st, dim, m, n, ld, nodes);
         std::vector<double> cost(2 * m, 0.0);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(cost.data(), A.cost, sizeof(double) * 2 * m, cudaMemcpyDeviceToHost, st);
@@ -533,7 +826,7 @@ asets_status run_hmf(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
             const size_t nb = sizeof(T) * n;
             if (u_out && u_out[i])
                 e = cudaMemcpyAsync(u_out[i], A.u + (long long)i * n, nb, cudaMemcpyDeviceToHost, st);
-            if (e == cudaSuccess && pt_out && pt_out[i])
+            if (e == cudaSuccess && pt_out && pt_out[i] && !pseudo)
                 e = cudaMemcpyAsync(pt_out[i], A.pt + (long long)i * n, nb, cudaMemcpyDeviceToHost, st);
             if (e == cudaSuccess && div_out && div_out[i])
                 e = cudaMemcpyAsync(div_out[i], A.div + (long long)i * n, nb, cudaMemcpyDeviceToHost, st);
@@ -547,7 +840,7 @@ asets_status run_hmf(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
         }
         if (e == cudaSuccess)
             e = cudaStreamSynchronize(st);
-        if (e == cudaSuccess) {
+        if (e == cudaSuccess && !pseudo) {
             // CalculateCostsFullFlow: each node adds its children's costs
             std::vector<double> dc(m), rc(m);
             for (int i = m - 1; i >= 0; --i) {
@@ -583,8 +876,8 @@ asets_status run_dag(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
                      const std::vector<int> &kids, const std::vector<int> &nparent,
                      const std::vector<int> &parent0, const std::vector<int> &order,
                      const void *const *Ct, const void *const *alpha_arr, const double *alpha_s,
-                     int its, double steps, double cc, void *const *outs[5],
-                     void *const *p_out[3])
+                     void *const *const ld[3], int its, double steps, double cc,
+                     void *const *outs[5], void *const *p_out[3])
 {
     cudaStream_t st = context_stream(ctx);
     const int sms = context_num_sms(ctx);
@@ -616,6 +909,15 @@ asets_status run_dag(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
     // child weights 1/(parents of the child); per node the sum of their squares
     std::vector<T> w(kids.size());
     std::vector<NodeDev<T>> nodes(m);
+    // paths from the root to each node (the top-down list has parents first),
+    // saturating at 2^20
+    std::vector<long long> paths(m, 0);
+    paths[0] = 1;
+    for (int q : order)
+        for (int k = 0; k < nchild[q]; ++k) {
+            long long &pr = paths[kids[begin[q] + k]];
+            pr = std::min(pr + paths[q], 1LL << 20);
+        }
     for (int i = 0; i < m; ++i) {
         double s2 = 0.0;
         for (int k = 0; k < nchild[i]; ++k) {
@@ -629,6 +931,7 @@ asets_status run_dag(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
         nd.child_begin = begin[i];
         nd.nchild = nchild[i];
         nd.wdiv = (T)(nparent[i] == 0 ? s2 : 1.0 + s2);
+        nd.nnorm = (int)paths[i];
         nd.alpha_s = (T)(alpha_s ? alpha_s[i] : 0.0);
         nd.ct = nullptr;
         nd.alpha = nullptr;
@@ -670,6 +973,8 @@ asets_status run_dag(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
             }
         }
     }
+    bool dirs = false;
+    ok = ok && setup_dirs<T>(get, st, dim, m, ld, nodes, A, e, dirs);
     struct Up {
         const void *src;
         size_t bytes;
@@ -692,15 +997,16 @@ asets_status run_dag(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
     } else if (e == cudaSuccess) {
         const int gp = h_grid(n, sms), gn = h_grid(n * (m - 1), sms);
         k_dag_init<T><<<gp, kThreads, 0, st>>>(A);
+        if (dirs)
+            k_norm_dirs<T><<<h_grid(n * m, sms), kThreads, 0, st>>>(A);
         for (int it = 0; it < its && e == cudaSuccess; ++it) {
             k_dag_g<T><<<gn, kThreads, 0, st>>>(A);
-            k2_gradient<T><<<gn, kThreads, 0, st>>>(A);
-            k3_projection<T><<<gn, kThreads, 0, st>>>(A);
-            k4_rescale<T><<<gn, kThreads, 0, st>>>(A);
-            k5_divergence<T><<<gn, kThreads, 0, st>>>(A);
+            spatial_passes(A, gn, st, dirs);
             k_dag_point<T><<<gp, kThreads, 0, st>>>(A);
             e = cudaGetLastError();
         }
+        if (e == cudaSuccess && dirs)
+            e = download_dirs<T>(st, dim, m, n, ld, nodes);
         T *const srcs[5] = {A.u, A.pt, A.pn, A.div, A.g};
         for (int i = 0; i < m && e == cudaSuccess; ++i) {
             for (int k = 0; k < 5 && e == cudaSuccess; ++k)
@@ -727,15 +1033,33 @@ asets_status run_dag(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
     return status;
 }
 
+// direction fields: a node with lx needs ly (and lz in 3D), as the .m
+// files index them unchecked
+bool check_dirs(int dim, int m, void *const *const ld[3], const char *fn)
+{
+    for (int i = 0; ld[0] && i < m; ++i) {
+        if (!ld[0][i])
+            continue;
+        for (int k = 1; k < dim; ++k)
+            if (!ld[k] || !ld[k][i]) {
+                set_last_error((std::string(fn) + ": a node with lx needs ly (and lz in 3D)").c_str());
+                return false;
+            }
+    }
+    return true;
+}
+
 }  // namespace
 
-extern "C" ASETS_API asets_status asets_dag_full_flow(
+extern "C" ASETS_API asets_status asets_dag_run(
     asets_context *ctx, int precision, int dim, int D1, int D2, int D3, int num_nodes,
     const int *nchild_in, const int *children, const void *const *Ct,
-    const void *const *alpha_arrays, const double *alpha_scalars, int numIts, double steps,
-    double cc, void *const *u, void *const *pt, void *const *pn, void *const *div,
-    void *const *g, void *const *p1, void *const *p2, void *const *p3)
+    const void *const *alpha_arrays, const double *alpha_scalars, void *const *lx,
+    void *const *ly, void *const *lz, int numIts, double steps, double cc, void *const *u,
+    void *const *pt, void *const *pn, void *const *div, void *const *g, void *const *p1,
+    void *const *p2, void *const *p3)
 {
+    void *const *const ld[3] = {lx, ly, lz};
     if (!ctx || !nchild_in || !Ct || (precision != 4 && precision != 8) || (dim != 2 && dim != 3) ||
         D1 < 1 || D2 < 1 || D3 < 1 || (dim == 2 && D3 != 1) || num_nodes < 2 || numIts < 0) {
         set_last_error("asets_dag_full_flow: bad arguments");
@@ -776,6 +1100,8 @@ extern "C" ASETS_API asets_status asets_dag_full_flow(
             set_last_error("asets_dag_full_flow: every leaf needs its Ct");
             return ASETS_ERR_INVALID_ARG;
         }
+    if (!check_dirs(dim, m, ld, "asets_dag_full_flow"))
+        return ASETS_ERR_INVALID_ARG;
     // the top-down list of MaxFullFlow: depth-first from the root, a node
     // entering the stack once all its parents are listed
     std::vector<int> order, stack{0};
@@ -810,22 +1136,36 @@ extern "C" ASETS_API asets_status asets_dag_full_flow(
     const asets_status s =
         precision == 8
             ? run_dag<double>(ctx, dim, D1, D2, D3, m, nchild, begin, kids, nparent, parent0, order,
-                              Ct, alpha_arrays, alpha_scalars, numIts, steps, cc, outs, p_out)
+                              Ct, alpha_arrays, alpha_scalars, ld, numIts, steps, cc, outs, p_out)
             : run_dag<float>(ctx, dim, D1, D2, D3, m, nchild, begin, kids, nparent, parent0, order,
-                             Ct, alpha_arrays, alpha_scalars, numIts, steps, cc, outs, p_out);
+                             Ct, alpha_arrays, alpha_scalars, ld, numIts, steps, cc, outs, p_out);
     cudaSetDevice(prev);
     return s;
 }
 
-extern "C" ASETS_API asets_status asets_hmf_full_flow(
+extern "C" ASETS_API asets_status asets_dag_full_flow(
     asets_context *ctx, int precision, int dim, int D1, int D2, int D3, int num_nodes,
-    const int *parent, const void *const *Ct, const void *const *alpha_arrays,
-    const double *alpha_scalars, int numIts, double steps, double cc, void *const *u,
-    void *const *pt, void *const *div, void *const *g, void *const *p1, void *const *p2,
-    void *const *p3, double *data_cost, double *regu_cost)
+    const int *nchild, const int *children, const void *const *Ct,
+    const void *const *alpha_arrays, const double *alpha_scalars, int numIts, double steps,
+    double cc, void *const *u, void *const *pt, void *const *pn, void *const *div,
+    void *const *g, void *const *p1, void *const *p2, void *const *p3)
 {
+    return asets_dag_run(ctx, precision, dim, D1, D2, D3, num_nodes, nchild, children, Ct,
+                         alpha_arrays, alpha_scalars, nullptr, nullptr, nullptr, numIts, steps, cc,
+                         u, pt, pn, div, g, p1, p2, p3);
+}
+
+extern "C" ASETS_API asets_status asets_hmf_run(
+    asets_context *ctx, int algorithm, int precision, int dim, int D1, int D2, int D3,
+    int num_nodes, const int *parent, const void *const *Ct, const void *const *alpha_arrays,
+    const double *alpha_scalars, void *const *lx, void *const *ly, void *const *lz, int numIts,
+    double steps, double cc, void *const *u, void *const *pt, void *const *div, void *const *g,
+    void *const *p1, void *const *p2, void *const *p3, double *data_cost, double *regu_cost)
+{
+    void *const *const ld[3] = {lx, ly, lz};
     if (!ctx || !parent || !Ct || (precision != 4 && precision != 8) || (dim != 2 && dim != 3) ||
-        D1 < 1 || D2 < 1 || D3 < 1 || (dim == 2 && D3 != 1) || num_nodes < 1 || numIts < 0) {
+        D1 < 1 || D2 < 1 || D3 < 1 || (dim == 2 && D3 != 1) || num_nodes < 1 || numIts < 0 ||
+        (algorithm != ASETS_HMF_FULL_FLOW && algorithm != ASETS_HMF_PSEUDO_FLOW)) {
         set_last_error("asets_hmf_full_flow: bad arguments");
         return ASETS_ERR_INVALID_ARG;
     }
@@ -850,18 +1190,38 @@ extern "C" ASETS_API asets_status asets_hmf_full_flow(
         set_last_error("asets_hmf_full_flow: the root needs children");
         return ASETS_ERR_INVALID_ARG;
     }
+    if (!check_dirs(dim, num_nodes, ld, "asets_hmf_run"))
+        return ASETS_ERR_INVALID_ARG;
+    if (algorithm == ASETS_HMF_PSEUDO_FLOW)
+        for (int i = 0; i < num_nodes; ++i)
+            if (nch[i] == 0 && (!u || !u[i])) {
+                set_last_error("asets_hmf_run: pseudo-flow reads every leaf's labels from u");
+                return ASETS_ERR_INVALID_ARG;
+            }
     int prev = 0;
     cudaGetDevice(&prev);
     cudaSetDevice(context_device(ctx));
     void *const *p_out[3] = {p1, p2, p3};
     const asets_status s =
         precision == 8
-            ? run_hmf<double>(ctx, dim, D1, D2, D3, num_nodes, parent, Ct, alpha_arrays,
-                              alpha_scalars, numIts, steps, cc, u, pt, div, g, p_out, data_cost,
-                              regu_cost)
-            : run_hmf<float>(ctx, dim, D1, D2, D3, num_nodes, parent, Ct, alpha_arrays,
-                             alpha_scalars, numIts, steps, cc, u, pt, div, g, p_out, data_cost,
-                             regu_cost);
+            ? run_hmf<double>(ctx, algorithm, dim, D1, D2, D3, num_nodes, parent, Ct,
+                              alpha_arrays, alpha_scalars, ld, numIts, steps, cc, u, pt, div, g,
+                              p_out, data_cost, regu_cost)
+            : run_hmf<float>(ctx, algorithm, dim, D1, D2, D3, num_nodes, parent, Ct,
+                             alpha_arrays, alpha_scalars, ld, numIts, steps, cc, u, pt, div, g,
+                             p_out, data_cost, regu_cost);
     cudaSetDevice(prev);
     return s;
+}
+
+extern "C" ASETS_API asets_status asets_hmf_full_flow(
+    asets_context *ctx, int precision, int dim, int D1, int D2, int D3, int num_nodes,
+    const int *parent, const void *const *Ct, const void *const *alpha_arrays,
+    const double *alpha_scalars, int numIts, double steps, double cc, void *const *u,
+    void *const *pt, void *const *div, void *const *g, void *const *p1, void *const *p2,
+    void *const *p3, double *data_cost, double *regu_cost)
+{
+    return asets_hmf_run(ctx, ASETS_HMF_FULL_FLOW, precision, dim, D1, D2, D3, num_nodes, parent,
+                         Ct, alpha_arrays, alpha_scalars, nullptr, nullptr, nullptr, numIts, steps,
+                         cc, u, pt, div, g, p1, p2, p3, data_cost, regu_cost);
 }

@@ -49,8 +49,9 @@ enum Epilogue : int {
 
 // Arguments of the column-per-thread iteration kernel (stencil2_kernel.cuh).
 // Halo slots are SL_BC..SL_ALPHA at the step's plane; tile slots carry the
-// old ps/pt/u and the capacities of the plane two steps behind (binary).
-enum TileSlot : int { TS_S0 = 0, TS_S1 = 1, TS_S2 = 2, TS_CS = 3, TS_CT = 4, NUM_TILE_SLOTS = 5 };
+// old pt and u and the capacities of the plane two steps behind (binary; the
+// new ps needs no old ps).
+enum TileSlot : int { TS_S1 = 0, TS_S2 = 1, TS_CS = 2, TS_CT = 3, NUM_TILE_SLOTS = 4 };
 
 // One problem of a launch, in device memory (TMA descriptors need 64-byte
 // alignment, which the CUtensorMap members give the struct).

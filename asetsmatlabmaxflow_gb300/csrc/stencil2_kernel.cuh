@@ -20,7 +20,7 @@
 //   Z: b''_r, b''_c of plane s-1; ps/pt/u (or div) of s-2    tile
 // with two block barriers per step.  Old-state planes come through a ring of
 // 4D TMA tiled loads; a stage holds the halo boxes of its plane and, for the
-// binary model, tile boxes of ps/pt/u/Cs/Ct three planes behind: step t reads
+// binary model, tile boxes of pt/u/Cs/Ct three planes behind: step t reads
 // them from the stage of plane s+1 (the plane s-2 it writes), which stays
 // resident until the next step's X.  Out-of-grid elements load as 0: the zero-flux
 // border of the reference.

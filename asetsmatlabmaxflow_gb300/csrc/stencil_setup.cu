@@ -40,8 +40,8 @@ int build_problem_desc(EncodeTiledFn fn, const StencilVariant &v, const StencilP
                 return r;
         }
         if (binary) {
-            float *tsrc[NUM_TILE_SLOTS] = {p.src[par][0], p.src[par][1], p.src[par][2],
-                                           const_cast<float *>(p.cs), const_cast<float *>(p.ct)};
+            float *tsrc[NUM_TILE_SLOTS] = {p.src[par][1], p.src[par][2], const_cast<float *>(p.cs),
+                                           const_cast<float *>(p.ct)};
             for (int ts = 0; ts < NUM_TILE_SLOTS; ++ts) {
                 int r = encode(fn, &A->tile[par][ts], tsrc[ts], p, 1, v.tr, v.tc);
                 if (r)

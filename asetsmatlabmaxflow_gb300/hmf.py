@@ -6,6 +6,10 @@
     s.MaxFullFlow(numIts, steps, cc)
 
 then read u, pt, div, g, px, py (pz), dataCost, reguCost from the nodes.
+MaxPseudoFlow(numIts, steps, cc) runs the class's pseudo-flow algorithm from
+the leaves' current labels u.  A node's direction fields lx, ly (, lz) --
+the geodesic shape constraint -- are optional; they are normalised when a
+run starts and kept normalised on the node, as the class does.
 Arrays use Matlab index order (numpy arrays shaped D, any memory order)."""
 from __future__ import annotations
 
@@ -35,6 +39,7 @@ class _HMF:
             self.Ct = np.zeros(0, self.C[0].Ct.dtype)
         self.alpha = alpha
         self.u = np.zeros(self.D, self.Ct.dtype)
+        self.lx = self.ly = self.lz = np.zeros(0)
 
     def _nodes(self):
         out = [self]
@@ -45,6 +50,16 @@ class _HMF:
     def MaxFullFlow(self, numIts: int, steps: float, cc: float, *, ctx=None) -> None:
         """numIts full-flow iterations from zero flows (InitializeFullFlow),
         then CalculateCostsFullFlow; results are stored on every node."""
+        self._run(0, numIts, steps, cc, ctx)
+
+    def MaxPseudoFlow(self, numIts: int, steps: float, cc: float, *, ctx=None) -> None:
+        """numIts pseudo-flow iterations from zero flows and the leaves'
+        labels u; leaves get the new labels, inner nodes the sum of their
+        children's (DeInitializePseudoFlow); pt and the costs are left as
+        they were."""
+        self._run(1, numIts, steps, cc, ctx)
+
+    def _run(self, algo, numIts, steps, cc, ctx):
         nodes = self._nodes()
         m = len(nodes)
         index = {id(n): i for i, n in enumerate(nodes)}
@@ -72,21 +87,64 @@ class _HMF:
             return (ctypes.c_void_p * m)(*[a.ctypes.data for a in lst])
 
         p3 = ptrs(pouts[2]) if self.DIM == 3 else None
+        if algo == 1:
+            for i, n in enumerate(nodes):
+                if not n.C:
+                    outs["u"][i][:] = np.asarray(n.u, dt).reshape(D, order="A").ravel(order="F")
+            del outs["pt"]
+        lp = _dir_arrays(nodes, self.DIM, D, dt)
         dc = np.zeros(m)
         rc = np.zeros(m)
-        N.check(N.lib().asets_hmf_full_flow(
-            (ctx or N.Context.default()).handle, dt.itemsize, self.DIM, D[0], D[1],
+        N.check(N.lib().asets_hmf_run(
+            (ctx or N.Context.default()).handle, algo, dt.itemsize, self.DIM, D[0], D[1],
             D[2] if self.DIM == 3 else 1, m, parent.ctypes.data, ct, al_arr, al_s.ctypes.data,
-            int(numIts), float(steps), float(cc), ptrs(outs["u"]), ptrs(outs["pt"]),
+            *lp["ptrs"], int(numIts), float(steps), float(cc), ptrs(outs["u"]),
+            ptrs(outs["pt"]) if "pt" in outs else None,
             ptrs(outs["div"]), ptrs(outs["g"]), ptrs(pouts[0]), ptrs(pouts[1]), p3,
             dc.ctypes.data, rc.ctypes.data))
+        _store_dirs(nodes, lp, D)
         names = ["px", "py", "pz"]
         for i, n in enumerate(nodes):
-            for k, s in shapes.items():
-                setattr(n, k, outs[k][i].reshape(s, order="F"))
+            for k, a in outs.items():
+                setattr(n, k, a[i].reshape(shapes[k], order="F"))
             for k in range(self.DIM):
                 setattr(n, names[k], pouts[k][i].reshape(fshape[k], order="F"))
-            n.dataCost, n.reguCost = float(dc[i]), float(rc[i])
+            if algo == 0:
+                n.dataCost, n.reguCost = float(dc[i]), float(rc[i])
+
+
+def _dir_arrays(nodes, dim, D, dt):
+    """Column-major copies of the nodes' direction fields (the class's
+    numel(h.lx) > 0 test) and the pointer tables for the C call."""
+    names = ["lx", "ly", "lz"][:dim]
+    cols = []
+    for n in nodes:
+        lx = getattr(n, "lx", None)
+        if lx is None or np.size(lx) == 0:
+            cols.append(None)
+            continue
+        row = []
+        for nm in names:
+            a = getattr(n, nm, None)
+            if a is None or np.size(a) == 0:
+                raise ValueError(f"a node with lx needs {', '.join(names[1:])} as well")
+            row.append(np.ascontiguousarray(np.asarray(a, dt).reshape(D, order="A").ravel(order="F")))
+        cols.append(row)
+    m = len(nodes)
+    ptrs = [None, None, None]
+    if any(c is not None for c in cols):
+        for k in range(dim):
+            ptrs[k] = (ctypes.c_void_p * m)(*[c[k].ctypes.data if c is not None else None
+                                               for c in cols])
+    return {"cols": cols, "ptrs": ptrs, "names": names}
+
+
+def _store_dirs(nodes, lp, D):
+    """The normalised fields back on the nodes, as the class keeps them."""
+    for n, row in zip(nodes, lp["cols"]):
+        if row is not None:
+            for nm, a in zip(lp["names"], row):
+                setattr(n, nm, a.reshape(D, order="F"))
 
 
 class asetsHMF2D(_HMF):
@@ -119,6 +177,7 @@ class _DAG:
         self.alpha = alpha
         self.u = np.zeros(self.D, self.Ct.dtype)
         self.pn = None
+        self.lx = self.ly = self.lz = np.zeros(0)
 
     def _nodes(self):
         out, seen, stack = [], set(), [self]
@@ -158,12 +217,14 @@ class _DAG:
         def ptrs(lst):
             return (ctypes.c_void_p * m)(*[a.ctypes.data for a in lst])
 
-        N.check(N.lib().asets_dag_full_flow(
+        lp = _dir_arrays(nodes, self.DIM, D, dt)
+        N.check(N.lib().asets_dag_run(
             (ctx or N.Context.default()).handle, dt.itemsize, self.DIM, D[0], D[1],
             D[2] if self.DIM == 3 else 1, m, nchild.ctypes.data, kids.ctypes.data, ct, al_arr,
-            al_s.ctypes.data, int(numIts), float(steps), float(cc),
+            al_s.ctypes.data, *lp["ptrs"], int(numIts), float(steps), float(cc),
             *[ptrs(outs[k]) for k in names], ptrs(pouts[0]), ptrs(pouts[1]),
             ptrs(pouts[2]) if self.DIM == 3 else None))
+        _store_dirs(nodes, lp, D)
         for i, n in enumerate(nodes):
             for k in names:
                 setattr(n, k, outs[k][i].reshape(D, order="F"))

@@ -109,6 +109,15 @@ _SIGS = {
                                            _VP, _VP, _VP, ctypes.c_int, ctypes.c_double,
                                            ctypes.c_double, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
                                            _VP]),
+    "asets_dag_run": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, _VP, _VP, _VP, _VP, _VP, _VP,
+                                     _VP, _VP, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                     _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "asets_hmf_run": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, _VP, _VP,
+                                     _VP, _VP, _VP, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_double, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
+                                     _VP]),
     "asets_hmf_full_flow": (ctypes.c_int, [_VP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP,
                                            _VP, _VP, ctypes.c_int, ctypes.c_double,

@@ -344,6 +344,28 @@ ASETS_API asets_status asets_hmf_full_flow(asets_context *ctx, int precision, in
                                            void *const *p1, void *const *p2, void *const *p3,
                                            double *data_cost, double *regu_cost);
 
+/* HMF with the class's optional parts (maxflow/asetsHMF2D.m, asetsHMF3D.m):
+ * algorithm ASETS_HMF_FULL_FLOW (MaxFullFlow, as asets_hmf_full_flow) or
+ * ASETS_HMF_PSEUDO_FLOW (MaxPseudoFlow: reads every leaf's initial labels
+ * from u[i] and writes the labels back, an inner node's u being the sum of
+ * its children's; pt is not touched and no costs are formed, as in the
+ * class).  lx, ly, lz: per node a direction field (D1*D2*D3, the class's
+ * geodesic shape constraint) or null; a node with lx needs ly (and lz in
+ * 3D).  The fields are normalised to unit length at initialisation (0 where
+ * the length is at most 0.001) and the normalised fields are written back
+ * into the same arrays, as the class keeps them.  Other arguments as
+ * asets_hmf_full_flow. */
+typedef enum { ASETS_HMF_FULL_FLOW = 0, ASETS_HMF_PSEUDO_FLOW = 1 } asets_hmf_algorithm;
+ASETS_API asets_status asets_hmf_run(asets_context *ctx, int algorithm, int precision, int dim,
+                                     int D1, int D2, int D3, int num_nodes, const int *parent,
+                                     const void *const *Ct, const void *const *alpha_arrays,
+                                     const double *alpha_scalars, void *const *lx,
+                                     void *const *ly, void *const *lz, int numIts, double steps,
+                                     double cc, void *const *u, void *const *pt,
+                                     void *const *div, void *const *g, void *const *p1,
+                                     void *const *p2, void *const *p3, double *data_cost,
+                                     double *regu_cost);
+
 /* DAG max-flow, full-flow iteration (maxflow/asetsDAGMF2D.m and
  * asetsDAGMF3D.m, MaxFullFlow; Matlab classes with no counterpart in the
  * reference's C code): as asets_hmf_full_flow, but a node may have several
@@ -363,6 +385,18 @@ ASETS_API asets_status asets_dag_full_flow(asets_context *ctx, int precision, in
                                            void *const *pt, void *const *pn, void *const *div,
                                            void *const *g, void *const *p1, void *const *p2,
                                            void *const *p3);
+
+/* DAG max-flow with direction fields (asetsDAGMF2D.m / 3D lx, ly, lz):
+ * as asets_dag_full_flow, the fields as in asets_hmf_run. */
+ASETS_API asets_status asets_dag_run(asets_context *ctx, int precision, int dim, int D1, int D2,
+                                     int D3, int num_nodes, const int *nchild,
+                                     const int *children, const void *const *Ct,
+                                     const void *const *alpha_arrays,
+                                     const double *alpha_scalars, void *const *lx,
+                                     void *const *ly, void *const *lz, int numIts, double steps,
+                                     double cc, void *const *u, void *const *pt,
+                                     void *const *pn, void *const *div, void *const *g,
+                                     void *const *p1, void *const *p2, void *const *p3);
 
 /* ------------------------------------------------------------------------
  * Matlab-semantics solvers: the reference's Matlab twins of the six solvers

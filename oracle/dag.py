@@ -3,14 +3,22 @@ max-flow solver's full-flow iteration, maxflow/asetsDAGMF2D.m and
 asetsDAGMF3D.m (MaxFullFlow: the top-down node list, InitializeFullFlow,
 UpdateSpatialFlows, PushDownFlows, PushCapacityUp, UpdateLabels), in the
 precision of Ct and in Matlab's evaluation order, to check the GPU solver
-(asetsmatlabmaxflow_gb300/csrc/hmf.cu).  Isotropic flows only.
+(asetsmatlabmaxflow_gb300/csrc/hmf.cu).  The geodesic branch (direction
+fields lx, ly, lz; asetsDAGMF2D.m:275-318, asetsDAGMF3D.m:281-331) shares
+the restatement of oracle/hmf.py, whose conventions it follows.
 """
 from __future__ import annotations
 
 import numpy as np
 
+from . import hmf as H
+
 
 class Node:
+    lx = ly = lz = None
+    dirs = H.Node.dirs
+    _normalize_dirs = H.Node._normalize_dirs
+
     def __init__(self, children, alpha, Ct=None):
         self.C = list(children)
         self.P = []
@@ -54,6 +62,7 @@ class Node:
         self.div = np.zeros(D, dt)
         self.u = np.zeros(D, dt)
         self.p = [np.zeros(D[:k] + (D[k] - 1,) + D[k + 1:], dt) for k in range(len(D))]
+        self._normalize_dirs()
 
     def max_full_flow(self, its, steps, cc):
         self.init()
@@ -121,34 +130,8 @@ class Node:
             hi = np.take(g, range(1, D[k]), axis=k)
             lo = np.take(g, range(0, D[k] - 1), axis=k)
             self.p[k] = (self.p[k] + hi) - lo
-        m = np.zeros(D, self.dt)
-        for k in range(nd):
-            sq = self.p[k] * self.p[k]
-            lo_sl = [slice(None)] * nd
-            hi_sl = [slice(None)] * nd
-            lo_sl[k] = slice(0, D[k] - 1)
-            hi_sl[k] = slice(1, D[k])
-            m[tuple(lo_sl)] = m[tuple(lo_sl)] + sq
-            m[tuple(hi_sl)] = m[tuple(hi_sl)] + sq
-        m = np.sqrt(m)
-        alm = np.broadcast_to(np.asarray(self.alpha, self.dt), D)
-        with np.errstate(divide="ignore", invalid="ignore"):
-            gm = np.where(m <= alm, t(1), alm / m).astype(self.dt)
-        for k in range(nd):
-            hi = np.take(gm, range(1, D[k]), axis=k)
-            lo = np.take(gm, range(0, D[k] - 1), axis=k)
-            self.p[k] = (t(0.5) * self.p[k]) * (hi + lo)
-        self.g = gm
-        dv = np.zeros(D, self.dt)
-        for k in range(nd):
-            lo_sl = [slice(None)] * nd
-            hi_sl = [slice(None)] * nd
-            lo_sl[k] = slice(0, D[k] - 1)
-            hi_sl[k] = slice(1, D[k])
-            if k == 0:
-                dv[tuple(lo_sl)] = self.p[0]
-                dv[tuple(hi_sl)] = dv[tuple(hi_sl)] - self.p[0]
-            else:
-                dv[tuple(lo_sl)] = dv[tuple(lo_sl)] + self.p[k]
-                dv[tuple(hi_sl)] = dv[tuple(hi_sl)] - self.p[k]
-        self.div = dv
+        ls = self.dirs()
+        e = None
+        if ls is not None:
+            self.p, e, _ = H.exemption(self.p, ls, D, self.dt)
+        self.p, self.g, self.div = H.project(self.p, self.alpha, D, self.dt, e)

@@ -1,6 +1,7 @@
 """DAG max-flow (full flow) on the GPU against the numpy restatement of
 asetsDAGMF2D.m / asetsDAGMF3D.m (oracle/dag.py): every state array bit for
-bit, in float32 and float64, on graphs with shared children."""
+bit, in float32 and float64, on graphs with shared children, with and
+without direction fields."""
 import numpy as np
 import pytest
 
@@ -81,3 +82,48 @@ def test_single_child_inner_node_is_rejected():
     root = asetsDAGMF2D([mid, asetsDAGMF2D([], 0.1, np.ones((4, 4)))], 0)
     with pytest.raises(N.AsetsError):
         root.MaxFullFlow(2, 0.1, 0.25)
+
+
+@pytest.mark.parametrize("shape,dtype,kind", [
+    ((23, 19), np.float32, "shared"),
+    ((23, 19), np.float64, "diamond"),
+    ((9, 8, 7), np.float64, "shared"),
+    ((10, 7, 6), np.float32, "diamond"),
+])
+def test_geodesic_full_flow_matches_restatement(shape, dtype, kind):
+    """Direction fields on a shared leaf and an inner node (the geodesic
+    branch of asetsDAGMF2D.m / 3D UpdateSpatialFlows): bit for bit."""
+    from asetsmatlabmaxflow_gb300.hmf import asetsDAGMF2D, asetsDAGMF3D
+
+    cls = asetsDAGMF2D if len(shape) == 2 else asetsDAGMF3D
+    ref, Lr = _graph(Dg.Node, shape, dtype, 6, kind)
+    gpu, Lg = _graph(cls, shape, dtype, 6, kind)
+    g = np.random.default_rng(8)
+    names = ("lx", "ly", "lz")[:len(shape)]
+    for r, q in ((Lr[1], Lg[1]), (ref.C[0], gpu.C[0])):
+        for nm in names:
+            a = (g.random(shape) - 0.5).astype(dtype)
+            a[g.random(shape) < 0.1] = 0
+            setattr(r, nm, a.copy())
+            setattr(q, nm, a.copy())
+    ref.max_full_flow(15, 0.1, 0.25)
+    gpu.MaxFullFlow(15, 0.1, 0.25)
+
+    def order(root):
+        out, seen, st = [], set(), [root]
+        while st:
+            n = st.pop(0)
+            if id(n) not in seen:
+                seen.add(id(n))
+                out.append(n)
+                st.extend(n.C)
+        return out
+
+    for r, q in zip(order(ref), order(gpu)):
+        for name in ("u", "pt", "div", "g"):
+            assert np.array_equal(_bits(getattr(q, name)), _bits(getattr(r, name))), name
+        for k, name in enumerate(("px", "py", "pz")[:len(shape)]):
+            assert np.array_equal(_bits(getattr(q, name)), _bits(r.p[k])), name
+        if r.lx is not None:
+            for nm in names:
+                assert np.array_equal(_bits(getattr(q, nm)), _bits(getattr(r, nm))), nm

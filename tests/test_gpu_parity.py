@@ -207,3 +207,23 @@ def test_warm_start_matches_oracle_warm_start(model, dims, L):
     if ps is not None:
         np.testing.assert_array_equal(bits(ps), bits(first["ps"]))
     s.close()
+
+
+@pytest.mark.parametrize("tile_config", [1, 2, 3])
+def test_every_binary3d_fast_variant_meets_parity_bar(tile_config):
+    """Each compiled variant of the fast binary 3D kernel (28 x 28, 28 x 12
+    and 28 x 8 tiles), selected explicitly, against the oracle."""
+    from asetsmatlabmaxflow_gb300 import native as N
+
+    model, dims, L, maxit, cc, steps = ORACLE_CASES[1]
+    inp = _rand(model, dims, L, 9)
+    ref = O.solve(model, dims, inp["Ct"], inp["alpha"], cs=inp["Cs"], nlab=L, max_it=maxit,
+                  err_bound=0.0, cc=cc, steps=steps)
+    refd = O.solve(model, dims, inp["Ct"], inp["alpha"], cs=inp["Cs"], nlab=L, max_it=maxit,
+                   err_bound=0.0, cc=cc, steps=steps, erru_double=True)
+    s = N.Solver(N.Context.default(), model, dims, L)
+    s.set_inputs(inp["Ct"], inp["alpha"], inp["Cs"])
+    s.run(maxit, 0.0, cc, steps, exact=False, tile_config=tile_config)
+    assert_north_star(model, dims, L, s.get_u().reshape(dims, order="F"),
+                      ref["u"].reshape(dims, order="F"), s.get_cvg(), refd["cvg"])
+    s.close()
