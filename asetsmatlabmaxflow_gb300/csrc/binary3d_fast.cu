@@ -1,12 +1,18 @@
 // Compiled instances of the fused iteration kernel for the binary model (ps/pt/u
-// epilogue), 3D tiles 28 x 28, 28 x 12, 28 x 8; fast projection, built with FMA
+// epilogue), 3D tiles 60 x 16 and 60 x 12 (two rows per thread), 28 x 28, 28 x 12, 28 x 8;
+// fast projection, built with FMA
 // contraction and flush to zero (held to the parity tolerance, not bit-exactness).
 #include "variants.cuh"
 
 namespace asets {
 
 static const StencilVariant kVariants[] = {
-    make_variant<3, 32, 4, EPI_BINARY, false, 1>(),  // default: the fewest halo threads
+    // default: two rows per thread (60 x 16 tiles, 640 threads), the plane
+    // loop unrolled by the ring depth (stage slots become constants)
+    make_variant<3, 20, 4, EPI_BINARY, false, 1, 4, 2>(),
+    make_variant<3, 16, 4, EPI_BINARY, false, 1, 4, 2>(),  // 60 x 12
+    // one row per thread: 28 x 28 tiles, the fewest halo threads
+    make_variant<3, 32, 4, EPI_BINARY, false, 1, 4>(),
     make_variant<3, 16, 4, EPI_BINARY, false>(),
     make_variant<3, 12, 4, EPI_BINARY, false>(),
 };

@@ -6,7 +6,9 @@
 namespace asets {
 
 static const StencilVariant kVariants[] = {
-    make_variant<3, 32, 4, EPI_DIV, false, 1>(),  // default: the fewest halo threads
+    // default: the fewest halo threads; the plane loop unrolled by the ring
+    // depth (stage slots become constants)
+    make_variant<3, 32, 4, EPI_DIV, false, 1, 4>(),
     make_variant<3, 16, 4, EPI_DIV, false>(),
     make_variant<3, 12, 4, EPI_DIV, false>(),
 };

@@ -7,13 +7,16 @@
 // and, for the binary model, updateDIVPSPTU and the erriter sum (:398-437).
 //
 // Geometry.  Rows r (Matlab y, contiguous), columns c (Matlab x in 3D) and a
-// stream axis s (z in 3D, x in 2D).  Each warp owns 32 consecutive rows: 28
-// tile rows plus two halo rows on each side.  In 3D warp w is column
-// c0 - 2 + w of a 28 x (NW-4) tile; in 2D the NW warps are consecutive
-// 28-row sub-tiles.  Every thread owns one (r, c) column for the whole sweep
-// along s, so its indices, border flags and carried values stay in registers;
-// row neighbours come through warp shuffles, column neighbours through three
-// small shared planes.  One iteration has a stencil radius of two cells, so
+// stream axis s (z in 3D, x in 2D).  Each warp owns 32*CELLS consecutive
+// rows: 32*CELLS - 4 tile rows plus two halo rows on each side.  In 3D warp
+// w is column c0 - 2 + w of a (32*CELLS - 4) x (NW-4) tile; in 2D the NW
+// warps are consecutive 28-row sub-tiles.  Every thread owns CELLS adjacent
+// rows of one column (CELLS = 1, or 2 in 3D) for the whole sweep along s, so
+// its indices, border flags and carried values stay in registers; row
+// neighbours come from the thread itself or, for its first and last cell,
+// through one warp shuffle, column neighbours through three small shared
+// planes.  With two cells the shared-memory and global accesses are 8-byte
+// pairs, and the per-step index, flag and barrier work is shared by both.  One iteration has a stencil radius of two cells, so
 // step s computes
 //   X: gk(s) = div b(s) - ((s0 - s1) + s2/cc)               all threads
 //   Y: gradient step b'(s); projection g2(s-1); b''_s(s-1)   tile + 1
@@ -43,11 +46,12 @@
 
 namespace asets {
 
-template <int DIM, int NW>
+template <int DIM, int NW, int CELLS = 1>
 struct ColGeom {
     static_assert(DIM == 2 || DIM == 3, "2D or 3D");
+    static_assert(CELLS == 1 || (CELLS == 2 && DIM == 3), "two cells per thread in 3D only");
     static constexpr int NT = 32 * NW;
-    static constexpr int TRW = 28;                            // tile rows per warp
+    static constexpr int TRW = 32 * CELLS - 4;                // tile rows per warp
     static constexpr int TR = (DIM == 3) ? TRW : TRW * NW;    // tile rows
     static constexpr int TC = (DIM == 3) ? NW - 4 : 1;        // tile columns
     static_assert(DIM == 2 || NW >= 5, "3D needs at least one tile column");
@@ -82,14 +86,68 @@ struct ColGeom {
             b += NUM_TILE_SLOTS * tile_floats() * 4;
         return b;
     }
-    static constexpr int plane_bytes() { return (DIM == 3) ? align128(NT * 4) : 0; }
+    static constexpr int plane_bytes() { return (DIM == 3) ? align128(NT * CELLS * 4) : 0; }
     template <int NSTAGE, int EPI>
     static constexpr int smem_bytes()
     {
-        // stages | GK | BC x2 | G2 | mbarriers | alignment slack
-        return NSTAGE * stage_bytes<EPI>() + 4 * plane_bytes() + NSTAGE * 8 + 128;
+        // stages | GK | BC | G2 | mbarriers | alignment slack
+        return NSTAGE * stage_bytes<EPI>() + 3 * plane_bytes() + NSTAGE * 8 + 128;
     }
 };
+
+// CELLS consecutive floats (CELLS = 1 or 2, 8-byte aligned for 2) into v
+template <int CELLS>
+__device__ __forceinline__ void ld_cells(const float *p, float (&v)[CELLS])
+{
+    if constexpr (CELLS == 2) {
+        const float2 t = *reinterpret_cast<const float2 *>(p);
+        v[0] = t.x;
+        v[1] = t.y;
+    } else {
+        v[0] = p[0];
+    }
+}
+template <int CELLS>
+__device__ __forceinline__ void st_cells(float *p, const float (&v)[CELLS])
+{
+    if constexpr (CELLS == 2)
+        *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]);
+    else
+        p[0] = v[0];
+}
+// global store of the cells whose flag is set; the flags of a pair are both
+// set except past the last row (cell 1 alone out of range)
+template <int CELLS>
+__device__ __forceinline__ void st_cells_if(float *__restrict__ p, const float (&v)[CELLS],
+                                            const bool (&ok)[CELLS])
+{
+    if constexpr (CELLS == 2) {
+        if (ok[1])
+            *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]);
+        else if (ok[0])
+            p[0] = v[0];
+    } else if (ok[0]) {
+        p[0] = v[0];
+    }
+}
+// value of the row above (r-1) / below (r+1) each cell: inside the thread,
+// or through one warp shuffle for the first / last cell
+template <int CELLS>
+__device__ __forceinline__ void rows_up(const float (&v)[CELLS], float (&up)[CELLS])
+{
+    up[0] = __shfl_up_sync(0xffffffffu, v[CELLS - 1], 1);
+#pragma unroll
+    for (int j = 1; j < CELLS; ++j)
+        up[j] = v[j - 1];
+}
+template <int CELLS>
+__device__ __forceinline__ void rows_down(const float (&v)[CELLS], float (&dn)[CELLS])
+{
+#pragma unroll
+    for (int j = 0; j + 1 < CELLS; ++j)
+        dn[j] = v[j + 1];
+    dn[CELLS - 1] = __shfl_down_sync(0xffffffffu, v[0], 1);
+}
 
 template <int NT>
 __device__ __forceinline__ void finish_item(float erru, const ProblemDesc &P, int li, int it,
@@ -142,12 +200,13 @@ __device__ __forceinline__ void finish_item(float erru, const ProblemDesc &P, in
     __syncthreads();
 }
 
-template <int DIM, int NW, int NSTAGE, int EPI, bool EXACT, int MINB>
+template <int DIM, int NW, int NSTAGE, int EPI, bool EXACT, int MINB, int UNROLL = 1, int CELLS = 1>
 __global__ void __launch_bounds__(32 * NW, MINB)
     stencil_col_kernel(const __grid_constant__ BatchArgs B)
 {
-    using G = ColGeom<DIM, NW>;
+    using G = ColGeom<DIM, NW, CELLS>;
     constexpr int NT = G::NT;
+    constexpr int C = CELLS;
     static_assert(NSTAGE >= 4, "stage of plane s stays resident until step s ends");
 
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -189,10 +248,13 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     const float *stages = reinterpret_cast<const float *>(smem);
     float *planes = reinterpret_cast<float *>(smem + NSTAGE * SB);
     constexpr int PF = G::plane_bytes() / 4;
+    // shared planes: gk, the column faces b'_c (one buffer: the neighbour's
+    // previous face is read in X, before the barrier that precedes this
+    // step's write in Y) and the projection factors g2
     float *GK = planes;
-    float *BCb0 = planes + PF, *BCb1 = planes + 2 * PF;
-    float *G2p = planes + 3 * PF;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NSTAGE * SB + 4 * G::plane_bytes());
+    float *BCp = planes + PF;
+    float *G2p = planes + 2 * PF;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + NSTAGE * SB + 3 * G::plane_bytes());
 
     if (tid == 0) {
         s_abort = 0;
@@ -202,15 +264,17 @@ __global__ void __launch_bounds__(32 * NW, MINB)
     }
     __syncthreads();
 
-    // per-thread constants
-    const int row_in_tile = (DIM == 3) ? lane : G::TRW * w + lane;   // G-row index + 0
-    const int si = row_in_tile + 2 + ((DIM == 3) ? w * G::LR : 0);   // halo box index
-    const int gi = lane + 32 * w;                                     // shared plane index (3D)
-    const int gi_left = (w >= 1) ? gi - 32 : gi;                      // column c-1 (clamped)
-    const int gi_right = (w + 1 < NW) ? gi + 32 : gi;                 // column c+1 (clamped)
-    const bool tile_row = (lane >= 2 && lane < 30);
+    // per-thread constants; the thread's cells are rows rho .. rho+C-1 of
+    // its warp's 32*C rows (two halo rows on each side)
+    const int rho = (DIM == 3) ? C * lane : G::TRW * w + lane;       // first cell's row index
+    const int si = rho + 2 + ((DIM == 3) ? w * G::LR : 0);            // halo box index
+    const int gi = (lane + 32 * w) * C;                               // shared plane index (3D)
+    const int gi_left = (w >= 1) ? gi - 32 * C : gi;                  // column c-1 (clamped)
+    const int gi_right = (w + 1 < NW) ? gi + 32 * C : gi;             // column c+1 (clamped)
+    const int lane_row = (DIM == 3) ? C * lane : lane;                // row within the warp
+    const bool tile_row = (lane_row >= 2 && lane_row < 32 * C - 2);
     const bool tile_col = (DIM == 3) ? (w >= 2 && w < G::TC + 2) : true;
-    const int ti = (DIM == 3) ? (lane - 2) + (w - 2) * G::TRW : (row_in_tile - 2);
+    const int ti = (DIM == 3) ? (lane_row - 2) + (w - 2) * G::TRW : (rho - 2);
     // The thread that issues the TMA loads and waits on their barriers; the
     // other threads block in the following CTA barrier instead of polling.
     const bool producer = (tid == NT - 32);
@@ -291,19 +355,28 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             for (int j = 0; j < NSTAGE && j < n_loads; ++j)
                 issue_load(j);
 
-        // this thread's column
-        const int r = r0 - 2 + row_in_tile;
+        // this thread's cells (rows r .. r+C-1 of column c)
+        const int r = r0 - 2 + rho;
         const int c = (DIM == 3) ? c0 - 2 + w : 0;
-        const bool in_r = (r >= 0 && r < nr), in_c = (c >= 0 && c < nc);
-        const bool inplane = in_r && in_c;
-        const bool is_tile = tile_row && tile_col && inplane;
-        const bool fr_ok = (r >= 1 && r < nr && in_c);          // row face r
-        const bool fr1_ok = (r + 1 >= 1 && r + 1 < nr && in_c); // row face r+1
-        const bool fc_ok = (in_r && c >= 1 && c < nc);
-        const bool fc1_ok = (in_r && c + 1 >= 1 && c + 1 < nc);
-        const float fr_f = fr_ok ? 1.f : 0.f, fr1_f = fr1_ok ? 1.f : 0.f;
-        const float fc_f = fc_ok ? 1.f : 0.f, fc1_f = fc1_ok ? 1.f : 0.f;
-        const float in_f = inplane ? 1.f : 0.f;
+        const bool in_c = (c >= 0 && c < nc);
+        bool inplane[C], is_tile[C], fr_ok[C], fr1_ok[C], fc_ok[C], fc1_ok[C];
+        float fr_f[C], fr1_f[C], fc_f[C], fc1_f[C], in_f[C];
+#pragma unroll
+        for (int j = 0; j < C; ++j) {
+            const int rj = r + j;
+            const bool in_r = (rj >= 0 && rj < nr);
+            inplane[j] = in_r && in_c;
+            is_tile[j] = tile_row && tile_col && inplane[j];
+            fr_ok[j] = (rj >= 1 && rj < nr && in_c);            // row face rj
+            fr1_ok[j] = (rj + 1 >= 1 && rj + 1 < nr && in_c);   // row face rj+1
+            fc_ok[j] = (in_r && c >= 1 && c < nc);
+            fc1_ok[j] = (in_r && c + 1 >= 1 && c + 1 < nc);
+            fr_f[j] = fr_ok[j] ? 1.f : 0.f;
+            fr1_f[j] = fr1_ok[j] ? 1.f : 0.f;
+            fc_f[j] = fc_ok[j] ? 1.f : 0.f;
+            fc1_f[j] = fc1_ok[j] ? 1.f : 0.f;
+            in_f[j] = inplane[j] ? 1.f : 0.f;
+        }
         // element offsets fit 32 bits: solves are limited to 2^31 - 1 voxel-labels
         const unsigned int col_off = (unsigned int)(lab_off + (long long)c * P.pitch + r);
         const unsigned int plane_stride = (unsigned int)P.plane_stride;
@@ -314,8 +387,20 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         float *__restrict__ d_s1 = P.dst_s[par][1];
         float *__restrict__ d_s2 = P.dst_s[par][2];
 
-        float gkprev = 0.f, bsprev = 0.f, g2prev = 1.f, alpha_prev = 1.f;
-        float br_prev = 0.f, bc_prev = 0.f, bss_cur = 0.f, bss_old = 0.f, dvp = 0.f;
+        float gkprev[C], bsprev[C], g2prev[C], alpha_prev[C];
+        float br_prev[C], bc_prev[C], bss_cur[C], bss_old[C], dvp[C];
+#pragma unroll
+        for (int j = 0; j < C; ++j) {
+            gkprev[j] = 0.f;
+            bsprev[j] = 0.f;
+            g2prev[j] = 1.f;
+            alpha_prev[j] = 1.f;
+            br_prev[j] = 0.f;
+            bc_prev[j] = 0.f;
+            bss_cur[j] = 0.f;
+            bss_old[j] = 0.f;
+            dvp[j] = 0.f;
+        }
 
         // A wait gave up: drain this item's loads [first, issued) (bounded),
         // record the error and leave the item.
@@ -351,6 +436,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             }
         }
 
+#pragma unroll UNROLL
         for (int t = 0; t < n_steps && !aborted; ++t) {
             const int s = p_first + t;
             const int st_cur = (q0 + t) % NSTAGE, st_nxt = (q0 + t + 1) % NSTAGE;
@@ -378,25 +464,55 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             // ---- X: gk(s) from the old state
             const float *Sc = stages + st_cur * (SB / 4) + si;   // this column in stage s
             const float *Sn = stages + st_nxt * (SB / 4) + si;   // and in stage s+1
-            float gk, by_own, bx_own = 0.f, bs_own, alpha_cur;
+            float gk[C], by_own[C], bx_own[C], bs_own[C], alpha_cur[C], bc_rt[C];
             {
-                by_own = Sc[OFF_BR];
-                float d = Sc[OFF_BR + 1] - by_own;
-                if constexpr (DIM == 3) {
-                    bx_own = Sc[OFF_BC];
-                    d = d + Sc[OFF_BC + G::LR];
-                    d = d - bx_own;
+                float d[C], v[C];
+                ld_cells<C>(Sc + OFF_BR, by_own);
+                {
+                    float nx[C];   // row faces r+1 .. r+C
+                    if constexpr (C == 2) {
+                        nx[0] = by_own[1];
+                        nx[1] = Sc[OFF_BR + 2];
+                    } else {
+                        nx[0] = Sc[OFF_BR + 1];
+                    }
+#pragma unroll
+                    for (int j = 0; j < C; ++j)
+                        d[j] = nx[j] - by_own[j];
                 }
-                bs_own = Sc[OFF_BS];
-                d = d + Sn[OFF_BS];
-                d = d - bs_own;
-                const float s0 = Sc[OFF_S0];
-                const float s1 = Sc[OFF_S1];
-                const float s2 = Sc[OFF_S2];
-                gk = d - ((s0 - s1) + div_cc<EXACT>(s2, cc, inv_cc));
-                alpha_cur = Sc[OFF_AL];
-                if constexpr (DIM == 3)
-                    GK[gi] = gk;
+                if constexpr (DIM == 3) {
+                    ld_cells<C>(Sc + OFF_BC, bx_own);
+                    ld_cells<C>(Sc + OFF_BC + G::LR, v);
+#pragma unroll
+                    for (int j = 0; j < C; ++j) {
+                        d[j] = d[j] + v[j];
+                        d[j] = d[j] - bx_own[j];
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < C; ++j)
+                        bx_own[j] = 0.f;
+                }
+                ld_cells<C>(Sc + OFF_BS, bs_own);
+                ld_cells<C>(Sn + OFF_BS, v);
+#pragma unroll
+                for (int j = 0; j < C; ++j) {
+                    d[j] = d[j] + v[j];
+                    d[j] = d[j] - bs_own[j];
+                }
+                float s0[C], s1[C], s2[C];
+                ld_cells<C>(Sc + OFF_S0, s0);
+                ld_cells<C>(Sc + OFF_S1, s1);
+                ld_cells<C>(Sc + OFF_S2, s2);
+#pragma unroll
+                for (int j = 0; j < C; ++j)
+                    gk[j] = d[j] - ((s0[j] - s1[j]) + div_cc<EXACT>(s2[j], cc, inv_cc));
+                ld_cells<C>(Sc + OFF_AL, alpha_cur);
+                if constexpr (DIM == 3) {
+                    st_cells<C>(GK + gi, gk);
+                    // b'_c(s-1) at c+1, written by the previous Y (before Y rewrites it)
+                    ld_cells<C>(BCp + gi_right, bc_rt);
+                }
             }
             __syncthreads();
 
@@ -405,36 +521,61 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                 issue_load(t + kLead);
 
             // ---- Y: gradient step b'(s), projection g2(s-1), stream faces b''(s-1)
-            const float gk_up = __shfl_up_sync(0xffffffffu, gk, 1);
-            const float brn = keep_if<EXACT>(steps * (gk - gk_up) + by_own, fr_ok && s_in, fr_f * s_f);
-            float bcn = 0.f, bc_rt = 0.f;
-            float *BCc = (t & 1) ? BCb1 : BCb0;
-            const float *BCp = (t & 1) ? BCb0 : BCb1;
+            float gk_up[C];
+            rows_up<C>(gk, gk_up);
+            float brn[C], bcn[C], bsn[C], br_dn[C], g2[C];
+#pragma unroll
+            for (int j = 0; j < C; ++j)
+                brn[j] = keep_if<EXACT>(steps * (gk[j] - gk_up[j]) + by_own[j], fr_ok[j] && s_in,
+                                        fr_f[j] * s_f);
             if constexpr (DIM == 3) {
-                const float gk_left = GK[gi_left];
-                bcn = keep_if<EXACT>(steps * (gk - gk_left) + bx_own, fc_ok && s_in, fc_f * s_f);
-                BCc[gi] = bcn;
-                bc_rt = BCp[gi_right];  // b'_c(s-1) at c+1
+                float gk_left[C];
+                ld_cells<C>(GK + gi_left, gk_left);
+#pragma unroll
+                for (int j = 0; j < C; ++j)
+                    bcn[j] = keep_if<EXACT>(steps * (gk[j] - gk_left[j]) + bx_own[j], fc_ok[j] && s_in,
+                                            fc_f[j] * s_f);
+                st_cells<C>(BCp + gi, bcn);
+            } else {
+#pragma unroll
+                for (int j = 0; j < C; ++j)
+                    bcn[j] = bc_rt[j] = 0.f;
             }
-            const float bsn = keep_if<EXACT>(steps * (gk - gkprev) + bs_own, inplane && sb_in, in_f * sb_f);
-            gkprev = gk;
-            const float br_dn = __shfl_down_sync(0xffffffffu, br_prev, 1);  // b'_r(s-1) at r+1
-            float g2;
+#pragma unroll
+            for (int j = 0; j < C; ++j) {
+                bsn[j] = keep_if<EXACT>(steps * (gk[j] - gkprev[j]) + bs_own[j], inplane[j] && sb_in,
+                                        in_f[j] * sb_f);
+                gkprev[j] = gk[j];
+            }
+            rows_down<C>(br_prev, br_dn);   // b'_r(s-1) at r+1
+#pragma unroll
+            for (int j = 0; j < C; ++j) {
+                if constexpr (DIM == 3)
+                    g2[j] = Proj<EXACT>::gk(bc_rt[j], bc_prev[j], br_dn[j], br_prev[j], bsn[j], bsprev[j],
+                                            alpha_prev[j]);
+                else
+                    g2[j] = Proj<EXACT>::gk(bsn[j], bsprev[j], br_dn[j], br_prev[j], alpha_prev[j]);
+            }
             if constexpr (DIM == 3)
-                g2 = Proj<EXACT>::gk(bc_rt, bc_prev, br_dn, br_prev, bsn, bsprev, alpha_prev);
-            else
-                g2 = Proj<EXACT>::gk(bsn, bsprev, br_dn, br_prev, alpha_prev);
-            if constexpr (DIM == 3)
-                G2p[gi] = g2;
+                st_cells<C>(G2p + gi, g2);
             const int sp = s - 1;
-            const float bssn = keep_if<EXACT>(((g2 + g2prev) * 0.5f) * bsprev, inplane && spb_in, in_f * spb_f);
-            if (is_tile && sp >= s_begin && sp < s_end)
-                d_bs[col_off + (unsigned int)sp * plane_stride] = bssn;
-            bss_old = bss_cur;
-            bss_cur = bssn;
-            g2prev = g2;
-            bsprev = bsn;
-            alpha_prev = alpha_cur;
+            {
+                float bssn[C];
+#pragma unroll
+                for (int j = 0; j < C; ++j)
+                    bssn[j] = keep_if<EXACT>(((g2[j] + g2prev[j]) * 0.5f) * bsprev[j],
+                                             inplane[j] && spb_in, in_f[j] * spb_f);
+                if (sp >= s_begin && sp < s_end)
+                    st_cells_if<C>(d_bs + col_off + (unsigned int)sp * plane_stride, bssn, is_tile);
+#pragma unroll
+                for (int j = 0; j < C; ++j) {
+                    bss_old[j] = bss_cur[j];
+                    bss_cur[j] = bssn[j];
+                    g2prev[j] = g2[j];
+                    bsprev[j] = bsn[j];
+                    alpha_prev[j] = alpha_cur[j];
+                }
+            }
             if constexpr (kEarly) {
                 // the stage of plane s+2 (read by the next step's X) arrives
                 // before this barrier, which also publishes Y's shared planes
@@ -455,56 +596,84 @@ __global__ void __launch_bounds__(32 * NW, MINB)
 
             // ---- Z: row/column faces of plane s-1 and the output of plane s-2
             {
-                const float g2_up = __shfl_up_sync(0xffffffffu, g2, 1);
-                const float g2_dn = __shfl_down_sync(0xffffffffu, g2, 1);
-                const float brr = keep_if<EXACT>(((g2 + g2_up) * 0.5f) * br_prev, fr_ok && sp_in, fr_f * sp_f);
-                const float brr1 = keep_if<EXACT>(((g2_dn + g2) * 0.5f) * br_dn, fr1_ok && sp_in, fr1_f * sp_f);
-                float dn = brr1 - brr;
-                float bcc = 0.f;
-                if constexpr (DIM == 3) {
-                    const float g2_l = G2p[gi_left];
-                    const float g2_r = G2p[gi_right];
-                    bcc = keep_if<EXACT>(((g2 + g2_l) * 0.5f) * bc_prev, fc_ok && sp_in, fc_f * sp_f);
-                    const float bcc1 = keep_if<EXACT>(((g2_r + g2) * 0.5f) * bc_rt, fc1_ok && sp_in, fc1_f * sp_f);
-                    dn = dn + bcc1;
-                    dn = dn - bcc;
+                float g2_up[C], g2_dn[C], brr[C], dn[C], bcc[C];
+                rows_up<C>(g2, g2_up);
+                rows_down<C>(g2, g2_dn);
+#pragma unroll
+                for (int j = 0; j < C; ++j) {
+                    brr[j] = keep_if<EXACT>(((g2[j] + g2_up[j]) * 0.5f) * br_prev[j], fr_ok[j] && sp_in,
+                                            fr_f[j] * sp_f);
+                    const float brr1 = keep_if<EXACT>(((g2_dn[j] + g2[j]) * 0.5f) * br_dn[j],
+                                                      fr1_ok[j] && sp_in, fr1_f[j] * sp_f);
+                    dn[j] = brr1 - brr[j];
+                    bcc[j] = 0.f;
                 }
-                if (is_tile) {
+                if constexpr (DIM == 3) {
+                    float g2_l[C], g2_r[C];
+                    ld_cells<C>(G2p + gi_left, g2_l);
+                    ld_cells<C>(G2p + gi_right, g2_r);
+#pragma unroll
+                    for (int j = 0; j < C; ++j) {
+                        bcc[j] = keep_if<EXACT>(((g2[j] + g2_l[j]) * 0.5f) * bc_prev[j], fc_ok[j] && sp_in,
+                                                fc_f[j] * sp_f);
+                        const float bcc1 = keep_if<EXACT>(((g2_r[j] + g2[j]) * 0.5f) * bc_rt[j],
+                                                          fc1_ok[j] && sp_in, fc1_f[j] * sp_f);
+                        dn[j] = dn[j] + bcc1;
+                        dn[j] = dn[j] - bcc[j];
+                    }
+                }
+                if (is_tile[0]) {
                     if (sp >= s_begin && sp < s_end) {
                         const unsigned int o = col_off + (unsigned int)sp * plane_stride;
-                        d_br[o] = brr;
+                        st_cells_if<C>(d_br + o, brr, is_tile);
                         if constexpr (DIM == 3)
-                            d_bc[o] = bcc;
+                            st_cells_if<C>(d_bc + o, bcc, is_tile);
                     }
                     const int so = s - 2;
                     if (so >= s_begin && so < s_end) {
-                        float dv = dvp + bss_cur;
-                        dv = dv - bss_old;
+                        float dv[C];
+#pragma unroll
+                        for (int j = 0; j < C; ++j) {
+                            dv[j] = dvp[j] + bss_cur[j];
+                            dv[j] = dv[j] - bss_old[j];
+                        }
                         const unsigned int o = col_off + (unsigned int)so * plane_stride;
                         if constexpr (EPI == EPI_BINARY) {
                             const float *T = stages + st_nxt * (SB / 4) + OFF_T0 + ti;
-                            const float pt = T[TS_S1 * TSZ];
-                            const float u = T[TS_S2 * TSZ];
-                            const float csv = T[TS_CS * TSZ];
-                            const float ctv = T[TS_CT * TSZ];
-                            const float ucc = div_cc<EXACT>(u, cc, inv_cc);
-                            float ps_n = ((pt - ucc) + dv) + inv_cc;
-                            ps_n = min_sel<EXACT>(ps_n, csv);
-                            float pt_n = (ps_n + ucc) - dv;
-                            pt_n = min_sel<EXACT>(pt_n, ctv);
-                            const float e = cc * ((pt_n + dv) - ps_n);
-                            erru += abs_ref(e);
-                            d_s0[o] = ps_n;
-                            d_s1[o] = pt_n;
-                            d_s2[o] = u - e;
+                            float pt[C], u[C], csv[C], ctv[C], ps_o[C], pt_o[C], u_o[C];
+                            ld_cells<C>(T + TS_S1 * TSZ, pt);
+                            ld_cells<C>(T + TS_S2 * TSZ, u);
+                            ld_cells<C>(T + TS_CS * TSZ, csv);
+                            ld_cells<C>(T + TS_CT * TSZ, ctv);
+#pragma unroll
+                            for (int j = 0; j < C; ++j) {
+                                const float ucc = div_cc<EXACT>(u[j], cc, inv_cc);
+                                float ps_n = ((pt[j] - ucc) + dv[j]) + inv_cc;
+                                ps_n = min_sel<EXACT>(ps_n, csv[j]);
+                                float pt_n = (ps_n + ucc) - dv[j];
+                                pt_n = min_sel<EXACT>(pt_n, ctv[j]);
+                                const float e = cc * ((pt_n + dv[j]) - ps_n);
+                                // cells past the last row hold zero state
+                                // and add nothing
+                                erru += abs_ref(e);
+                                ps_o[j] = ps_n;
+                                pt_o[j] = pt_n;
+                                u_o[j] = u[j] - e;
+                            }
+                            st_cells_if<C>(d_s0 + o, ps_o, is_tile);
+                            st_cells_if<C>(d_s1 + o, pt_o, is_tile);
+                            st_cells_if<C>(d_s2 + o, u_o, is_tile);
                         } else {
-                            d_s0[o] = dv;
+                            st_cells_if<C>(d_s0 + o, dv, is_tile);
                         }
                     }
                 }
-                dvp = dn;
-                br_prev = brn;
-                bc_prev = bcn;
+#pragma unroll
+                for (int j = 0; j < C; ++j) {
+                    dvp[j] = dn[j];
+                    br_prev[j] = brn[j];
+                    bc_prev[j] = bcn[j];
+                }
             }
         }
         q0 += n_loads;

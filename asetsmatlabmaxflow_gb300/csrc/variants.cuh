@@ -6,10 +6,11 @@
 
 namespace asets {
 
-template <int DIM, int NW, int NSTAGE, int EPI, bool EXACT, int MINB = (DIM == 3 ? 2 : 4)>
+template <int DIM, int NW, int NSTAGE, int EPI, bool EXACT, int MINB = (DIM == 3 ? 2 : 4),
+          int UNROLL = 1, int CELLS = 1>
 StencilVariant make_variant()
 {
-    using G = ColGeom<DIM, NW>;
+    using G = ColGeom<DIM, NW, CELLS>;
     StencilVariant v;
     v.dim = DIM;
     v.epi = EPI;
@@ -22,7 +23,7 @@ StencilVariant make_variant()
     v.box_rows = G::LR;
     v.box_cols = G::LC;
     v.box_cols_bc = G::LC_BC;
-    v.fn = reinterpret_cast<const void *>(&stencil_col_kernel<DIM, NW, NSTAGE, EPI, EXACT, MINB>);
+    v.fn = reinterpret_cast<const void *>(&stencil_col_kernel<DIM, NW, NSTAGE, EPI, EXACT, MINB, UNROLL, CELLS>);
     return v;
 }
 
