@@ -419,9 +419,9 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         // reads the tile boxes of stage t+1), so after the X barrier no one
         // reads stage t any more and step t refills its slot with plane
         // t+NSTAGE.  Labelled models (kEarly): the first two stages arrive
-        // here and every later one before the Y barrier two steps ahead (two
-        // barriers per step).  Binary: its larger stages are waited for at the
-        // top of the step that first reads them (three barriers per step).
+        // here and every later one before the Y barrier two steps ahead.
+        // Binary: every thread waits for its larger stages at the top of the
+        // step that first reads them.  Two block barriers per step.
         constexpr bool kEarly = (EPI == EPI_DIV);   // wait before the Y barrier
         constexpr int kLead = NSTAGE;                // refill the slot read by this X
         if constexpr (kEarly) {
@@ -440,19 +440,17 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         for (int t = 0; t < n_steps && !aborted; ++t) {
             const int s = p_first + t;
             const int st_cur = (q0 + t) % NSTAGE, st_nxt = (q0 + t + 1) % NSTAGE;
+            bool wait_ok = true;
             if constexpr (!kEarly) {
-                bool ok = true;
-                if (producer) {
-                    ok = mbar_wait_bounded(&bars[st_cur], ((q0 + t) / NSTAGE) & 1, &s_abort);
-                    ok = ok && mbar_wait_bounded(&bars[st_nxt], ((q0 + t + 1) / NSTAGE) & 1, &s_abort);
-                }
-                // the barrier publishes the completed stages to every thread
-                if (__syncthreads_or(!ok)) {
-                    aborted = true;
-                    // loads issued: the prologue, then one per earlier step
-                    abort_item(t, min(n_loads, t + NSTAGE));
-                    break;
-                }
+                // Every thread waits on the mbarrier of the stage it is about
+                // to read (stage t+1; stage t too on the first step), which
+                // also makes the stage's data visible to it: no block barrier
+                // here, so a warp starts X as soon as its data is there
+                // instead of after the slowest warp's Z.  A timeout is acted
+                // on at the X barrier.
+                if (t == 0)
+                    wait_ok = mbar_wait_bounded(&bars[st_cur], ((q0 + t) / NSTAGE) & 1, &s_abort);
+                wait_ok = wait_ok && mbar_wait_bounded(&bars[st_nxt], ((q0 + t + 1) / NSTAGE) & 1, &s_abort);
             }
             const bool s_in = (s >= 0 && s < ns);
             const bool sb_in = (s >= 1 && s < ns);          // stream face s is interior
@@ -514,7 +512,16 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                     ld_cells<C>(BCp + gi_right, bc_rt);
                 }
             }
-            __syncthreads();
+            if constexpr (!kEarly) {
+                if (__syncthreads_or(!wait_ok)) {
+                    aborted = true;
+                    // loads issued: the prologue, then one per earlier step
+                    abort_item(t, min(n_loads, t + NSTAGE));
+                    break;
+                }
+            } else {
+                __syncthreads();
+            }
 
             // refill a slot whose last readers finished before the barrier
             if (producer && t + kLead < n_loads)
