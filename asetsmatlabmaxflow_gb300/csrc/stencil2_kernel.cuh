@@ -418,40 +418,23 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         // Step t reads the stages of planes t and t+1 (X; the binary Z also
         // reads the tile boxes of stage t+1), so after the X barrier no one
         // reads stage t any more and step t refills its slot with plane
-        // t+NSTAGE.  Labelled models (kEarly): the first two stages arrive
-        // here and every later one before the Y barrier two steps ahead.
-        // Binary: every thread waits for its larger stages at the top of the
-        // step that first reads them.  Two block barriers per step.
-        constexpr bool kEarly = (EPI == EPI_DIV);   // wait before the Y barrier
-        constexpr int kLead = NSTAGE;                // refill the slot read by this X
-        if constexpr (kEarly) {
-            bool ok = true;
-            if (producer) {
-                ok = mbar_wait_bounded(&bars[q0 % NSTAGE], (q0 / NSTAGE) & 1, &s_abort);
-                ok = ok && mbar_wait_bounded(&bars[(q0 + 1) % NSTAGE], ((q0 + 1) / NSTAGE) & 1, &s_abort);
-            }
-            if (__syncthreads_or(!ok)) {
-                aborted = true;
-                abort_item(0, min(NSTAGE, n_loads));
-            }
-        }
+        // t+NSTAGE.  Every thread waits for the stages it reads at the top of
+        // the step that first reads them.  Two block barriers per step.
+        constexpr int kLead = NSTAGE;   // refill the slot read by this X
 
 #pragma unroll UNROLL
         for (int t = 0; t < n_steps && !aborted; ++t) {
             const int s = p_first + t;
             const int st_cur = (q0 + t) % NSTAGE, st_nxt = (q0 + t + 1) % NSTAGE;
+            // Every thread waits on the mbarrier of the stage it is about to
+            // read (stage t+1; stage t too on the first step), which also
+            // makes the stage's data visible to it: no block barrier here, so
+            // a warp starts X as soon as its data is there instead of after
+            // the slowest warp's Z.  A timeout is acted on at the X barrier.
             bool wait_ok = true;
-            if constexpr (!kEarly) {
-                // Every thread waits on the mbarrier of the stage it is about
-                // to read (stage t+1; stage t too on the first step), which
-                // also makes the stage's data visible to it: no block barrier
-                // here, so a warp starts X as soon as its data is there
-                // instead of after the slowest warp's Z.  A timeout is acted
-                // on at the X barrier.
-                if (t == 0)
-                    wait_ok = mbar_wait_bounded(&bars[st_cur], ((q0 + t) / NSTAGE) & 1, &s_abort);
-                wait_ok = wait_ok && mbar_wait_bounded(&bars[st_nxt], ((q0 + t + 1) / NSTAGE) & 1, &s_abort);
-            }
+            if (t == 0)
+                wait_ok = mbar_wait_bounded(&bars[st_cur], ((q0 + t) / NSTAGE) & 1, &s_abort);
+            wait_ok = wait_ok && mbar_wait_bounded(&bars[st_nxt], ((q0 + t + 1) / NSTAGE) & 1, &s_abort);
             const bool s_in = (s >= 0 && s < ns);
             const bool sb_in = (s >= 1 && s < ns);          // stream face s is interior
             const bool sp_in = (s - 1 >= 0 && s - 1 < ns);
@@ -512,15 +495,11 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                     ld_cells<C>(BCp + gi_right, bc_rt);
                 }
             }
-            if constexpr (!kEarly) {
-                if (__syncthreads_or(!wait_ok)) {
-                    aborted = true;
-                    // loads issued: the prologue, then one per earlier step
-                    abort_item(t, min(n_loads, t + NSTAGE));
-                    break;
-                }
-            } else {
-                __syncthreads();
+            if (__syncthreads_or(!wait_ok)) {
+                aborted = true;
+                // loads issued: the prologue, then one per earlier step
+                abort_item(t, min(n_loads, t + NSTAGE));
+                break;
             }
 
             // refill a slot whose last readers finished before the barrier
@@ -583,23 +562,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                     alpha_prev[j] = alpha_cur[j];
                 }
             }
-            if constexpr (kEarly) {
-                // the stage of plane s+2 (read by the next step's X) arrives
-                // before this barrier, which also publishes Y's shared planes
-                bool ok = true;
-                if (producer && t + 2 < n_loads) {
-                    const unsigned int q = q0 + t + 2;
-                    ok = mbar_wait_bounded(&bars[q % NSTAGE], (q / NSTAGE) & 1, &s_abort);
-                }
-                if (__syncthreads_or(!ok)) {
-                    aborted = true;
-                    // loads issued: the prologue, then one per step
-                    abort_item(t + 2, min(n_loads, t + NSTAGE + 1));
-                    break;
-                }
-            } else {
-                __syncthreads();
-            }
+            __syncthreads();
 
             // ---- Z: row/column faces of plane s-1 and the output of plane s-2
             {

@@ -53,8 +53,10 @@ def parse():
                     help="run one solve of N iterations of the workload and exit (for ncu)")
     ap.add_argument("--shape", default="256,256,256", help="volume for --profile-iters")
     ap.add_argument("--tile-config", type=int, default=0, help="kernel variant for --profile-iters")
-    ap.add_argument("--profile-model", default="binary", choices=["binary", "potts"],
-                    help="model for --profile-iters (potts: the warm-start workload, seed 1000000)")
+    ap.add_argument("--profile-model", default="binary",
+                    choices=["binary", "potts", "potts192", "ishikawa1024"],
+                    help="model for --profile-iters (potts: the warm-start workload, seed 1000000; "
+                         "potts192: Potts 3D 192^3 L=4; ishikawa1024: Ishikawa 2D 1024^2 L=8)")
     ap.add_argument("--profile-conv", type=int, default=0,
                     help="run the warm-start network's forward pass on an S^3 volume and exit")
     return ap.parse_args()
@@ -101,6 +103,21 @@ def profile_run(args):
         ms, n = run.s.last_run_stats()
         print(json.dumps({"profile_run": "potts 128^3 L=6", "iterations": it,
                           "ms_per_iteration": ms / max(args.profile_iters, 1)}))
+        return
+    if args.profile_model in ("potts192", "ishikawa1024"):
+        # the multi-region configurations: cc 0.3, steps 0.11 (3D) / 0.16 (2D)
+        if args.profile_model == "potts192":
+            ct, a = synth.potts3d(seed=0)
+            model, dims, L, steps = "potts", ct.shape[:3], ct.shape[3], 0.11
+        else:
+            ct, a = synth.ishikawa2d(seed=0)
+            model, dims, L, steps = "ishikawa", ct.shape[:2], ct.shape[2], 0.16
+        s = N.Solver(N.Context.default(), model, dims, L)
+        s.set_inputs(ct, a)
+        it = s.run(args.profile_iters, 0.0, 0.3, steps, tile_config=args.tile_config)
+        ms, n = s.last_run_stats()
+        print(json.dumps({"profile_run": f"{model} {'x'.join(map(str, dims))} L={L}",
+                          "iterations": it, "ms_per_iteration": ms / max(args.profile_iters, 1)}))
         return
     shape = tuple(int(x) for x in args.shape.split(","))
     cs, ct, alpha = synth.binary3d(seed=0, shape=shape)
@@ -452,7 +469,7 @@ def main():
                     "h2d_bytes_per_step": 3 * nvox * 4, "d2h_bytes_per_step": nvox * 4 + ITERS * 4},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "peak_kind": peak_kind, "kernel": "stencil_col_kernel<3, 32 warps (28x28 tile), 4 stages, binary, fast>",
+                         "peak_kind": peak_kind, "kernel": "stencil_col_kernel<3, 20 warps, 2 rows per thread (60x16 tile), 4 stages, binary, fast>",
                          "bytes_per_voxel_iter": BYTES_PER_VOXEL_ITER,
                          "launch_ms": per_launch_ms},
             "time_to_errbound": {"err_bound": 1e-4, "iterations": conv_it, "ms": conv_ms,
