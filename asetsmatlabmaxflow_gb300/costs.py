@@ -4,8 +4,6 @@ applications.  Host arrays in Matlab index order (Fortran), label last;
 torch CUDA tensors are accepted as device arrays (flat, Matlab layout)."""
 from __future__ import annotations
 
-import ctypes
-
 import numpy as np
 
 from . import native as N

@@ -32,7 +32,6 @@ using namespace asets;
 namespace {
 
 constexpr long long kNoallocMaxCells = 262144;  // padded voxels (row pitch x Nx x Nz)
-constexpr size_t kAlign = 256;
 constexpr size_t kFieldBytes = (size_t)kNoallocMaxCells * sizeof(float);
 // 3 inputs + 2 parities x (3 flow components + ps + pt + u)
 constexpr size_t kNumFields = 3 + 2 * 6;

@@ -7,7 +7,6 @@ from __future__ import annotations
 
 import ctypes
 import os
-from pathlib import Path
 
 import numpy as np
 

@@ -418,7 +418,7 @@ ASETS_API asets_status asets_matlab_solve(asets_context *ctx, int model, int pre
 
 /* ------------------------------------------------------------------------
  * Cost terms and regularisation weights on the GPU: the step before the
- * solvers in the reference's applications (applications/*.m; no counterpart
+ * solvers in the reference's applications (the applications folder; no counterpart
  * in its C code).  Arrays in Matlab layout, label slowest; `where` says
  * whether the pointers are host or device memory.  Normalisation divides by
  * the volume's own range, (I - min I) / (max I - min I), in float32.

@@ -7,7 +7,6 @@ this module, and only as the checker or the timed CPU baseline.
 from __future__ import annotations
 
 import ctypes
-from pathlib import Path
 
 import numpy as np
 
