@@ -90,6 +90,7 @@ struct LabelArgs {
     int pitch, nr, nlab;
     float cc, inv_cc, inv_cc_l;  // 1/cc and 1/(cc*L) as the reference rounds them
     int exact;               // 1: the reference's divisions; 0: reciprocal multiplies
+    unsigned int *done_count;  // batch: finished-problem counter, or null
 };
 
 int label_kernel_grid(long long cells, int num_sms);

@@ -8,10 +8,12 @@
 
 namespace asets {
 
+// done_count (or null): counter of finished problems of a batch, bumped when
+// this problem finishes.
 template <int NT>
 __device__ __forceinline__ void finish_iteration(float erru, IterControl *ctl, double *partials,
                                                  float *cvg, int it, double *s_red,
-                                                 int *s_is_last)
+                                                 int *s_is_last, unsigned int *done_count)
 {
     const double part = block_sum_double<NT>(erru, s_red);
     if (threadIdx.x == 0) {
@@ -36,15 +38,21 @@ __device__ __forceinline__ void finish_iteration(float erru, IterControl *ctl, d
             cvg[it] = c;
             ctl->last_iter = it;
             const bool conv = ctl->break_lt ? (c < ctl->err_bound) : (c <= ctl->err_bound);
+            int done = 0;
             if (ctl->error || conv) {
-                ctl->done = 1;
+                done = 1;
                 ctl->it_num = it;
             } else if (it + 1 >= ctl->max_it) {
-                ctl->done = 1;
+                done = 1;
                 ctl->it_num = ctl->max_it;
             }
             ctl->ticket = 0;
             ctl->iter = it + 1;
+            if (done) {
+                ctl->done = 1;
+                if (done_count)
+                    atomicAdd(done_count, 1u);
+            }
             __threadfence();
         }
     }

@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(kLabelThreads) potts_label_kernel(LabelArgs A)
             }
         }
     }
-    finish_iteration<kLabelThreads>(erru, ctl, A.partials, A.cvg, it, s_red, &s_is_last);
+    finish_iteration<kLabelThreads>(erru, ctl, A.partials, A.cvg, it, s_red, &s_is_last, A.done_count);
 }
 
 template <bool EXACT>
@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(kLabelThreads) ishikawa_label_kernel(LabelArgs
             u_below = u_k;
         }
     }
-    finish_iteration<kLabelThreads>(erru, ctl, A.partials, A.cvg, it, s_red, &s_is_last);
+    finish_iteration<kLabelThreads>(erru, ctl, A.partials, A.cvg, it, s_red, &s_is_last, A.done_count);
 }
 
 int label_kernel_grid(long long cells, int num_sms)

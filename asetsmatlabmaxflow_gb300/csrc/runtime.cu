@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <chrono>
 #include <cstdarg>
@@ -1268,9 +1269,10 @@ extern "C" ASETS_API asets_status asets_solver_last_run_stats(asets_solver *s, f
 }
 
 // ---------------------------------------------------------------- batch
-// Many independent binary problems solved together: one launch per
-// dimension group and iteration over all live problems' work items; each
-// problem converges (and retires) on its own.
+// Many independent problems solved together: per iteration one launch of
+// the fused flow pass per group (binary / labelled x 2D / 3D) over all live
+// problems' work items, then, for the labelled models, each problem's label
+// kernel; each problem converges (and retires) on its own.
 struct asets_batch {
     asets_context *ctx = nullptr;
     std::vector<asets_solver *> members;
@@ -1285,14 +1287,23 @@ struct asets_batch {
         BatchArgs bargs;
         int grid = 0;
         int tile_config = 0;
-    } groups[2];  // [0] 2D, [1] 3D
+    } groups[4];  // [0] binary 2D, [1] binary 3D, [2] labelled 2D, [3] labelled 3D
     unsigned int *d_done = nullptr;
     ChunkGraph graph;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, flag_ev[2] = {nullptr, nullptr};
     std::vector<void *> allocations;
     float last_ms = 0.f;
     int last_launches = 0;
+    asets_batch *level[kMaxLevels] = {};  // multilevel runs: the members' coarse levels
 };
+
+// done counter, then three queue words per group
+static constexpr int kBatchCounters = 16;
+
+static int batch_group(const asets_solver *s)
+{
+    return (s->dim == 3 ? 1 : 0) + (s->model == ASETS_BINARY ? 0 : 2);
+}
 
 extern "C" ASETS_API asets_status asets_batch_create(asets_context *ctx, asets_batch **out)
 {
@@ -1303,11 +1314,11 @@ extern "C" ASETS_API asets_status asets_batch_create(asets_context *ctx, asets_b
     std::unique_ptr<asets_batch> b(new asets_batch);
     b->ctx = ctx;
     void *p = nullptr;
-    CU_TRY(cudaMalloc(&p, 16 * sizeof(unsigned int)));
+    CU_TRY(cudaMalloc(&p, kBatchCounters * sizeof(unsigned int)));
     b->allocations.push_back(p);
     b->d_done = static_cast<unsigned int *>(p);
-    b->groups[0].d_queue = b->d_done + 4;
-    b->groups[1].d_queue = b->d_done + 8;
+    for (int g = 0; g < 4; ++g)
+        b->groups[g].d_queue = b->d_done + 4 + 3 * g;
     CU_TRY(cudaEventCreate(&b->ev0));
     CU_TRY(cudaEventCreate(&b->ev1));
     CU_TRY(cudaEventCreateWithFlags(&b->flag_ev[0], cudaEventDisableTiming));
@@ -1320,6 +1331,8 @@ extern "C" ASETS_API void asets_batch_destroy(asets_batch *b)
 {
     if (!b)
         return;
+    for (asets_batch *lb : b->level)
+        asets_batch_destroy(lb);
     DeviceGuard guard(b->ctx->device);
     cudaStreamSynchronize(b->ctx->stream);
     b->graph.reset();
@@ -1337,8 +1350,6 @@ extern "C" ASETS_API asets_status asets_batch_add(asets_batch *b, asets_solver *
         return fail(ASETS_ERR_INVALID_ARG, "NULL argument");
     if (s->ctx != b->ctx)
         return fail(ASETS_ERR_INVALID_ARG, "solver belongs to another context");
-    if (s->model != ASETS_BINARY)
-        return fail(ASETS_ERR_UNSUPPORTED, "batches hold binary problems");
     for (asets_solver *m : b->members)
         if (m == s)
             return fail(ASETS_ERR_INVALID_ARG, "solver already in the batch");
@@ -1387,7 +1398,7 @@ static asets_status batch_layout(asets_batch *b, asets_batch::Group &g)
         sp.nr = s->nr;
         sp.nc = s->nc;
         sp.ns = s->ns;
-        sp.flow_labels = 1;
+        sp.flow_labels = s->flow_labels;
         const int items = problem_items(sp, *g.v, d.zchunks);
         asets_status st = ensure_items(s, items);
         if (st != ASETS_OK)
@@ -1438,7 +1449,8 @@ static asets_status batch_layout(asets_batch *b, asets_batch::Group &g)
 
 static cudaError_t batch_launch_iteration(asets_batch *b)
 {
-    for (auto &g : b->groups) {
+    for (int gi = 0; gi < 4; ++gi) {
+        auto &g = b->groups[gi];
         if (g.idx.empty())
             continue;
         void *params[] = {&g.bargs};
@@ -1446,12 +1458,26 @@ static cudaError_t batch_launch_iteration(asets_batch *b)
                                          g.v->smem_bytes, b->ctx->stream);
         if (e != cudaSuccess)
             return e;
+        if (gi < 2)
+            continue;
+        // labelled models: each problem's label kernel closes its iteration
+        // (it returns at once for a finished problem) and counts it when done
+        for (int i : g.idx) {
+            asets_solver *s = b->members[i];
+            LabelArgs la = label_args(s);
+            la.done_count = b->d_done;
+            const int grid = label_kernel_grid(s->cells, s->ctx->num_sms);
+            e = s->model == ASETS_POTTS ? launch_potts_labels(la, grid, b->ctx->stream)
+                                        : launch_ishikawa_labels(la, grid, b->ctx->stream);
+            if (e != cudaSuccess)
+                return e;
+        }
     }
     return cudaSuccess;
 }
 
 // Prepare every member and lay out the groups for the given tile configs.
-static asets_status batch_prepare(asets_batch *b, int flags, const int tile_config[2], int maxIt,
+static asets_status batch_prepare(asets_batch *b, int flags, const int tile_config[4], int maxIt,
                                   float errBound, float cc, float steps)
 {
     for (auto &g : b->groups) {
@@ -1462,7 +1488,7 @@ static asets_status batch_prepare(asets_batch *b, int flags, const int tile_conf
         asets_solver *s = b->members[i];
         if (!s->inputs_set)
             return fail(ASETS_ERR_INVALID_ARG, "batch member %zu has no inputs", i);
-        const int gi = (s->dim == 3) ? 1 : 0;
+        const int gi = batch_group(s);
         asets_status st = prepare_run(s, flags, tile_config[gi], maxIt, errBound, cc, steps);
         if (st != ASETS_OK)
             return st;
@@ -1471,7 +1497,7 @@ static asets_status batch_prepare(asets_batch *b, int flags, const int tile_conf
         b->groups[gi].tile_config = tile_config[gi];
     }
     cudaStream_t st = b->ctx->stream;
-    CU_TRY(cudaMemsetAsync(b->d_done, 0, 16 * sizeof(unsigned int), st));
+    CU_TRY(cudaMemsetAsync(b->d_done, 0, kBatchCounters * sizeof(unsigned int), st));
     for (auto &g : b->groups) {
         asets_status s2 = batch_layout(b, g);
         if (s2 != ASETS_OK)
@@ -1495,14 +1521,14 @@ static asets_status batch_execute(asets_batch *b, int maxIt, int *chunks)
 static std::mutex g_tune_mu;
 static std::vector<std::pair<std::string, int>> g_tune_cache;
 
-static asets_status batch_autotune(asets_batch *b, int flags, float cc, float steps, int tile_config[2])
+static asets_status batch_autotune(asets_batch *b, int flags, float cc, float steps, int tile_config[4])
 {
     const int exact = (flags & ASETS_FLAG_EXACT) ? 1 : 0;
-    for (int gi = 0; gi < 2; ++gi) {
+    for (int gi = 0; gi < 2; ++gi) {  // the binary groups
         long long vox = 0;
         int count = 0;
         for (asets_solver *s : b->members)
-            if ((s->dim == 3) == (gi == 1)) {
+            if (batch_group(s) == gi) {
                 vox += s->cells;
                 ++count;
             }
@@ -1527,7 +1553,7 @@ static asets_status batch_autotune(asets_batch *b, int flags, float cc, float st
         int best = 1;
         float best_ms = 1e30f;
         for (int cand = 1; cand <= n; ++cand) {
-            int tc[2] = {tile_config[0], tile_config[1]};
+            int tc[4] = {tile_config[0], tile_config[1], tile_config[2], tile_config[3]};
             tc[gi] = cand;
             asets_status st = batch_prepare(b, flags, tc, kGraphIters, 0.0f, cc, steps);
             if (st != ASETS_OK)
@@ -1569,7 +1595,7 @@ extern "C" ASETS_API asets_status asets_batch_run(asets_batch *b, const asets_op
     cudaStream_t st = b->ctx->stream;
     // one kernel variant per dimension group (default: the first)
     const int tc0 = (opt && opt->tile_config > 0) ? opt->tile_config : 1;
-    int tile_config[2] = {tc0, tc0};
+    int tile_config[4] = {tc0, tc0, tc0, tc0};
     if ((flags & ASETS_FLAG_AUTOTUNE) && maxIt > 0) {
         asets_status ts = batch_autotune(b, flags, cc, steps, tile_config);
         if (ts != ASETS_OK)
@@ -1594,10 +1620,11 @@ extern "C" ASETS_API asets_status asets_batch_run(asets_batch *b, const asets_op
     float ms = 0.f;
     CU_TRY(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
     b->last_ms = ms;
-    int ngroups = 0;
-    for (auto &g : b->groups)
-        ngroups += g.idx.empty() ? 0 : 1;
-    b->last_launches = chunks * kGraphIters * ngroups;
+    int per_iter = 0;  // flow passes, plus the labelled members' label kernels
+    for (int gi = 0; gi < 4; ++gi)
+        if (!b->groups[gi].idx.empty())
+            per_iter += 1 + (gi >= 2 ? (int)b->groups[gi].idx.size() : 0);
+    b->last_launches = chunks * kGraphIters * per_iter;
     b->groups[0].tile_config = tile_config[0];
     b->groups[1].tile_config = tile_config[1];
     for (size_t i = 0; i < b->members.size(); ++i) {
@@ -1633,6 +1660,90 @@ extern "C" ASETS_API asets_status asets_batch_last_run_stats(asets_batch *b, flo
     if (tile_configs) {
         tile_configs[0] = b->groups[0].tile_config;
         tile_configs[1] = b->groups[1].tile_config;
+    }
+    return ASETS_OK;
+}
+
+// Coarse-to-fine solve of every member (asets_solver_run_multilevel for a
+// batch): level k of all members that have one runs as one batch, each
+// member's coarsest level from its own initial state, every finer level from
+// the prolonged solution of the level below.
+extern "C" ASETS_API asets_status asets_batch_run_multilevel(asets_batch *b,
+                                                             const asets_options *opt,
+                                                             int levels, int maxIt,
+                                                             float errBound, float cc,
+                                                             float steps, int *itNums)
+{
+    if (!b || levels < 1 || maxIt < 0)
+        return fail(ASETS_ERR_INVALID_ARG, "bad multilevel arguments");
+    std::lock_guard<std::recursive_mutex> lock(b->ctx->mu);
+    DeviceGuard guard(b->ctx->device);
+    const size_t m = b->members.size();
+    std::vector<int> built(m, 1);
+    std::vector<std::array<asets_solver *, kMaxLevels>> lv(m);
+    int top = 0;
+    for (size_t i = 0; i < m; ++i) {
+        asets_solver *s = b->members[i];
+        if (!s->inputs_set)
+            return fail(ASETS_ERR_INVALID_ARG, "batch member %zu has no inputs", i);
+        asets_status st = ml_prepare(s, levels, &built[i]);
+        if (st != ASETS_OK)
+            return st;
+        lv[i][0] = s;
+        for (int k = 1; k < built[i]; ++k)
+            lv[i][k] = lv[i][k - 1]->coarse;
+        s->ml_levels = 0;
+        top = std::max(top, built[i]);
+    }
+    std::vector<int> its(m, 0);
+    for (int k = top - 1; k >= 0; --k) {
+        asets_batch *lb = b;
+        if (k > 0) {
+            if (!b->level[k]) {
+                asets_status st = asets_batch_create(b->ctx, &b->level[k]);
+                if (st != ASETS_OK)
+                    return st;
+            }
+            lb = b->level[k];
+            lb->members.clear();
+            lb->graph.reset();
+        }
+        std::vector<size_t> who;
+        for (size_t i = 0; i < m; ++i) {
+            if (built[i] <= k)
+                continue;
+            if (k < built[i] - 1) {
+                asets_status st = ml_prolong(lv[i][k + 1], lv[i][k]);
+                if (st != ASETS_OK)
+                    return st;
+            }
+            if (k > 0)
+                lb->members.push_back(lv[i][k]);
+            who.push_back(i);
+        }
+        std::vector<int> lit(lb->members.size(), 0);
+        asets_status st = asets_batch_run(lb, opt, maxIt, errBound, cc, steps, lit.data());
+        for (size_t i : who)
+            if (k < built[i] - 1) {
+                lv[i][k]->warm = false;  // the prolonged state is consumed by this run
+                lv[i][k]->warm_flows = false;
+            }
+        if (st != ASETS_OK)
+            return st;
+        // the full-resolution batch is `b` itself: its itNums are in member order
+        for (size_t j = 0; j < who.size(); ++j) {
+            const size_t i = who[j];
+            const int it = (k > 0) ? lit[j] : lit[i];
+            b->members[i]->ml_iters[k] = it;
+            b->members[i]->ml_ms[k] = lb->last_ms;
+            if (k == 0)
+                its[i] = it;
+        }
+    }
+    for (size_t i = 0; i < m; ++i) {
+        b->members[i]->ml_levels = built[i];
+        if (itNums)
+            itNums[i] = its[i];
     }
     return ASETS_OK;
 }

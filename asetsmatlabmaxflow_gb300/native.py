@@ -150,6 +150,9 @@ _SIGS = {
     "asets_batch_last_run_stats": (ctypes.c_int, [_VP, ctypes.POINTER(ctypes.c_float),
                                                   ctypes.POINTER(ctypes.c_int),
                                                   ctypes.POINTER(ctypes.c_int), _VP]),
+    "asets_batch_run_multilevel": (ctypes.c_int, [_VP, _VP, ctypes.c_int, ctypes.c_int,
+                                                  ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                                  _VP]),
     "asets_conv3d_bf16": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, ctypes.c_int, ctypes.c_int,
                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "asets_wsnet_num_params": (ctypes.c_int, []),
@@ -413,7 +416,8 @@ class Solver:
 
 
 class Batch:
-    """Many binary solvers run together (asets_batch_*)."""
+    """Many solvers run together (asets_batch_*): binary and labelled models,
+    2D and 3D, each converging on its own."""
 
     def __init__(self, ctx: Context):
         self.ctx = ctx
@@ -433,6 +437,19 @@ class Batch:
         its = (ctypes.c_int * max(len(self.members), 1))()
         check(lib().asets_batch_run(self._h, ctypes.byref(opt), max_it, err_bound, cc, steps,
                                     ctypes.addressof(its)))
+        for s in self.members:
+            s.last_max_it = max_it
+        return list(its[:len(self.members)])
+
+    def run_multilevel(self, levels: int, max_it: int, err_bound: float, cc: float, steps: float,
+                       *, exact: bool = False) -> list[int]:
+        """Coarse-to-fine solve of every member (asets_batch_run_multilevel);
+        full-resolution itNum per member, per-level ones in each member's
+        multilevel_stats()."""
+        opt = Options(flags=FLAG_EXACT if exact else 0, tile_config=0)
+        its = (ctypes.c_int * max(len(self.members), 1))()
+        check(lib().asets_batch_run_multilevel(self._h, ctypes.byref(opt), levels, max_it,
+                                               err_bound, cc, steps, ctypes.addressof(its)))
         for s in self.members:
             s.last_max_it = max_it
         return list(its[:len(self.members)])

@@ -318,6 +318,64 @@ def evaluate(net: N.WarmStartNet, cold_budget: int, seeds, *, level: int = LEVEL
     return out
 
 
+def evaluate_batched(net: N.WarmStartNet, cold_budget: int, seeds, *, level: int = LEVELS - 1,
+                     runs: list | None = None) -> dict:
+    """The batched form on held-out seeds: every problem solved in one batch
+    (asets_batch_*), cold -- one batch of the full-resolution solvers --
+    against the learned warm start -- the network's coarsest-level state for
+    each problem, then one batch per level (asets_batch_run_multilevel),
+    members whose full-resolution iterations reach the cold budget solved
+    again cold as one batch.  Wall times of the whole batch, per-member
+    iterations and label agreement with the cold batch's labels."""
+    own = runs is None
+    runs = runs or [Runner() for _ in seeds]
+    for run, sd in zip(runs, seeds):
+        ct, a1, af = problem(sd)
+        run.load(ct, af)
+    ctx = runs[0].ctx
+    cold = N.Batch(ctx)
+    for run in runs:
+        run.lv[0].set_initial(None)
+        cold.add(run.s)
+    cold_its, cold_ms = _sync_ms(lambda: cold.run(MAX_IT, EVAL_ERR, CC, STEPS))
+    lab_c = [labels(run.lv[0].read_state()[0], run.n).clone() for run in runs]
+    cold.close()
+
+    warm = N.Batch(ctx)
+    for run in runs:
+        warm.add(run.s)
+
+    def warm_path():
+        for run in runs:
+            lv = run.lv[level]
+            net.predict(lv.shape, lv.ct, lv.alpha, *lv.state)
+            lv.set_initial(lv.state)
+        its = warm.run_multilevel(len(runs[0].lv), MAX_IT, EVAL_ERR, CC, STEPS)
+        fb = [i for i, it in enumerate(its) if it >= cold_budget]
+        if fb:
+            again = N.Batch(ctx)
+            for i in fb:
+                runs[i].lv[0].set_initial(None)
+                again.add(runs[i].s)
+            again.run(MAX_IT, EVAL_ERR, CC, STEPS)
+            again.close()
+        return its, fb
+
+    (warm_its, fb), warm_ms = _sync_ms(warm_path)
+    level_its = [run.s.multilevel_stats()[0] for run in runs]
+    agree = [float((labels(run.lv[0].read_state()[0], run.n) == lc).float().mean())
+             for run, lc in zip(runs, lab_c)]
+    warm.close()
+    if own:
+        for run in runs:
+            run.close()
+    return {"problems": len(runs), "cold_batch_ms": cold_ms, "warm_batch_ms": warm_ms,
+            "wall_ratio_cold_over_warm": cold_ms / warm_ms,
+            "cold_iters": list(cold_its), "warm_iters": list(warm_its),
+            "warm_level_iters": level_its, "fallbacks": len(fb),
+            "agree_cold_mean": float(np.mean(agree)), "agree_cold_min": float(min(agree))}
+
+
 def summarize(res: list[EvalResult]) -> dict:
     c_it = np.array([r.cold_it for r in res], float)
     w_it = np.array([r.warm_its[0] + (r.cold_it if r.fallback else 0) for r in res], float)

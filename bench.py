@@ -280,11 +280,18 @@ def warm_start_run(ctx, nseeds: int) -> dict:
     net, budget, level = W.load(ctx)
     run = W.Runner(ctx)
     W.evaluate(net, budget, [W.HELDOUT_SEED0 + 900], level=level, tight=False, run=run)  # warm-up
-    res = W.evaluate(net, budget, range(W.HELDOUT_SEED0, W.HELDOUT_SEED0 + nseeds), level=level,
-                     tight=False, run=run)
+    seeds = list(range(W.HELDOUT_SEED0, W.HELDOUT_SEED0 + nseeds))
+    res = W.evaluate(net, budget, seeds, level=level, tight=False, run=run)
     run.close()
+    # the same problems as one batch: cold batch against warm-started batch
+    runs = [W.Runner(ctx) for _ in seeds]
+    W.evaluate_batched(net, budget, seeds, level=level, runs=runs)  # warm-up
+    batched = W.evaluate_batched(net, budget, seeds, level=level, runs=runs)
+    for r in runs:
+        r.close()
     net.close()
     out = W.summarize(res)
+    out["batched"] = batched
     out["workload"] = ("Potts 3D 128^3 L=6 (means U[0,1], Voronoi 30-80 cells, noise U[.05,.2], "
                        "alpha U[.1,.5]), cc 0.3, steps 0.11, errBound 1e-4, held-out seeds "
                        f"{W.HELDOUT_SEED0}..{W.HELDOUT_SEED0 + nseeds - 1}; wall ms per solve")

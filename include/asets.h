@@ -232,7 +232,10 @@ typedef struct asets_batch asets_batch;
 
 ASETS_API asets_status asets_batch_create(asets_context *ctx, asets_batch **out);
 ASETS_API void asets_batch_destroy(asets_batch *b);
-/* Add a binary solver whose inputs are set; the batch does not own it. */
+/* Add a solver whose inputs are set (any model, 2D or 3D); the batch does
+ * not own it.  Members are grouped by dimension and by binary / labelled
+ * model; a group shares one fused-pass launch per iteration, and each
+ * labelled member's label kernel follows it. */
 ASETS_API asets_status asets_batch_add(asets_batch *b, asets_solver *s);
 /* Solve every member; itNums (optional) receives one itNum per member in
  * the order they were added.  Results are read from each solver
@@ -240,9 +243,20 @@ ASETS_API asets_status asets_batch_add(asets_batch *b, asets_solver *s);
 ASETS_API asets_status asets_batch_run(asets_batch *b, const asets_options *opt, int maxIt,
                                        float errBound, float cc, float steps, int *itNums);
 /* Device time of the last run, kernel launches, iterations summed over the
- * members, and the tile configuration used for the 2D and 3D groups. */
+ * members, and the tile configuration used for the binary 2D and 3D groups. */
 ASETS_API asets_status asets_batch_last_run_stats(asets_batch *b, float *ms, int *kernel_launches,
                                                   int *iterations, int *tile_configs);
+/* Coarse-to-fine solve of every member, the batch form of
+ * asets_solver_run_multilevel: level k of all members that have one runs as
+ * one batch (coarsest first, each member's coarsest level from its own
+ * initial state, e.g. a learned warm start set on asets_solver_level()),
+ * every finer level from the prolonged solution of the level below.
+ * itNums receives the full-resolution itNum per member; per-level itNums
+ * and the device time of each level's batch are in
+ * asets_solver_multilevel_stats of each member. */
+ASETS_API asets_status asets_batch_run_multilevel(asets_batch *b, const asets_options *opt,
+                                                  int levels, int maxIt, float errBound,
+                                                  float cc, float steps, int *itNums);
 
 /* ------------------------------------------------------------------------
  * Learned warm start building block (no counterpart in the reference):

@@ -88,3 +88,62 @@ def test_batch_autotune_and_repeat_are_deterministic():
     for s, u in zip(solvers, u1):
         np.testing.assert_array_equal(bits(s.get_u()), bits(u))
     b.close()
+
+
+def _labelled_problems():
+    """Potts and Ishikawa members of uneven sizes, 2D and 3D, with the
+    parameters of the multi-region configurations."""
+    from scipy.ndimage import gaussian_filter
+
+    g = np.random.default_rng(21)
+    out = []
+    for model, dims, L in [("potts", (97, 130), 4), ("potts", (40, 36, 28), 5),
+                           ("ishikawa", (120, 88), 6), ("ishikawa", (30, 34, 26), 4),
+                           ("potts", (64, 48, 40), 3)]:
+        ct = np.asfortranarray(gaussian_filter(g.random(dims + (L,)), 1.5).astype(np.float32))
+        la = L if model == "potts" else L - 1
+        alpha = np.asfortranarray((0.1 + 0.3 * g.random(dims + (la,))).astype(np.float32))
+        out.append((model, dims, L, ct, alpha))
+    return out
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_mixed_batch_with_labelled_members_equals_individual_solves(exact):
+    """Potts and Ishikawa problems (2D and 3D) batched with binary ones:
+    every member as when solved alone -- same itNum, u bit-identical in
+    EXACT mode -- while they converge at different iterations."""
+    from asetsmatlabmaxflow_gb300 import native as N
+
+    ctx = N.Context.default()
+    max_it, err_bound, cc, steps = 300, 2e-4, 0.3, 0.11
+    members = []
+    for model, dims, L, ct, alpha in _labelled_problems():
+        s = N.Solver(ctx, model, dims, L)
+        s.set_inputs(ct, alpha)
+        members.append(s)
+    for shape, cs, ct, alpha in _problems()[:2] + _problems()[4:5]:
+        s = N.Solver(ctx, "binary", shape)
+        s.set_inputs(ct, alpha, cs)
+        members.append(s)
+    ref = []
+    for s in members:
+        it = s.run(max_it, err_bound, cc, steps, exact=exact)
+        ref.append((it, s.get_u().copy(), s.get_cvg()[:it + 1].copy()))
+    b = N.Batch(ctx)
+    for s in members:
+        b.add(s)
+    its = b.run(max_it, err_bound, cc, steps, exact=exact)
+    assert len(set(its)) > 2
+    for s, it, (it_ref, u_ref, cvg_ref) in zip(members, its, ref):
+        assert it == it_ref
+        u = s.get_u()
+        if exact:
+            np.testing.assert_array_equal(bits(u), bits(u_ref))
+        else:
+            assert float(np.max(np.abs(u - u_ref))) <= 1e-5
+        np.testing.assert_allclose(s.get_cvg()[:it + 1], cvg_ref, rtol=1e-5)
+    st = b.last_run_stats()
+    assert st["iterations"] == sum(min(i + 1, max_it) for i in its)
+    b.close()
+    for s in members:
+        s.close()

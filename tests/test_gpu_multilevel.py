@@ -107,3 +107,42 @@ def test_level_handles_and_limits():
     with pytest.raises(N.AsetsError):
         s.level(2)
     s.close()
+
+
+@pytest.mark.parametrize("exact", [True, False])
+def test_batched_multilevel_equals_individual_multilevel(exact):
+    """asets_batch_run_multilevel: members of uneven sizes (so with different
+    level counts), Potts, Ishikawa and binary, 2D and 3D, solved level by
+    level as batches, come out as their own multilevel solves -- the same
+    itNum at every level, u bit-identical in EXACT mode."""
+    from asetsmatlabmaxflow_gb300 import native as N
+
+    ctx = N.Context.default()
+    members = [("potts", (72, 64, 40), 4), ("potts", (33, 20, 9), 3), ("ishikawa", (90, 70), 5),
+               ("binary", (96, 80, 48), 1), ("potts", (120, 100), 3)]
+    levels, max_it, err = 3, 400, 1e-4
+    solvers, ref = [], []
+    for j, (model, dims, L) in enumerate(members):
+        inp = _inputs(model, dims, L, 30 + j)
+        steps = 0.11 if len(dims) == 3 else 0.16
+        s = N.Solver(ctx, model, dims, L)
+        s.set_inputs(inp["Ct"], inp["alpha"], inp["Cs"])
+        # one cc and steps for the batch: the 3D value for all
+        it = s.run_multilevel(levels, max_it, err, 0.3, 0.11, exact=exact)
+        ref.append((it, s.multilevel_stats()[0], s.get_u().copy()))
+        solvers.append(s)
+    assert len({len(r[1]) for r in ref}) > 1  # members have different level counts
+    b = N.Batch(ctx)
+    for s in solvers:
+        b.add(s)
+    its = b.run_multilevel(levels, max_it, err, 0.3, 0.11, exact=exact)
+    for s, it, (it_ref, lv_ref, u_ref) in zip(solvers, its, ref):
+        assert it == it_ref
+        assert s.multilevel_stats()[0] == lv_ref
+        if exact:
+            np.testing.assert_array_equal(bits(s.get_u()), bits(u_ref))
+        else:
+            assert float(np.max(np.abs(s.get_u() - u_ref))) <= 1e-5
+    b.close()
+    for s in solvers:
+        s.close()

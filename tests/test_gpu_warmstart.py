@@ -31,3 +31,20 @@ def test_trained_network_gains_over_the_method_without_it():
     # the same multilevel solve started cold
     assert s["coarsest_iters_learned_mean"] < s["coarsest_iters_cold_start_mean"]
     net.close()
+
+
+def test_batched_warm_start_matches_single_solves():
+    """The batched warm-started solve (one batch per level) gives each
+    problem the iterations of its own warm-started multilevel solve, and the
+    cold batch each problem's cold itNum."""
+    from asetsmatlabmaxflow_gb300 import warmstart as W
+
+    net, budget, level = W.load()
+    seeds = [W.HELDOUT_SEED0 + 7, W.HELDOUT_SEED0 + 8, W.HELDOUT_SEED0 + 9]
+    single = W.evaluate(net, budget, seeds, level=level, tight=False)
+    batched = W.evaluate_batched(net, budget, seeds, level=level)
+    assert batched["cold_iters"] == [r.cold_it for r in single]
+    assert batched["warm_level_iters"] == [r.warm_its for r in single]
+    assert batched["fallbacks"] == sum(r.fallback for r in single)
+    assert batched["warm_batch_ms"] < batched["cold_batch_ms"]
+    net.close()
