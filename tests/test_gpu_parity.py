@@ -227,3 +227,27 @@ def test_every_binary3d_fast_variant_meets_parity_bar(tile_config):
     assert_north_star(model, dims, L, s.get_u().reshape(dims, order="F"),
                       ref["u"].reshape(dims, order="F"), s.get_cvg(), refd["cvg"])
     s.close()
+
+
+@pytest.mark.parametrize("dims", [(33, 41, 29), (61, 17, 9), (5, 7, 3), (121, 13, 6), (1, 9, 8)])
+def test_odd_shapes_binary3d_against_oracle(dims):
+    """Binary 3D volumes whose row count is odd, below one tile, or a single
+    row: the default two-rows-per-thread kernel's last pair straddles the
+    volume's end (one cell stored alone).  EXACT bit-exact, fast to the
+    parity bar, both against the oracle."""
+    from asetsmatlabmaxflow_gb300 import native as N
+
+    inp = _rand("binary", dims, 1, 11)
+    maxit, cc, steps = 30, 0.35, 0.11
+    ref = O.solve("binary", dims, inp["Ct"], inp["alpha"], cs=inp["Cs"], max_it=maxit,
+                  err_bound=0.0, cc=cc, steps=steps)
+    refd = O.solve("binary", dims, inp["Ct"], inp["alpha"], cs=inp["Cs"], max_it=maxit,
+                   err_bound=0.0, cc=cc, steps=steps, erru_double=True)
+    s = N.Solver(N.Context.default(), "binary", dims)
+    s.set_inputs(inp["Ct"], inp["alpha"], inp["Cs"])
+    assert s.run(maxit, 0.0, cc, steps, exact=True) == ref["it"]
+    np.testing.assert_array_equal(bits(s.get_u()), bits(ref["u"]))
+    s.run(maxit, 0.0, cc, steps, exact=False)
+    assert_north_star("binary", dims, 1, s.get_u().reshape(dims, order="F"),
+                      ref["u"].reshape(dims, order="F"), s.get_cvg(), refd["cvg"])
+    s.close()
