@@ -439,8 +439,12 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             const bool sb_in = (s >= 1 && s < ns);          // stream face s is interior
             const bool sp_in = (s - 1 >= 0 && s - 1 < ns);
             const bool spb_in = (s - 1 >= 1 && s - 1 < ns);
-            const float s_f = s_in ? 1.f : 0.f, sb_f = sb_in ? 1.f : 0.f;
-            const float sp_f = sp_in ? 1.f : 0.f, spb_f = spb_in ? 1.f : 0.f;
+            // Stream-face masks.  The fast path skips the plane masks of the
+            // row and column faces: outside the volume every state plane
+            // loads as zero and the border stream faces are stored as zero,
+            // so gk, b' and b'' of such planes come out zero anyway (EXACT
+            // keeps the reference's selects).
+            const float sb_f = sb_in ? 1.f : 0.f, spb_f = spb_in ? 1.f : 0.f;
 
             // ---- X: gk(s) from the old state
             const float *Sc = stages + st_cur * (SB / 4) + si;   // this column in stage s
@@ -513,14 +517,14 @@ __global__ void __launch_bounds__(32 * NW, MINB)
 #pragma unroll
             for (int j = 0; j < C; ++j)
                 brn[j] = keep_if<EXACT>(steps * (gk[j] - gk_up[j]) + by_own[j], fr_ok[j] && s_in,
-                                        fr_f[j] * s_f);
+                                        fr_f[j]);
             if constexpr (DIM == 3) {
                 float gk_left[C];
                 ld_cells<C>(GK + gi_left, gk_left);
 #pragma unroll
                 for (int j = 0; j < C; ++j)
                     bcn[j] = keep_if<EXACT>(steps * (gk[j] - gk_left[j]) + bx_own[j], fc_ok[j] && s_in,
-                                            fc_f[j] * s_f);
+                                            fc_f[j]);
                 st_cells<C>(BCp + gi, bcn);
             } else {
 #pragma unroll
@@ -572,9 +576,9 @@ __global__ void __launch_bounds__(32 * NW, MINB)
 #pragma unroll
                 for (int j = 0; j < C; ++j) {
                     brr[j] = keep_if<EXACT>(((g2[j] + g2_up[j]) * 0.5f) * br_prev[j], fr_ok[j] && sp_in,
-                                            fr_f[j] * sp_f);
+                                            fr_f[j]);
                     const float brr1 = keep_if<EXACT>(((g2_dn[j] + g2[j]) * 0.5f) * br_dn[j],
-                                                      fr1_ok[j] && sp_in, fr1_f[j] * sp_f);
+                                                      fr1_ok[j] && sp_in, fr1_f[j]);
                     dn[j] = brr1 - brr[j];
                     bcc[j] = 0.f;
                 }
@@ -585,9 +589,9 @@ __global__ void __launch_bounds__(32 * NW, MINB)
 #pragma unroll
                     for (int j = 0; j < C; ++j) {
                         bcc[j] = keep_if<EXACT>(((g2[j] + g2_l[j]) * 0.5f) * bc_prev[j], fc_ok[j] && sp_in,
-                                                fc_f[j] * sp_f);
+                                                fc_f[j]);
                         const float bcc1 = keep_if<EXACT>(((g2_r[j] + g2[j]) * 0.5f) * bc_rt[j],
-                                                          fc1_ok[j] && sp_in, fc1_f[j] * sp_f);
+                                                          fc1_ok[j] && sp_in, fc1_f[j]);
                         dn[j] = dn[j] + bcc1;
                         dn[j] = dn[j] - bcc[j];
                     }
