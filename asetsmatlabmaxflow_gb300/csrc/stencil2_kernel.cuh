@@ -360,7 +360,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         const int c = (DIM == 3) ? c0 - 2 + w : 0;
         const bool in_c = (c >= 0 && c < nc);
         bool inplane[C], is_tile[C], fr_ok[C], fr1_ok[C], fc_ok[C], fc1_ok[C];
-        float fr_f[C], fr1_f[C], fc_f[C], fc1_f[C], in_f[C];
+        float fr_f[C], fr1_f[C], fc_f[C], fc1_f[C];
 #pragma unroll
         for (int j = 0; j < C; ++j) {
             const int rj = r + j;
@@ -375,7 +375,6 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             fr1_f[j] = fr1_ok[j] ? 1.f : 0.f;
             fc_f[j] = fc_ok[j] ? 1.f : 0.f;
             fc1_f[j] = fc1_ok[j] ? 1.f : 0.f;
-            in_f[j] = inplane[j] ? 1.f : 0.f;
         }
         // element offsets fit 32 bits: solves are limited to 2^31 - 1 voxel-labels
         const unsigned int col_off = (unsigned int)(lab_off + (long long)c * P.pitch + r);
@@ -440,10 +439,11 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             const bool sp_in = (s - 1 >= 0 && s - 1 < ns);
             const bool spb_in = (s - 1 >= 1 && s - 1 < ns);
             // Stream-face masks.  The fast path skips the plane masks of the
-            // row and column faces: outside the volume every state plane
-            // loads as zero and the border stream faces are stored as zero,
-            // so gk, b' and b'' of such planes come out zero anyway (EXACT
-            // keeps the reference's selects).
+            // row and column faces and the in-volume factor of the stream
+            // faces: outside the volume every state element loads as zero
+            // and the border faces are stored as zero, so gk, b' and b'' of
+            // such cells and planes come out zero anyway (EXACT keeps the
+            // reference's selects).
             const float sb_f = sb_in ? 1.f : 0.f, spb_f = spb_in ? 1.f : 0.f;
 
             // ---- X: gk(s) from the old state
@@ -533,8 +533,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             }
 #pragma unroll
             for (int j = 0; j < C; ++j) {
-                bsn[j] = keep_if<EXACT>(steps * (gk[j] - gkprev[j]) + bs_own[j], inplane[j] && sb_in,
-                                        in_f[j] * sb_f);
+                bsn[j] = keep_if<EXACT>(steps * (gk[j] - gkprev[j]) + bs_own[j], inplane[j] && sb_in, sb_f);
                 gkprev[j] = gk[j];
             }
             rows_down<C>(br_prev, br_dn);   // b'_r(s-1) at r+1
@@ -554,7 +553,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
 #pragma unroll
                 for (int j = 0; j < C; ++j)
                     bssn[j] = keep_if<EXACT>(((g2[j] + g2prev[j]) * 0.5f) * bsprev[j],
-                                             inplane[j] && spb_in, in_f[j] * spb_f);
+                                             inplane[j] && spb_in, spb_f);
                 if (sp >= s_begin && sp < s_end)
                     st_cells_if<C>(d_bs + col_off + (unsigned int)sp * plane_stride, bssn, is_tile);
 #pragma unroll
