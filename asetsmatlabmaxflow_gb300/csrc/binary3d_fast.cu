@@ -8,8 +8,9 @@ namespace asets {
 
 static const StencilVariant kVariants[] = {
     // default: two rows per thread (60 x 16 tiles, 640 threads), the plane
-    // loop unrolled by the ring depth (stage slots become constants)
-    make_variant<3, 20, 4, EPI_BINARY, false, 1, 4, 2>(),
+    // loop unrolled by the ring depth (stage slots become constants), the
+    // refill issued in Z by the producer's halo-column warp
+    make_variant<3, 20, 4, EPI_BINARY, false, 1, 4, 2, true>(),
     make_variant<3, 16, 4, EPI_BINARY, false, 1, 4, 2>(),  // 60 x 12
     // one row per thread: 28 x 28 tiles, the fewest halo threads
     make_variant<3, 32, 4, EPI_BINARY, false, 1, 4>(),

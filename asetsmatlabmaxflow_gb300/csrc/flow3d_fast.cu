@@ -7,8 +7,9 @@ namespace asets {
 
 static const StencilVariant kVariants[] = {
     // default: the fewest halo threads; the plane loop unrolled by the ring
-    // depth (stage slots become constants)
-    make_variant<3, 32, 4, EPI_DIV, false, 1, 4>(),
+    // depth (stage slots become constants), the refill issued in Z by the
+    // producer's halo-column warp
+    make_variant<3, 32, 4, EPI_DIV, false, 1, 4, 1, true>(),
     make_variant<3, 16, 4, EPI_DIV, false>(),
     make_variant<3, 12, 4, EPI_DIV, false>(),
 };

@@ -200,7 +200,11 @@ __device__ __forceinline__ void finish_item(float erru, const ProblemDesc &P, in
     __syncthreads();
 }
 
-template <int DIM, int NW, int NSTAGE, int EPI, bool EXACT, int MINB, int UNROLL = 1, int CELLS = 1>
+// LATE: the producer issues the refill at the start of Z instead of right
+// after the X barrier.  In 3D its warp is a halo column, which has no
+// epilogue work in Z, so the issue leaves the Y barrier's critical path.
+template <int DIM, int NW, int NSTAGE, int EPI, bool EXACT, int MINB, int UNROLL = 1, int CELLS = 1,
+          bool LATE = false>
 __global__ void __launch_bounds__(32 * NW, MINB)
     stencil_col_kernel(const __grid_constant__ BatchArgs B)
 {
@@ -507,7 +511,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             }
 
             // refill a slot whose last readers finished before the barrier
-            if (producer && t + kLead < n_loads)
+            if (!LATE && producer && t + kLead < n_loads)
                 issue_load(t + kLead);
 
             // ---- Y: gradient step b'(s), projection g2(s-1), stream faces b''(s-1)
@@ -566,6 +570,9 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                 }
             }
             __syncthreads();
+
+            if (LATE && producer && t + kLead < n_loads)
+                issue_load(t + kLead);
 
             // ---- Z: row/column faces of plane s-1 and the output of plane s-2
             {

@@ -7,7 +7,7 @@
 namespace asets {
 
 template <int DIM, int NW, int NSTAGE, int EPI, bool EXACT, int MINB = (DIM == 3 ? 2 : 4),
-          int UNROLL = 1, int CELLS = 1>
+          int UNROLL = 1, int CELLS = 1, bool LATE = false>
 StencilVariant make_variant()
 {
     using G = ColGeom<DIM, NW, CELLS>;
@@ -23,7 +23,7 @@ StencilVariant make_variant()
     v.box_rows = G::LR;
     v.box_cols = G::LC;
     v.box_cols_bc = G::LC_BC;
-    v.fn = reinterpret_cast<const void *>(&stencil_col_kernel<DIM, NW, NSTAGE, EPI, EXACT, MINB, UNROLL, CELLS>);
+    v.fn = reinterpret_cast<const void *>(&stencil_col_kernel<DIM, NW, NSTAGE, EPI, EXACT, MINB, UNROLL, CELLS, LATE>);
     return v;
 }
 
