@@ -6,7 +6,7 @@
 namespace asets {
 
 static const StencilVariant kVariants[] = {
-    make_variant<2, 8, 4, EPI_BINARY, false, 4, 4>(),  // plane loop unrolled by the ring depth
+    make_variant<2, 8, 4, EPI_BINARY, false, 4, 4>(),  // plane loop unrolled by 4
     make_variant<2, 2, 4, EPI_BINARY, false>(),
 };
 

@@ -1,5 +1,5 @@
 // Compiled instances of the fused iteration kernel for the binary model (ps/pt/u
-// epilogue), 3D tiles 60 x 16 and 60 x 12 (two rows per thread), 28 x 28, 28 x 12, 28 x 8;
+// epilogue), 3D tiles 60 x 12 and 60 x 16 (two rows per thread), 28 x 28, 28 x 12, 28 x 8;
 // fast projection, built with FMA
 // contraction and flush to zero (held to the parity tolerance, not bit-exactness).
 #include "variants.cuh"
@@ -7,11 +7,11 @@
 namespace asets {
 
 static const StencilVariant kVariants[] = {
-    // default: two rows per thread (60 x 16 tiles, 640 threads), the plane
-    // loop unrolled by the ring depth (stage slots become constants), the
-    // refill issued in Z by the producer's halo-column warp
-    make_variant<3, 20, 4, EPI_BINARY, false, 1, 4, 2, true>(),
-    make_variant<3, 16, 4, EPI_BINARY, false, 1, 4, 2>(),  // 60 x 12
+    // default: two rows per thread (60 x 12 tiles, 512 threads), a ring of
+    // five stages, the plane loop unrolled by 4, the refill issued in Z by
+    // the producer's halo-column warp
+    make_variant<3, 16, 5, EPI_BINARY, false, 1, 4, 2, true>(),
+    make_variant<3, 20, 4, EPI_BINARY, false, 1, 4, 2, true>(),   // 60 x 16, four stages
     // one row per thread: 28 x 28 tiles, the fewest halo threads
     make_variant<3, 32, 4, EPI_BINARY, false, 1, 4>(),
     make_variant<3, 16, 4, EPI_BINARY, false>(),

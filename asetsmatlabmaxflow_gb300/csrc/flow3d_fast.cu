@@ -6,10 +6,10 @@
 namespace asets {
 
 static const StencilVariant kVariants[] = {
-    // default: the fewest halo threads; the plane loop unrolled by the ring
-    // depth (stage slots become constants), the refill issued in Z by the
-    // producer's halo-column warp
+    // default: the fewest halo threads; the plane loop unrolled by 4, the
+    // refill issued in Z by the producer's halo-column warp
     make_variant<3, 32, 4, EPI_DIV, false, 1, 4, 1, true>(),
+    make_variant<3, 16, 6, EPI_DIV, false, 1, 4, 1, true>(),  // 28 x 12, six stages (large volumes)
     make_variant<3, 16, 4, EPI_DIV, false>(),
     make_variant<3, 12, 4, EPI_DIV, false>(),
 };

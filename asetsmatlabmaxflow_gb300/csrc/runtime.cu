@@ -980,6 +980,58 @@ static asets_status finish_run(asets_solver *s, const IterControl &out, int *itN
     return ASETS_OK;
 }
 
+// ASETS_FLAG_AUTOTUNE for one solver: time every kernel variant of its kind
+// on one chunk of iterations of this problem (each from the same initial
+// state) and keep the fastest; the choice is cached per process by model,
+// size and exactness.
+static std::mutex g_solver_tune_mu;
+static std::vector<std::pair<std::string, int>> g_solver_tune;
+
+static asets_status solver_autotune(asets_solver *s, int flags, float cc, float steps,
+                                    int *tile_config)
+{
+    const int exact = (flags & ASETS_FLAG_EXACT) ? 1 : 0;
+    char key[128];
+    snprintf(key, sizeof key, "model%d/%dx%dx%d/L%d/exact%d", (int)s->model, s->ny, s->nx, s->nz,
+             s->nlab, exact);
+    {
+        std::lock_guard<std::mutex> lk(g_solver_tune_mu);
+        for (auto &kv : g_solver_tune)
+            if (kv.first == key) {
+                *tile_config = kv.second;
+                return ASETS_OK;
+            }
+    }
+    cudaStream_t st = s->ctx->stream;
+    int n = 0;
+    stencil_variants(s->dim, s->model == ASETS_BINARY ? EPI_BINARY : EPI_DIV, exact, &n);
+    int best = 1;
+    float best_ms = 1e30f;
+    for (int cand = 1; cand <= n; ++cand) {
+        asets_status ss = prepare_run(s, flags, cand, kGraphIters, 0.0f, cc, steps);
+        if (ss != ASETS_OK)
+            return ss;
+        ss = capture_chunk(s->graph, st, [&] { return launch_iteration(s); });
+        if (ss != ASETS_OK)
+            return ss;
+        CU_TRY(cudaEventRecord(s->ev0, st));
+        CU_TRY(cudaGraphLaunch(s->graph.exec, st));
+        CU_TRY(cudaEventRecord(s->ev1, st));
+        CU_TRY(cudaEventSynchronize(s->ev1));
+        float ms = 0.f;
+        CU_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = cand;
+        }
+    }
+    s->graph.reset();  // the run captures its own chunk
+    std::lock_guard<std::mutex> lk(g_solver_tune_mu);
+    g_solver_tune.emplace_back(key, best);
+    *tile_config = best;
+    return ASETS_OK;
+}
+
 extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_options *opt,
                                                    int maxIt, float errBound, float cc,
                                                    float steps, int *itNum)
@@ -994,7 +1046,13 @@ extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_
     std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
     DeviceGuard guard(s->ctx->device);
     cudaStream_t st = s->ctx->stream;
-    asets_status ss = prepare_run(s, flags, opt ? opt->tile_config : 0, maxIt, errBound, cc, steps);
+    int tile_config = opt ? opt->tile_config : 0;
+    if ((flags & ASETS_FLAG_AUTOTUNE) && tile_config == 0 && maxIt > 0) {
+        asets_status ts = solver_autotune(s, flags, cc, steps, &tile_config);
+        if (ts != ASETS_OK)
+            return ts;
+    }
+    asets_status ss = prepare_run(s, flags, tile_config, maxIt, errBound, cc, steps);
     if (ss != ASETS_OK)
         return ss;
     // the labelled models pass cc by value to the label kernel: recapture
@@ -1524,7 +1582,7 @@ static std::vector<std::pair<std::string, int>> g_tune_cache;
 static asets_status batch_autotune(asets_batch *b, int flags, float cc, float steps, int tile_config[4])
 {
     const int exact = (flags & ASETS_FLAG_EXACT) ? 1 : 0;
-    for (int gi = 0; gi < 2; ++gi) {  // the binary groups
+    for (int gi = 0; gi < 4; ++gi) {
         long long vox = 0;
         int count = 0;
         for (asets_solver *s : b->members)
@@ -1535,7 +1593,7 @@ static asets_status batch_autotune(asets_batch *b, int flags, float cc, float st
         if (!count)
             continue;
         char key[96];
-        snprintf(key, sizeof key, "dim%d/exact%d/n%d/logvox%d", gi + 2, exact, count,
+        snprintf(key, sizeof key, "group%d/exact%d/n%d/logvox%d", gi, exact, count,
                  (int)std::log2((double)std::max(vox, 1LL)));
         {
             std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -1549,7 +1607,7 @@ static asets_status batch_autotune(asets_batch *b, int flags, float cc, float st
                 continue;
         }
         int n = 0;
-        stencil_variants(gi == 1 ? 3 : 2, EPI_BINARY, (flags & ASETS_FLAG_EXACT) ? 1 : 0, &n);
+        stencil_variants((gi & 1) ? 3 : 2, gi >= 2 ? EPI_DIV : EPI_BINARY, exact, &n);
         int best = 1;
         float best_ms = 1e30f;
         for (int cand = 1; cand <= n; ++cand) {

@@ -312,8 +312,9 @@ class Solver:
         check(lib().asets_solver_set_initial(self._h, where, _ptr(u0), _ptr(ps0), _ptr(pt0)))
 
     def run(self, max_it: int, err_bound: float, cc: float, steps: float, *, exact: bool = False,
-            tile_config: int = 0, flags: int = 0) -> int:
-        opt = Options(flags=flags | (FLAG_EXACT if exact else 0), tile_config=tile_config)
+            tile_config: int = 0, flags: int = 0, autotune: bool = False) -> int:
+        flags |= (FLAG_EXACT if exact else 0) | (FLAG_AUTOTUNE if autotune else 0)
+        opt = Options(flags=flags, tile_config=tile_config)
         it = ctypes.c_int(0)
         check(lib().asets_solver_run(self._h, ctypes.byref(opt), max_it, err_bound, cc, steps,
                                      ctypes.byref(it)))

@@ -59,8 +59,11 @@ typedef struct asets_options {
 #define ASETS_FLAG_EXACT 0x1
 /* Skip the alpha(x) > 0 validation pass. */
 #define ASETS_FLAG_NO_ALPHA_CHECK 0x2
-/* Batches: time the tile configurations on the batch before solving and
- * use the fastest (the choice is cached per process). */
+/* Time the kernel variants (tile shapes, ring depths) on the problem -- one
+ * chunk of iterations each, from the same initial state -- before solving
+ * and use the fastest; the choice is cached per process (single solves by
+ * model, size and exactness; batches by group and problem mix).  Ignored
+ * when opt->tile_config selects a variant. */
 #define ASETS_FLAG_AUTOTUNE 0x4
 
 ASETS_API int asets_abi_version(void);

@@ -104,3 +104,37 @@ def test_border_faces_are_ignored():
     assert np.array_equal(bits(s.get_u()), bits(ref.get_u()))
     s.close()
     ref.close()
+
+
+@pytest.mark.parametrize("model,dims,L", [("binary", (70, 52, 33), 1), ("potts", (40, 44, 30), 4),
+                                          ("ishikawa", (130, 90), 5)])
+def test_autotuned_solve_equals_default(model, dims, L):
+    """ASETS_FLAG_AUTOTUNE on a single solve: the variants are timed from
+    the problem's initial state, then the solve runs with the fastest --
+    EXACT results bit-identical to the default variant's, fast results to
+    the parity tolerance; a second call reuses the cached choice."""
+    from asetsmatlabmaxflow_gb300 import native as N
+    from tests.gpu_helpers import bits
+
+    g = np.random.default_rng(3)
+    n = int(np.prod(dims))
+    ct = g.random(n * L).astype(np.float32)
+    la = 1 if model == "binary" else (L if model == "potts" else L - 1)
+    alpha = (0.1 + 0.3 * g.random(n * la)).astype(np.float32)
+    cs = g.random(n).astype(np.float32) if model == "binary" else None
+    steps = 0.11 if len(dims) == 3 else 0.16
+    s = N.Solver(N.Context.default(), model, dims, L)
+    s.set_inputs(ct, alpha, cs)
+    for exact in (True, False):
+        it0 = s.run(120, 1e-4, 0.3, steps, exact=exact)
+        u0 = s.get_u().copy()
+        for _ in range(2):
+            it1 = s.run(120, 1e-4, 0.3, steps, exact=exact, autotune=True)
+            u1 = s.get_u()
+            if exact:
+                assert it1 == it0
+                np.testing.assert_array_equal(bits(u1), bits(u0))
+            else:
+                assert abs(it1 - it0) <= 1
+                assert float(np.max(np.abs(u1 - u0))) <= 1e-3
+    s.close()
