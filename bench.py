@@ -476,7 +476,7 @@ def main():
                     "h2d_bytes_per_step": 3 * nvox * 4, "d2h_bytes_per_step": nvox * 4 + ITERS * 4},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "peak_kind": peak_kind, "kernel": "stencil_col_kernel<3, 20 warps, 2 rows per thread (60x16 tile), 4 stages, refill in Z, binary, fast>",
+                         "peak_kind": peak_kind, "kernel": "stencil_col_kernel<3, 16 warps, 2 rows per thread (60x12 tile), 5 stages, refill in Z, binary, fast>",
                          "bytes_per_voxel_iter": BYTES_PER_VOXEL_ITER,
                          "launch_ms": per_launch_ms},
             "time_to_errbound": {"err_bound": 1e-4, "iterations": conv_it, "ms": conv_ms,
