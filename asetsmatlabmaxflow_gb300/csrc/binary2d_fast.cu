@@ -1,13 +1,18 @@
 // Compiled instances of the fused iteration kernel for the binary model (ps/pt/u
-// epilogue), 2D tiles 224-row, 56-row; fast projection, built with FMA contraction and
-// flush to zero (held to the parity tolerance, not bit-exactness).
+// epilogue), 2D tiles 240-row (two rows per thread), 224-row, 56-row; fast
+// projection, built with FMA contraction and flush to zero (held to the parity
+// tolerance, not bit-exactness).
 #include "variants.cuh"
 
 namespace asets {
 
 static const StencilVariant kVariants[] = {
-    make_variant<2, 8, 4, EPI_BINARY, false, 4, 4>(),  // plane loop unrolled by 4
-    make_variant<2, 2, 4, EPI_BINARY, false>(),
+    // default: two rows per thread, 240-row tiles, 6 stages, the plane loop
+    // unrolled by 4
+    make_variant<2, 4, 6, EPI_BINARY, false, 4, 4, 2>(),
+    make_variant<2, 8, 4, EPI_BINARY, false, 4, 4>(),       // 224-row tiles
+    make_variant<2, 2, 4, EPI_BINARY, false>(),             // 56-row tiles (short columns)
+    make_variant<2, 4, 4, EPI_BINARY, false, 4, 4, 2>(),
 };
 
 const StencilVariant *binary2d_fast_variants(int *count)

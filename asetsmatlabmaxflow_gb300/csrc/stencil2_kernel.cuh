@@ -10,8 +10,8 @@
 // stream axis s (z in 3D, x in 2D).  Each warp owns 32*CELLS consecutive
 // rows: 32*CELLS - 4 tile rows plus two halo rows on each side.  In 3D warp
 // w is column c0 - 2 + w of a (32*CELLS - 4) x (NW-4) tile; in 2D the NW
-// warps are consecutive 28-row sub-tiles.  Every thread owns CELLS adjacent
-// rows of one column (CELLS = 1, or 2 in 3D) for the whole sweep along s, so
+// warps are consecutive (32*CELLS - 4)-row sub-tiles.  Every thread owns
+// CELLS adjacent rows (1 or 2) of one column for the whole sweep along s, so
 // its indices, border flags and carried values stay in registers; row
 // neighbours come from the thread itself or, for its first and last cell,
 // through one warp shuffle, column neighbours through three small shared
@@ -49,7 +49,7 @@ namespace asets {
 template <int DIM, int NW, int CELLS = 1>
 struct ColGeom {
     static_assert(DIM == 2 || DIM == 3, "2D or 3D");
-    static_assert(CELLS == 1 || (CELLS == 2 && DIM == 3), "two cells per thread in 3D only");
+    static_assert(CELLS == 1 || CELLS == 2, "one or two cells per thread");
     static constexpr int NT = 32 * NW;
     static constexpr int TRW = 32 * CELLS - 4;                // tile rows per warp
     static constexpr int TR = (DIM == 3) ? TRW : TRW * NW;    // tile rows
@@ -270,12 +270,12 @@ __global__ void __launch_bounds__(32 * NW, MINB)
 
     // per-thread constants; the thread's cells are rows rho .. rho+C-1 of
     // its warp's 32*C rows (two halo rows on each side)
-    const int rho = (DIM == 3) ? C * lane : G::TRW * w + lane;       // first cell's row index
+    const int rho = (DIM == 3) ? C * lane : G::TRW * w + C * lane;   // first cell's row index
     const int si = rho + 2 + ((DIM == 3) ? w * G::LR : 0);            // halo box index
     const int gi = (lane + 32 * w) * C;                               // shared plane index (3D)
     const int gi_left = (w >= 1) ? gi - 32 * C : gi;                  // column c-1 (clamped)
     const int gi_right = (w + 1 < NW) ? gi + 32 * C : gi;             // column c+1 (clamped)
-    const int lane_row = (DIM == 3) ? C * lane : lane;                // row within the warp
+    const int lane_row = C * lane;                                    // row within the warp
     const bool tile_row = (lane_row >= 2 && lane_row < 32 * C - 2);
     const bool tile_col = (DIM == 3) ? (w >= 2 && w < G::TC + 2) : true;
     const int ti = (DIM == 3) ? (lane_row - 2) + (w - 2) * G::TRW : (rho - 2);

@@ -251,3 +251,25 @@ def test_odd_shapes_binary3d_against_oracle(dims):
     assert_north_star("binary", dims, 1, s.get_u().reshape(dims, order="F"),
                       ref["u"].reshape(dims, order="F"), s.get_cvg(), refd["cvg"])
     s.close()
+
+
+@pytest.mark.parametrize("tile_config", [1, 2, 3, 4])
+def test_every_binary2d_fast_variant_meets_parity_bar(tile_config):
+    """Each compiled variant of the fast binary 2D kernel (224- and 56-row
+    tiles, two rows per thread with 240-row tiles and four or six stages),
+    selected explicitly, against the oracle, on a column length that is not
+    a multiple of any tile and is odd."""
+    from asetsmatlabmaxflow_gb300 import native as N
+
+    model, dims, L, maxit, cc, steps = "binary", (301, 170), 1, 60, 0.3, 0.16
+    inp = _rand(model, dims, L, 13)
+    ref = O.solve(model, dims, inp["Ct"], inp["alpha"], cs=inp["Cs"], nlab=L, max_it=maxit,
+                  err_bound=0.0, cc=cc, steps=steps)
+    refd = O.solve(model, dims, inp["Ct"], inp["alpha"], cs=inp["Cs"], nlab=L, max_it=maxit,
+                   err_bound=0.0, cc=cc, steps=steps, erru_double=True)
+    s = N.Solver(N.Context.default(), model, dims, L)
+    s.set_inputs(inp["Ct"], inp["alpha"], inp["Cs"])
+    s.run(maxit, 0.0, cc, steps, exact=False, tile_config=tile_config)
+    assert_north_star(model, dims, L, s.get_u().reshape(dims, order="F"),
+                      ref["u"].reshape(dims, order="F"), s.get_cvg(), refd["cvg"])
+    s.close()
