@@ -343,8 +343,10 @@ class Solver:
         return ps, pt
 
     def run_multilevel(self, levels: int, max_it: int, err_bound: float, cc: float, steps: float,
-                       *, exact: bool = False, tile_config: int = 0, flags: int = 0) -> int:
-        opt = Options(flags=flags | (FLAG_EXACT if exact else 0), tile_config=tile_config)
+                       *, exact: bool = False, tile_config: int = 0, flags: int = 0,
+                       autotune: bool = False) -> int:
+        flags |= (FLAG_EXACT if exact else 0) | (FLAG_AUTOTUNE if autotune else 0)
+        opt = Options(flags=flags, tile_config=tile_config)
         it = ctypes.c_int(0)
         check(lib().asets_solver_run_multilevel(self._h, ctypes.byref(opt), levels, max_it,
                                                 err_bound, cc, steps, ctypes.byref(it)))
@@ -443,11 +445,12 @@ class Batch:
         return list(its[:len(self.members)])
 
     def run_multilevel(self, levels: int, max_it: int, err_bound: float, cc: float, steps: float,
-                       *, exact: bool = False) -> list[int]:
+                       *, exact: bool = False, autotune: bool = False) -> list[int]:
         """Coarse-to-fine solve of every member (asets_batch_run_multilevel);
         full-resolution itNum per member, per-level ones in each member's
         multilevel_stats()."""
-        opt = Options(flags=FLAG_EXACT if exact else 0, tile_config=0)
+        opt = Options(flags=(FLAG_EXACT if exact else 0) | (FLAG_AUTOTUNE if autotune else 0),
+                      tile_config=0)
         its = (ctypes.c_int * max(len(self.members), 1))()
         check(lib().asets_batch_run_multilevel(self._h, ctypes.byref(opt), levels, max_it,
                                                err_bound, cc, steps, ctypes.addressof(its)))

@@ -47,6 +47,9 @@ CC, STEPS = 0.3, 0.11
 TRAIN_ERR = 1e-5
 EVAL_ERR = 1e-4
 MAX_IT = 20000
+# every solve times the kernel variants for its size once (cached per
+# process) and runs the fastest: the coarse levels gain from narrower tiles
+AUTOTUNE = True
 HELDOUT_SEED0 = 1_000_000  # held-out seeds start here; training seeds below it
 
 
@@ -146,18 +149,18 @@ class Runner:
 
     def cold(self, err: float, max_it: int = MAX_IT) -> int:
         self.lv[0].set_initial(None)
-        return self.s.run(max_it, err, CC, STEPS)
+        return self.s.run(max_it, err, CC, STEPS, autotune=AUTOTUNE)
 
     def warm(self, state, err: float, max_it: int) -> int:
         """Full-resolution solve from `state`."""
         self.lv[0].set_initial(state)
-        return self.s.run(max_it, err, CC, STEPS)
+        return self.s.run(max_it, err, CC, STEPS, autotune=AUTOTUNE)
 
     def multilevel(self, err: float, max_it: int = MAX_IT, top_state=None):
         """Coarse-to-fine solve; the coarsest level starts from `top_state`
         (or cold).  Returns (full-resolution itNum, per-level itNum)."""
         self.top.set_initial(top_state)
-        it = self.s.run_multilevel(len(self.lv), max_it, err, CC, STEPS)
+        it = self.s.run_multilevel(len(self.lv), max_it, err, CC, STEPS, autotune=AUTOTUNE)
         return it, self.s.multilevel_stats()[0]
 
     def close(self):
@@ -337,7 +340,7 @@ def evaluate_batched(net: N.WarmStartNet, cold_budget: int, seeds, *, level: int
     for run in runs:
         run.lv[0].set_initial(None)
         cold.add(run.s)
-    cold_its, cold_ms = _sync_ms(lambda: cold.run(MAX_IT, EVAL_ERR, CC, STEPS))
+    cold_its, cold_ms = _sync_ms(lambda: cold.run(MAX_IT, EVAL_ERR, CC, STEPS, autotune=AUTOTUNE))
     lab_c = [labels(run.lv[0].read_state()[0], run.n).clone() for run in runs]
     cold.close()
 
@@ -350,14 +353,15 @@ def evaluate_batched(net: N.WarmStartNet, cold_budget: int, seeds, *, level: int
             lv = run.lv[level]
             net.predict(lv.shape, lv.ct, lv.alpha, *lv.state)
             lv.set_initial(lv.state)
-        its = warm.run_multilevel(len(runs[0].lv), MAX_IT, EVAL_ERR, CC, STEPS)
+        its = warm.run_multilevel(len(runs[0].lv), MAX_IT, EVAL_ERR, CC, STEPS,
+                                  autotune=AUTOTUNE)
         fb = [i for i, it in enumerate(its) if it >= cold_budget]
         if fb:
             again = N.Batch(ctx)
             for i in fb:
                 runs[i].lv[0].set_initial(None)
                 again.add(runs[i].s)
-            again.run(MAX_IT, EVAL_ERR, CC, STEPS)
+            again.run(MAX_IT, EVAL_ERR, CC, STEPS, autotune=AUTOTUNE)
             again.close()
         return its, fb
 
