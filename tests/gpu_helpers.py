@@ -29,7 +29,7 @@ def labels_of(model: str, u: np.ndarray, dims, nlab: int) -> np.ndarray:
     return (u.reshape(n, nlab - 1, order="F") > 0.5).sum(axis=1)
 
 
-def assert_north_star(model, dims, nlab, u_gpu, u_ref, cvg_gpu, cvg_ref, *, it=None):
+def assert_parity_bar(model, dims, nlab, u_gpu, u_ref, cvg_gpu, cvg_ref, *, it=None):
     """max|u_gpu - u_ref| <= 1e-3, >= 99.99% label agreement, erriter
     within 1e-3 relative (the parity bar of the port)."""
     du = float(np.max(np.abs(u_gpu.ravel(order="F") - u_ref.ravel(order="F")))) if u_gpu.size else 0.0

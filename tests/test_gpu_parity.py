@@ -6,7 +6,7 @@ import pytest
 
 from oracle import oracle as O
 from tests import golden_cases as G
-from tests.gpu_helpers import assert_north_star, bits, require_gpu
+from tests.gpu_helpers import assert_parity_bar, bits, require_gpu
 
 pytestmark = pytest.mark.gpu
 
@@ -46,7 +46,7 @@ def test_fast_mode_meets_parity_bar(name):
     u, cvg, it, _ = _run_golden(case, exact=False)
     assert int(it.ravel()[0]) == case["it"]
     n = min(case["it"] + 1, case["max_it"])
-    assert_north_star(case["model"], case["dims"], case["nlab"], u, case["u"], cvg, case["cvg"], it=n)
+    assert_parity_bar(case["model"], case["dims"], case["nlab"], u, case["u"], cvg, case["cvg"], it=n)
 
 
 @pytest.mark.parametrize("name", ["binary2d_reftest", "binary3d_odd", "potts2d_odd",
@@ -61,7 +61,7 @@ def test_dropin_mex_file_matches_reference(name):
     assert u.shape == case["u"].shape and cvg.shape == (case["max_it"], 1)
     assert it.dtype == np.uint16 and timet.dtype == np.float32 and timet.ravel()[0] > 0
     n = min(case["it"] + 1, case["max_it"])
-    assert_north_star(case["model"], case["dims"], case["nlab"], u, case["u"], cvg, case["cvg"], it=n)
+    assert_parity_bar(case["model"], case["dims"], case["nlab"], u, case["u"], cvg, case["cvg"], it=n)
     assert "number of iterations" in MexFunction.last_print()
 
 
@@ -131,7 +131,7 @@ def test_against_oracle_at_larger_sizes(model, dims, L, maxit, cc, steps):
     it = s.run(maxit, 0.0, cc, steps, exact=False)
     u = s.get_u()
     shape = dims + ((L,) if model == "potts" else ((L - 1,) if model == "ishikawa" else ()))
-    assert_north_star(model, dims, L, u.reshape(shape, order="F"),
+    assert_parity_bar(model, dims, L, u.reshape(shape, order="F"),
                       ref["u"].reshape(shape, order="F"), s.get_cvg(), refd["cvg"])
     s.close()
 
@@ -224,7 +224,7 @@ def test_every_binary3d_fast_variant_meets_parity_bar(tile_config):
     s = N.Solver(N.Context.default(), model, dims, L)
     s.set_inputs(inp["Ct"], inp["alpha"], inp["Cs"])
     s.run(maxit, 0.0, cc, steps, exact=False, tile_config=tile_config)
-    assert_north_star(model, dims, L, s.get_u().reshape(dims, order="F"),
+    assert_parity_bar(model, dims, L, s.get_u().reshape(dims, order="F"),
                       ref["u"].reshape(dims, order="F"), s.get_cvg(), refd["cvg"])
     s.close()
 
@@ -248,7 +248,7 @@ def test_odd_shapes_binary3d_against_oracle(dims):
     assert s.run(maxit, 0.0, cc, steps, exact=True) == ref["it"]
     np.testing.assert_array_equal(bits(s.get_u()), bits(ref["u"]))
     s.run(maxit, 0.0, cc, steps, exact=False)
-    assert_north_star("binary", dims, 1, s.get_u().reshape(dims, order="F"),
+    assert_parity_bar("binary", dims, 1, s.get_u().reshape(dims, order="F"),
                       ref["u"].reshape(dims, order="F"), s.get_cvg(), refd["cvg"])
     s.close()
 
@@ -270,6 +270,6 @@ def test_every_binary2d_fast_variant_meets_parity_bar(tile_config):
     s = N.Solver(N.Context.default(), model, dims, L)
     s.set_inputs(inp["Ct"], inp["alpha"], inp["Cs"])
     s.run(maxit, 0.0, cc, steps, exact=False, tile_config=tile_config)
-    assert_north_star(model, dims, L, s.get_u().reshape(dims, order="F"),
+    assert_parity_bar(model, dims, L, s.get_u().reshape(dims, order="F"),
                       ref["u"].reshape(dims, order="F"), s.get_cvg(), refd["cvg"])
     s.close()
