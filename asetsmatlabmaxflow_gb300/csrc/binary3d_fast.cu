@@ -8,9 +8,9 @@ namespace asets {
 
 static const StencilVariant kVariants[] = {
     // default: two rows per thread (60 x 12 tiles, 512 threads), a ring of
-    // five stages, the plane loop unrolled by 4, the refill issued in Z by
+    // five stages, the plane loop unrolled by 8, the refill issued in Z by
     // the producer's halo-column warp
-    make_variant<3, 16, 5, EPI_BINARY, false, 1, 4, 2, true>(),
+    make_variant<3, 16, 5, EPI_BINARY, false, 1, 8, 2, true>(),
     make_variant<3, 20, 4, EPI_BINARY, false, 1, 4, 2, true>(),   // 60 x 16, four stages
     // one row per thread: 28 x 28 tiles, the fewest halo threads
     make_variant<3, 32, 4, EPI_BINARY, false, 1, 4>(),
