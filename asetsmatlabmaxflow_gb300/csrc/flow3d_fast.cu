@@ -12,6 +12,8 @@ static const StencilVariant kVariants[] = {
     make_variant<3, 16, 6, EPI_DIV, false, 1, 4, 1, true>(),  // 28 x 12, six stages (large volumes)
     make_variant<3, 16, 4, EPI_DIV, false>(),
     make_variant<3, 12, 4, EPI_DIV, false>(),
+    make_variant<3, 12, 8, EPI_DIV, false, 2, 4, 1, true>(),   // 28 x 8, eight stages (small volumes)
+    make_variant<3, 16, 8, EPI_DIV, false, 1, 4, 1, true>(),   // 28 x 12, eight stages
 };
 
 const StencilVariant *flow3d_fast_variants(int *count)
