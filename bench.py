@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solver measurement")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the binary 2D / Potts 3D / Ishikawa 2D workloads")
     ap.add_argument("--warm-seeds", type=int, default=4,
                     help="held-out Potts problems for the warm-start comparison (0: skip)")
     ap.add_argument("--profile-iters", type=int, default=0,
@@ -271,6 +273,53 @@ def batch_run(ctx) -> dict:
     return out
 
 
+def configs_run(ctx) -> list:
+    """The other workloads of the metric, each on its own solver: binary 2D
+    256^2 (pars [256,256,300,1e-4,0.3,0.16]), Potts 3D 192^3 L=4 and
+    Ishikawa 2D 1024^2 L=8 (cc 0.3, steps 0.11 / 0.16).  Per workload: 100
+    fixed iterations (errBound 0) give the device time per iteration (both
+    passes of a labelled iteration) and its algorithmic-byte roofline, then
+    one solve to errBound 1e-4.  Variants autotuned (ASETS_FLAG_AUTOTUNE)."""
+    from asetsmatlabmaxflow_gb300 import native as N
+    from asetsmatlabmaxflow_gb300 import synth
+
+    peak, peak_kind = peaks()
+    rows = []
+    cs2, ct2, a2 = synth.binary2d(seed=0)
+    ct3, a3 = synth.potts3d(seed=0)
+    cti, ai = synth.ishikawa2d(seed=0)
+    # name, model, dims, labels, inputs, steps, maxIt, bytes per voxel-iteration
+    table = (
+        ("binary2d_256^2", "binary", cs2.shape, 1, (ct2, a2, cs2), 0.16, 300, 52),
+        ("potts3d_192^3_L4", "potts", ct3.shape[:3], ct3.shape[3], (ct3, a3), 0.11, 2000,
+         48 * ct3.shape[3] + 8),
+        ("ishikawa2d_1024^2_L8", "ishikawa", cti.shape[:2], cti.shape[2], (cti, ai), 0.16, 2000,
+         (4 * cti.shape[2] - 3) * 8 + (2 * cti.shape[2] - 1) * 4),
+    )
+    fixed = 100
+    for name, model, dims, L, inputs, steps_, max_it, bpv in table:
+        s = N.Solver(ctx, model, dims, L) if model != "binary" else N.Solver(ctx, model, dims)
+        s.set_inputs(*inputs)
+        nvox = int(np.prod(dims))
+        s.run(fixed, 0.0, 0.3, steps_, autotune=True)  # tune + warm-up
+        s.run(fixed, 0.0, 0.3, steps_, autotune=True)
+        ms, _ = s.last_run_stats()
+        it_ms = ms / fixed
+        achieved = bpv * nvox / (it_ms * 1e-3) / 1e9
+        it = s.run(max_it, 1e-4, 0.3, steps_, autotune=True)
+        conv_ms, _ = s.last_run_stats()
+        rows.append({"workload": name, "voxels": nvox, "labels": L,
+                     "gvoxel_iter_per_s": nvox / (it_ms * 1e-3) / 1e9,
+                     "ms_per_iteration": it_ms, "bytes_per_voxel_iter": bpv,
+                     "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                                  "unit": "GB/s", "frac": achieved / peak,
+                                  "peak_kind": peak_kind},
+                     "err_bound": 1e-4, "max_it": max_it, "itnum": it,
+                     "ms_to_errbound": conv_ms})
+        s.close()
+    return rows
+
+
 def warm_start_run(ctx, nseeds: int) -> dict:
     """Potts 3D 128^3, L = 6, errBound 1e-4 on held-out seeds: cold start vs
     the multilevel solve vs the multilevel solve whose coarsest level starts
@@ -455,6 +504,7 @@ def main():
     ok = bool(np.isfinite(h_u.numpy()).all())
 
     batch = None if args.no_batch else batch_run(ctx)
+    configs = configs_run(ctx) if (rank == 0 and not args.no_configs) else None
     warm = warm_start_run(ctx, args.warm_seeds) if (rank == 0 and args.warm_seeds > 0) else None
 
     cpu = None
@@ -488,6 +538,7 @@ def main():
             "clocks": clk.summary(),
             "gpu_launches": launches,
             "batch": batch,
+            "configs": configs,
             "finite": ok,
         }
         if cpu is not None:
