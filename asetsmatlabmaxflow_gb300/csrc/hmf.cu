@@ -97,14 +97,24 @@ template <class T>
 struct Pix {
     int y, x, z;
     long long c;
+    // 32-bit unsigned arithmetic: every index of a solve (pixels times
+    // nodes) is below 2^31 (entry check)
     __device__ Pix(const HArgs<T> &A, long long c_) : c(c_)
     {
-        y = (int)(c % A.d1);
-        const long long q = c / A.d1;
-        x = (int)(q % A.d2);
-        z = (int)(q / A.d2);
+        const unsigned int cc_ = (unsigned int)c_;
+        const unsigned int q = cc_ / (unsigned int)A.d1;
+        y = (int)(cc_ - q * (unsigned int)A.d1);
+        const unsigned int z_ = q / (unsigned int)A.d2;
+        x = (int)(q - z_ * (unsigned int)A.d2);
+        z = (int)z_;
     }
 };
+
+// node offset of the element t of a node-major loop over n pixels per node
+__device__ __forceinline__ int node_of(long long t, long long n)
+{
+    return (int)((unsigned int)t / (unsigned int)n);
+}
 template <class T>
 __device__ __forceinline__ long long i1(const HArgs<T> &A, int y, int x, int z)
 {
@@ -169,7 +179,7 @@ __global__ void k2_gradient(const HArgs<T> A)
 {
     H_LOOP(A.n * (A.m - 1))
     {
-        const int i = 1 + (int)(t / A.n);
+        const int i = 1 + node_of(t, A.n);
         const Pix<T> p(A, t - (long long)(i - 1) * A.n);
         const T *g = A.g + (long long)i * A.n;
         const T gc = g[p.c];
@@ -195,7 +205,7 @@ __global__ void k3_projection(const HArgs<T> A)
 {
     H_LOOP(A.n * (A.m - 1))
     {
-        const int i = 1 + (int)(t / A.n);
+        const int i = 1 + node_of(t, A.n);
         const Pix<T> p(A, t - (long long)(i - 1) * A.n);
         const T *f1 = A.p1 + (long long)i * A.f1;
         const T *f2 = A.p2 + (long long)i * A.f2;
@@ -240,7 +250,7 @@ __global__ void k4_rescale(const HArgs<T> A)
 {
     H_LOOP(A.n * (A.m - 1))
     {
-        const int i = 1 + (int)(t / A.n);
+        const int i = 1 + node_of(t, A.n);
         const Pix<T> p(A, t - (long long)(i - 1) * A.n);
         const T *g = A.g + (long long)i * A.n;
         const T gc = g[p.c];
@@ -267,7 +277,7 @@ __global__ void k5_divergence(const HArgs<T> A)
 {
     H_LOOP(A.n * (A.m - 1))
     {
-        const int i = 1 + (int)(t / A.n);
+        const int i = 1 + node_of(t, A.n);
         const Pix<T> p(A, t - (long long)(i - 1) * A.n);
         const T *f1 = A.p1 + (long long)i * A.f1;
         const T *f2 = A.p2 + (long long)i * A.f2;
@@ -298,7 +308,7 @@ __global__ void k_norm_dirs(const HArgs<T> A)
 {
     H_LOOP(A.n * A.m)
     {
-        const int i = (int)(t / A.n);
+        const int i = node_of(t, A.n);
         const long long c = t - (long long)i * A.n;
         const NodeDev<T> &nd = A.nodes[i];
         T *const *l = nd.l;
@@ -334,7 +344,7 @@ __global__ void k_exempt_a(const HArgs<T> A)
 {
     H_LOOP(A.n * (A.m - 1))
     {
-        const int i = 1 + (int)(t / A.n);
+        const int i = 1 + node_of(t, A.n);
         T *const *l = A.nodes[i].l;
         if (!l[0])
             continue;
@@ -381,7 +391,7 @@ __global__ void k_exempt_e(const HArgs<T> A)
 {
     H_LOOP(A.n * (A.m - 1))
     {
-        const int i = 1 + (int)(t / A.n);
+        const int i = 1 + node_of(t, A.n);
         T *const *l = A.nodes[i].l;
         if (!l[0])
             continue;
@@ -489,7 +499,7 @@ __global__ void k_costs(const HArgs<T> A)
 {
     H_LOOP(A.n * A.m)
     {
-        const int i = (int)(t / A.n);
+        const int i = node_of(t, A.n);
         const long long c = t - (long long)i * A.n;
         const NodeDev<T> &nd = A.nodes[i];
         const double u = (double)A.u[t];
@@ -539,7 +549,7 @@ __global__ void k_dag_g(const HArgs<T> A)
 {
     H_LOOP(A.n * (A.m - 1))
     {
-        const int i = 1 + (int)(t / A.n);
+        const int i = 1 + node_of(t, A.n);
         const long long c = t - (long long)(i - 1) * A.n;
         const long long o = (long long)i * A.n + c;
         const T in = dag_in(A, A.nodes[i], i, c);
@@ -1065,6 +1075,10 @@ extern "C" ASETS_API asets_status asets_dag_run(
         set_last_error("asets_dag_full_flow: bad arguments");
         return ASETS_ERR_INVALID_ARG;
     }
+    if ((long long)D1 * D2 * D3 * num_nodes >= (1LL << 31)) {
+        set_last_error("asets_dag_full_flow: pixels x nodes must stay below 2^31");
+        return ASETS_ERR_INVALID_ARG;
+    }
     const int m = num_nodes;
     std::vector<int> nchild(nchild_in, nchild_in + m), begin(m, 0), nparent(m, 0), parent0(m, -1);
     int total = 0;
@@ -1167,6 +1181,10 @@ extern "C" ASETS_API asets_status asets_hmf_run(
         D1 < 1 || D2 < 1 || D3 < 1 || (dim == 2 && D3 != 1) || num_nodes < 1 || numIts < 0 ||
         (algorithm != ASETS_HMF_FULL_FLOW && algorithm != ASETS_HMF_PSEUDO_FLOW)) {
         set_last_error("asets_hmf_full_flow: bad arguments");
+        return ASETS_ERR_INVALID_ARG;
+    }
+    if ((long long)D1 * D2 * D3 * num_nodes >= (1LL << 31)) {
+        set_last_error("asets_hmf_full_flow: pixels x nodes must stay below 2^31");
         return ASETS_ERR_INVALID_ARG;
     }
     if (parent[0] != -1) {

@@ -122,6 +122,8 @@ EncodeTiledFn context_encoder(asets_context *ctx);
 int context_num_sms(asets_context *ctx);
 int context_device(asets_context *ctx);
 cudaStream_t context_stream(asets_context *ctx);
+// Memory pool of the context's short-lived scratch (nullptr if it cannot be made).
+cudaMemPool_t context_pool(asets_context *ctx);
 
 // ---------------------------------------------------------------- warm-start net
 // One 3x3x3 convolution, 16 -> 16 channels (conv_tc.cu).

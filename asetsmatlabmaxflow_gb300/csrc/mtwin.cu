@@ -74,18 +74,29 @@ __device__ __forceinline__ T mn(T a, T b)
     return (a <= b || a != a) ? a : b;
 }
 
+// Cell coordinates in 32-bit unsigned arithmetic: every index of a solve
+// (cells and faces times labels) is below 2^31 (entry check), and a 64-bit
+// division costs several times a 32-bit one.
 template <class T>
 struct Cell {
     int y, x, z;
     long long g;
     __device__ Cell(const MTArgs<T> &A, long long g_) : g(g_)
     {
-        y = (int)(g % A.rows);
-        const long long q = g / A.rows;
-        x = (int)(q % A.cols);
-        z = (int)(q / A.cols);
+        const unsigned int gg = (unsigned int)g_;
+        const unsigned int q = gg / (unsigned int)A.rows;
+        y = (int)(gg - q * (unsigned int)A.rows);
+        const unsigned int z_ = q / (unsigned int)A.cols;
+        x = (int)(q - z_ * (unsigned int)A.cols);
+        z = (int)z_;
     }
 };
+
+// label of the element t of a label-major loop over n cells per label
+__device__ __forceinline__ int label_of(long long t, long long n)
+{
+    return (int)((unsigned int)t / (unsigned int)n);
+}
 // face arrays: p1 rows x (cols+1) x slices (along columns), p2 (rows+1) x
 // cols x slices (along rows), p3 rows x cols x (slices+1) (along slices)
 template <class T>
@@ -140,7 +151,7 @@ __global__ void mt_step(const MTArgs<T> A)
         return;
     MT_LOOP(A.n * A.nflow)
     {
-        const int k = (int)(t / A.n);
+        const int k = label_of(t, A.n);
         const Cell<T> c(A, t - (long long)k * A.n);
         const T u0 = ud<T, M>(A, k, c.g);
         // binary: pp + steps*(d); Potts/Ishikawa: steps*(d) + pp
@@ -165,7 +176,7 @@ __global__ void mt_gk(const MTArgs<T> A)
         return;
     MT_LOOP(A.n * A.nflow)
     {
-        const int k = (int)(t / A.n);
+        const int k = label_of(t, A.n);
         const Cell<T> c(A, t - (long long)k * A.n);
         const T *f1 = A.p1 + (long long)k * A.f1, *f2 = A.p2 + (long long)k * A.f2;
         const T a = f1[j1(A, c.y, c.x, c.z)], b = f1[j1(A, c.y, c.x + 1, c.z)];
@@ -193,7 +204,7 @@ __global__ void mt_rescale(const MTArgs<T> A)
         return;
     MT_LOOP(A.n * A.nflow)
     {
-        const int k = (int)(t / A.n);
+        const int k = label_of(t, A.n);
         const Cell<T> c(A, t - (long long)k * A.n);
         const T g0 = A.gk[t];
         auto sc = [&](T *f, T gnb) { *f = mul(mul(A.half, add(g0, gnb)), *f); };
@@ -524,6 +535,10 @@ extern "C" ASETS_API asets_status asets_matlab_solve(
         (model == MT_BINARY && !Cs) || (model == MT_POTTS && nlab < 1) ||
         (model == MT_ISHIKAWA && nlab < 2) || model < 0 || model > 2) {
         set_last_error("asets_matlab_solve: bad arguments");
+        return ASETS_ERR_INVALID_ARG;
+    }
+    if ((long long)(rows + 1) * (cols + 1) * (slices + 1) * (nlab > 1 ? nlab : 1) >= (1LL << 31)) {
+        set_last_error("asets_matlab_solve: volume x labels must stay below 2^31 elements");
         return ASETS_ERR_INVALID_ARG;
     }
     const auto t0 = std::chrono::steady_clock::now();

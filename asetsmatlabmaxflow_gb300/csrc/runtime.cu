@@ -82,6 +82,7 @@ struct asets_context {
     std::recursive_mutex mu;
     asets_solver *cached = nullptr;  // solver reused by the one-shot calls
     int *pinned_flags = nullptr;     // host-visible done flags of in-flight chunks
+    cudaMemPool_t pool = nullptr;    // scratch of the cost-term calls (keeps small blocks mapped)
 };
 
 struct ChunkGraph {
@@ -167,6 +168,27 @@ EncodeTiledFn context_encoder(asets_context *ctx) { return ctx->encode; }
 int context_num_sms(asets_context *ctx) { return ctx->num_sms; }
 int context_device(asets_context *ctx) { return ctx->device; }
 cudaStream_t context_stream(asets_context *ctx) { return ctx->stream; }
+
+cudaMemPool_t context_pool(asets_context *ctx)
+{
+    std::lock_guard<std::recursive_mutex> lock(ctx->mu);
+    if (!ctx->pool) {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = ctx->device;
+        if (cudaMemPoolCreate(&ctx->pool, &props) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->pool = nullptr;
+            return nullptr;
+        }
+        // blocks up to this size stay mapped between calls; larger frees
+        // go back to the device at the next synchronisation
+        cuuint64_t keep = 64ull << 20;
+        cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    return ctx->pool;
+}
 }  // namespace asets
 
 extern "C" ASETS_API int asets_abi_version(void) { return ASETS_ABI_VERSION; }
@@ -238,6 +260,8 @@ extern "C" ASETS_API void asets_context_destroy(asets_context *ctx)
         }
         if (ctx->pinned_flags)
             cudaFreeHost(ctx->pinned_flags);
+        if (ctx->pool)
+            cudaMemPoolDestroy(ctx->pool);  // every call freed its blocks before returning
     }
     delete ctx;
 }

@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-solver measurement")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the binary 2D / Potts 3D / Ishikawa 2D workloads")
+    ap.add_argument("--no-next", action="store_true",
+                    help="skip the hierarchical/DAG, Matlab-semantics, star-shape and cost-term "
+                         "measurements")
     ap.add_argument("--warm-seeds", type=int, default=4,
                     help="held-out Potts problems for the warm-start comparison (0: skip)")
     ap.add_argument("--profile-iters", type=int, default=0,
@@ -320,6 +323,186 @@ def configs_run(ctx) -> list:
     return rows
 
 
+def _per_iteration_s(solve, n: int) -> float:
+    """Seconds per iteration of a synchronous host-array solve: the
+    difference of an n- and a 2n-iteration solve (copies and set-up cancel),
+    best of two."""
+    import torch
+
+    def wall(k):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        solve(k)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t
+
+    solve(2)  # warm-up
+    d = [wall(2 * n) - wall(n) for _ in range(2)]
+    return max(min(d), 1e-9) / n
+
+
+def _hmf_tree(make, shape, dt, seed):
+    """Five leaves (Ct = sqrt|I - i/4|), the first two under an inner node."""
+    g = np.random.default_rng(seed)
+    img = g.random(shape).astype(dt)
+    leaves = [make([], 0.15, np.sqrt(np.abs(img - dt(i / 4))).astype(dt)) for i in range(5)]
+    return make([make(leaves[:2], 0.2)] + leaves[2:], 0)
+
+
+def _dag_graph(make, shape, dt, seed):
+    """Four leaves, two inner nodes sharing two of them."""
+    g = np.random.default_rng(seed)
+    img = g.random(shape).astype(dt)
+    L = [make([], 0.15, np.abs(img - dt(i / 3)).astype(dt)) for i in range(4)]
+    return make([make([L[0], L[1], L[2]], 0.2), make([L[1], L[2], L[3]], 0.25)], 0)
+
+
+def next_rows_run(ctx, stream, cpu: bool) -> list:
+    """The solvers beside the mex path (hierarchical / DAG max-flow, the
+    Matlab-semantics solvers, star-shape Potts 2D) and the cost-term kernels:
+    device time per iteration (host-array solves: difference of two solve
+    lengths; cost kernels: CUDA events on device arrays), rate against the
+    algorithmic bytes, and (cpu) the numpy restatement timed on one core for
+    a few iterations of the same problem.  `stream` is the context's stream."""
+    import torch
+
+    from asetsmatlabmaxflow_gb300 import costs as K
+    from asetsmatlabmaxflow_gb300 import hmf as HM
+    from asetsmatlabmaxflow_gb300 import matlab as M
+    from asetsmatlabmaxflow_gb300 import native as N
+    from asetsmatlabmaxflow_gb300 import starshape as SS
+    from asetsmatlabmaxflow_gb300 import synth
+
+    peak, peak_kind = peaks()
+    rows = []
+
+    def row(name, units, unit_name, bytes_per_unit, bytes_note, sec_per_it, cpu_fn=None,
+            cpu_its=0, dtype="f32"):
+        r = {"workload": name, "dtype": dtype, "ms_per_iteration": 1e3 * sec_per_it,
+             f"g{unit_name}_per_s": units / sec_per_it / 1e9,
+             "bytes_per_unit": bytes_per_unit, "bytes": bytes_note,
+             "roofline": {"bound": "hbm", "achieved": units * bytes_per_unit / sec_per_it / 1e9,
+                          "peak": peak, "unit": "GB/s",
+                          "frac": units * bytes_per_unit / sec_per_it / 1e9 / peak,
+                          "peak_kind": peak_kind}}
+        if cpu and cpu_fn is not None:
+            t = time.perf_counter()
+            cpu_fn(cpu_its)
+            s = (time.perf_counter() - t) / cpu_its
+            r["cpu_baseline"] = {"value": units / s / 1e9, "unit": f"G{unit_name}/s", "cores": 1,
+                                 "kind": "port",
+                                 "sample": f"{cpu_its} iterations incl. initialisation, numpy, "
+                                           "same problem"}
+        rows.append(r)
+
+    shape2 = (1024, 1024)
+    npix = shape2[0] * shape2[1]
+    # hierarchical max-flow, float32: 6 nodes below the root (5 leaves)
+    state = {}
+
+    def hmf(k):
+        if "h" not in state:
+            state["h"] = _hmf_tree(HM.asetsHMF2D, shape2, np.float32, 0)
+        state["h"].MaxFullFlow(k, 0.1, 0.25, ctx=ctx)
+
+    def hmf_cpu(k):
+        from oracle import hmf as OH
+        _hmf_tree(OH.Node, shape2, np.float32, 0).max_full_flow(k, 0.1, 0.25)
+
+    row("hmf2d_1024^2_6nodes_full_flow", 6 * npix, "node-pixel-iter", 32 + 4 * 5 / 6 + 8 / 6,
+        "per node-pixel: px, py, pt, u read+written; Ct of the 5 leaves and the root's pt",
+        _per_iteration_s(hmf, 20), hmf_cpu, 2)
+
+    def dag(k):
+        if "d" not in state:
+            state["d"] = _dag_graph(HM.asetsDAGMF2D, shape2, np.float32, 0)
+        state["d"].MaxFullFlow(k, 0.1, 0.25, ctx=ctx)
+
+    def dag_cpu(k):
+        from oracle import dag as OD
+        _dag_graph(OD.Node, shape2, np.float32, 0).max_full_flow(k, 0.1, 0.25)
+
+    row("dag2d_1024^2_6nodes_full_flow", 6 * npix, "node-pixel-iter", 32 + 4 * 4 / 6 + 8 / 6,
+        "per node-pixel: px, py, pt, u read+written; Ct of the 4 leaves and the root's pt "
+        "(the shared children's pn not counted)", _per_iteration_s(dag, 20), dag_cpu, 2)
+
+    # Matlab-semantics binary 3D, float32, 256^3 (never breaks: errBound 0, '<' rule)
+    cs, ct, al = synth.binary3d(seed=0, shape=(256, 256, 256))
+    nvox = cs.size
+
+    def mt3(k):
+        M.asetsBinaryMF3D(cs, ct, al, [256, 256, 256, k, 0.0, 0.35, 0.11], ctx=ctx)
+
+    def mt3_cpu(k):
+        from oracle import mtwin as OM
+        OM.binary(cs, ct, al, k, 0.0, 0.35, 0.11)
+
+    row("matlab_binary3d_256^3", nvox, "voxel-iter", 60,
+        "bx, by, bz, ps, pt, u read+written, Cs, Ct, alpha read (fp32)",
+        _per_iteration_s(mt3, 20), mt3_cpu, 2)
+
+    # Matlab-semantics Potts 2D, float64, 1024^2 L=4
+    g = np.random.default_rng(0)
+    ctp = g.random(shape2 + (4,))
+    alp = np.full(shape2 + (4,), 0.3)
+
+    def mp2(k):
+        M.asetsPotts2D(ctp, alp, [1024, 1024, 4, k, 0.0, 0.3, 0.16], ctx=ctx)
+
+    def mp2_cpu(k):
+        from oracle import mtwin as OM
+        OM.potts(ctp, alp, k, 0.0, 0.3, 0.16)
+
+    row("matlab_potts2d_1024^2_L4_f64", npix, "pixel-iter", (4 * 4 + 1) * 16 + 2 * 4 * 8,
+        "(4L+1) state arrays read+written, Ct and alpha read (fp64)",
+        _per_iteration_s(mp2, 20), mp2_cpu, 2, dtype="f64")
+
+    # star-shape Potts 2D, float64, 512^2 L=4
+    ss = (512, 512)
+    cts = g.random(ss + (4,))
+    als = 0.1 + 0.3 * g.random(ss + (4,))
+    pts = np.array([[64, 64], [448, 64], [64, 448], [448, 448]])
+
+    def star(k):
+        SS.asetsPotts2D_starShape(cts, als, [512, 512, 4, k, 0.0, 0.25, 0.11, 0.05], pts, ctx=ctx)
+
+    def star_cpu(k):
+        from oracle import starshape as OS
+        OS.solve(cts, als, [512, 512, 4, k, 0.0, 0.25, 0.11, 0.05], [tuple(p) for p in pts])
+
+    row("starshape_potts2d_512^2_L4_f64", ss[0] * ss[1], "pixel-iter",
+        (5 * 4 + 1) * 16 + 4 * 4 * 8,
+        "px, py, pt, u, v per label and ps read+written; Ct, alpha, two direction fields read (fp64)",
+        _per_iteration_s(star, 20), star_cpu, 2, dtype="f64")
+
+    # cost terms on device arrays, 256^3: CUDA events on the context's stream
+    img = torch.from_numpy(np.asfortranarray(ct).ravel(order="F").copy()).cuda()
+    out = torch.empty(nvox * 4, device="cuda")
+    models = np.array([0.2, 0.4, 0.6, 0.8], np.float32)
+
+    def events(fn, n=10):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) * 1e-3 / n
+
+    row("cost_l1_256^3_L4", nvox, "voxel", 8 + 16,
+        "image read twice (range, then costs), 4 costs written", events(
+            lambda: N.check(N.lib().asets_cost_l1(ctx.handle, N.DEVICE, img.data_ptr(), nvox,
+                                                  models.ctypes.data, 4, 1, out.data_ptr()))))
+    row("alpha_contrast_256^3", nvox, "voxel", 12,
+        "image read twice (range, then gradient), alpha written", events(
+            lambda: N.check(N.lib().asets_alpha_contrast(ctx.handle, N.DEVICE, img.data_ptr(),
+                                                         256, 256, 256, 1, 0.1, 0.9, 10.0, 1, 1,
+                                                         out.data_ptr()))))
+    return rows
+
+
 def warm_start_run(ctx, nseeds: int) -> dict:
     """Potts 3D 128^3, L = 6, errBound 1e-4 on held-out seeds: cold start vs
     the multilevel solve vs the multilevel solve whose coarsest level starts
@@ -506,6 +689,8 @@ def main():
     batch = None if args.no_batch else batch_run(ctx)
     configs = configs_run(ctx) if (rank == 0 and not args.no_configs) else None
     warm = warm_start_run(ctx, args.warm_seeds) if (rank == 0 and args.warm_seeds > 0) else None
+    nxt = next_rows_run(ctx, stream, not args.no_cpu_baseline) \
+        if (rank == 0 and not args.no_next) else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -539,6 +724,7 @@ def main():
             "gpu_launches": launches,
             "batch": batch,
             "configs": configs,
+            "next": nxt,
             "finite": ok,
         }
         if cpu is not None:

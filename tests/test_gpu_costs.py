@@ -14,7 +14,9 @@ def _gpu():
     require_gpu()
 
 
-SHAPES = [(37, 29, 11), (64, 48), (5, 1, 3), (128, 1)]
+# (40, 36, 70): 16-byte paths (element count a multiple of 4) and several
+# plane blocks of the alpha kernel; the others ragged
+SHAPES = [(37, 29, 11), (64, 48), (5, 1, 3), (128, 1), (40, 36, 70)]
 
 
 def _img(shape, seed):
