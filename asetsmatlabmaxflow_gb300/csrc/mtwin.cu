@@ -9,10 +9,11 @@
 // evaluation order (IEEE operations, no contraction), so u matches a numpy
 // restatement in the same precision bit for bit.
 //
-// Per iteration, four passes over every flow label (binary 1, Potts L,
+// Per iteration, five passes over every flow label (binary 1, Potts L,
 // Ishikawa L-1):
-//   1 gradient step of the face flows from ud = divp - ((A - B) + u/cc),
+//   0 ud = divp - ((A - B) + u/cc) per cell (into the gk buffer),
 //     (A, B) = (ps, pt) binary, (ps, pt_k) Potts, (pt_k, pt_k+1) Ishikawa
+//   1 gradient step of the face flows from ud of the cell and the one below
 //   2 projection factor gk = 1/max(1, |p|/alpha) per cell
 //   3 face flows *= 0.5 (gk + gk of the cell below)
 //   4 per cell: divp of every label, then the model's sink/source flows and
@@ -144,6 +145,21 @@ __device__ __forceinline__ T ud(const MTArgs<T> &A, int k, long long g)
     return sub(A.divp[o], add(sub(a, b), dvd(A.u[o], A.cc)));
 }
 
+// ud of every flow label and cell, into the gk buffer (free until mt_gk):
+// the face pass then reads it for the cell and its three lower neighbours
+// instead of forming it four times.
+template <class T, int M>
+__global__ void mt_ud(const MTArgs<T> A)
+{
+    if (finished(A))
+        return;
+    MT_LOOP(A.n * A.nflow)
+    {
+        const int k = label_of(t, A.n);
+        A.gk[t] = ud<T, M>(A, k, t - (long long)k * A.n);
+    }
+}
+
 template <class T, int M, int D>
 __global__ void mt_step(const MTArgs<T> A)
 {
@@ -153,19 +169,19 @@ __global__ void mt_step(const MTArgs<T> A)
     {
         const int k = label_of(t, A.n);
         const Cell<T> c(A, t - (long long)k * A.n);
-        const T u0 = ud<T, M>(A, k, c.g);
+        const T u0 = A.gk[t];
         // binary: pp + steps*(d); Potts/Ishikawa: steps*(d) + pp
         auto upd = [&](T *f, T nb) {
             const T s = mul(A.steps, sub(u0, nb));
             *f = (M == MT_BINARY) ? add(*f, s) : add(s, *f);
         };
         if (c.x >= 1)
-            upd(A.p1 + (long long)k * A.f1 + j1(A, c.y, c.x, c.z), ud<T, M>(A, k, c.g - A.rows));
+            upd(A.p1 + (long long)k * A.f1 + j1(A, c.y, c.x, c.z), A.gk[t - A.rows]);
         if (c.y >= 1)
-            upd(A.p2 + (long long)k * A.f2 + j2(A, c.y, c.x, c.z), ud<T, M>(A, k, c.g - 1));
+            upd(A.p2 + (long long)k * A.f2 + j2(A, c.y, c.x, c.z), A.gk[t - 1]);
         if (D == 3 && c.z >= 1)
             upd(A.p3 + (long long)k * A.f3 + j3(A, c.y, c.x, c.z),
-                ud<T, M>(A, k, c.g - (long long)A.rows * A.cols));
+                A.gk[t - (long long)A.rows * A.cols]);
     }
 }
 
@@ -466,6 +482,7 @@ asets_status mt_run(asets_context *ctx, int rows, int cols, int slices, int nlab
         int h_done = 0;
         for (int done_it = 0; e == cudaSuccess && done_it < iterNum; done_it += kChunk) {
             for (int i = 0; i < kChunk && done_it + i < iterNum; ++i) {
+                mt_ud<T, M><<<grid, kThreads, 0, st>>>(A);
                 mt_step<T, M, D><<<grid, kThreads, 0, st>>>(A);
                 mt_gk<T, M, D><<<grid, kThreads, 0, st>>>(A);
                 mt_rescale<T, M, D><<<grid, kThreads, 0, st>>>(A);

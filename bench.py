@@ -59,9 +59,13 @@ def parse():
     ap.add_argument("--shape", default="256,256,256", help="volume for --profile-iters")
     ap.add_argument("--tile-config", type=int, default=0, help="kernel variant for --profile-iters")
     ap.add_argument("--profile-model", default="binary",
-                    choices=["binary", "potts", "potts192", "ishikawa1024"],
+                    choices=["binary", "potts", "potts192", "ishikawa1024", "hmf", "dag", "costs",
+                             "matlab3d", "starshape"],
                     help="model for --profile-iters (potts: the warm-start workload, seed 1000000; "
-                         "potts192: Potts 3D 192^3 L=4; ishikawa1024: Ishikawa 2D 1024^2 L=8)")
+                         "potts192: Potts 3D 192^3 L=4; ishikawa1024: Ishikawa 2D 1024^2 L=8; "
+                         "hmf / dag: the 1024^2 six-node tree / graph of the `next` entries; "
+                         "costs: N pairs of L1-cost and contrast-alpha calls on 256^3; "
+                         "matlab3d: Matlab-semantics binary 3D 256^3; starshape: 512^2 L=4)")
     ap.add_argument("--profile-conv", type=int, default=0,
                     help="run the warm-start network's forward pass on an S^3 volume and exit")
     return ap.parse_args()
@@ -108,6 +112,50 @@ def profile_run(args):
         ms, n = run.s.last_run_stats()
         print(json.dumps({"profile_run": "potts 128^3 L=6", "iterations": it,
                           "ms_per_iteration": ms / max(args.profile_iters, 1)}))
+        return
+    if args.profile_model in ("hmf", "dag"):
+        from asetsmatlabmaxflow_gb300 import hmf as HM
+
+        make = _hmf_tree if args.profile_model == "hmf" else _dag_graph
+        cls = HM.asetsHMF2D if args.profile_model == "hmf" else HM.asetsDAGMF2D
+        make(cls, (1024, 1024), np.float32, 0).MaxFullFlow(args.profile_iters, 0.1, 0.25)
+        print(json.dumps({"profile_run": f"{args.profile_model} 1024x1024, 6 nodes",
+                          "iterations": args.profile_iters}))
+        return
+    if args.profile_model == "matlab3d":
+        from asetsmatlabmaxflow_gb300 import matlab as M
+
+        cs, ct, al = synth.binary3d(seed=0, shape=(256, 256, 256))
+        M.asetsBinaryMF3D(cs, ct, al, [256, 256, 256, args.profile_iters, 0.0, 0.35, 0.11])
+        print(json.dumps({"profile_run": "matlab binary 3D 256^3", "iterations": args.profile_iters}))
+        return
+    if args.profile_model == "starshape":
+        from asetsmatlabmaxflow_gb300 import starshape as SS
+
+        g = np.random.default_rng(0)
+        ct = g.random((512, 512, 4))
+        al = 0.1 + 0.3 * g.random((512, 512, 4))
+        pts = np.array([[64, 64], [448, 64], [64, 448], [448, 448]])
+        SS.asetsPotts2D_starShape(ct, al, [512, 512, 4, args.profile_iters, 0.0, 0.25, 0.11, 0.05],
+                                  pts)
+        print(json.dumps({"profile_run": "star-shape Potts 2D 512^2 L=4",
+                          "iterations": args.profile_iters}))
+        return
+    if args.profile_model == "costs":
+        import torch
+
+        cs, ct, al = synth.binary3d(seed=0, shape=(256, 256, 256))
+        img = torch.from_numpy(ct.ravel(order="F").copy()).cuda()
+        out = torch.empty(img.numel() * 4, device="cuda")
+        models = np.array([0.2, 0.4, 0.6, 0.8], np.float32)
+        h = N.Context.default().handle
+        for _ in range(args.profile_iters):
+            N.check(N.lib().asets_cost_l1(h, N.DEVICE, img.data_ptr(), img.numel(),
+                                          models.ctypes.data, 4, 1, out.data_ptr()))
+            N.check(N.lib().asets_alpha_contrast(h, N.DEVICE, img.data_ptr(), 256, 256, 256, 1,
+                                                 0.1, 0.9, 10.0, 1, 1, out.data_ptr()))
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_run": "costs 256^3", "calls": args.profile_iters}))
         return
     if args.profile_model in ("potts192", "ishikawa1024"):
         # the multi-region configurations: cc 0.3, steps 0.11 (3D) / 0.16 (2D)
@@ -324,21 +372,26 @@ def configs_run(ctx) -> list:
 
 
 def _per_iteration_s(solve, n: int) -> float:
-    """Seconds per iteration of a synchronous host-array solve: the
-    difference of an n- and a 2n-iteration solve (copies and set-up cancel),
-    best of two."""
+    """Seconds per iteration of a synchronous host-array solve: the slope of
+    the wall time of n-, 2n- and 4n-iteration solves (best of two each;
+    copies and set-up do not depend on the iteration count)."""
     import torch
 
     def wall(k):
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        solve(k)
-        torch.cuda.synchronize()
-        return time.perf_counter() - t
+        best = float("inf")
+        for _ in range(2):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            solve(k)
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t)
+        return best
 
     solve(2)  # warm-up
-    d = [wall(2 * n) - wall(n) for _ in range(2)]
-    return max(min(d), 1e-9) / n
+    ks = np.array([n, 2 * n, 4 * n], float)
+    ts = np.array([wall(int(k)) for k in ks])
+    slope = float(np.polyfit(ks, ts, 1)[0])
+    return max(slope, 1e-9)
 
 
 def _hmf_tree(make, shape, dt, seed):
