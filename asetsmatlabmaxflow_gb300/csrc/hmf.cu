@@ -582,50 +582,26 @@ __global__ void k_dag_g(const HArgs<T> A)
     }
 }
 
-// Bytes of dynamic shared memory that k_dag_point stages the graph in: the
-// node table, the top-down order, the child lists and their weights.
-template <class T>
-size_t dag_smem_bytes(int m, int nkids)
-{
-    return sizeof(NodeDev<T>) * m + sizeof(T) * nkids + sizeof(int) * (m + nkids);
-}
-
 // pn reset, PushDownFlows (top-down), PushCapacityUp (bottom-up), labels.
-// The graph is read from shared memory (staged once per block): every pixel
-// walks all nodes several times.
 template <class T>
-__global__ void k_dag_point(const HArgs<T> A, int nkids)
+__global__ void k_dag_point(const HArgs<T> A)
 {
-    extern __shared__ __align__(16) unsigned char dag_sm[];
-    NodeDev<T> *ns = reinterpret_cast<NodeDev<T> *>(dag_sm);
-    T *ws = reinterpret_cast<T *>(ns + A.m);
-    int *os = reinterpret_cast<int *>(ws + nkids);
-    int *cs = os + A.m;
-    for (int i = threadIdx.x; i < A.m; i += kThreads) {
-        ns[i] = A.nodes[i];
-        os[i] = A.order[i];
-    }
-    for (int i = threadIdx.x; i < nkids; i += kThreads) {
-        ws[i] = A.wchild[i];
-        cs[i] = A.children[i];
-    }
-    __syncthreads();
     H_LOOP(A.n)
     {
         const long long c = t;
         for (int i = 0; i < A.m; ++i)
-            if (ns[i].nparent > 1)
+            if (A.nodes[i].nparent > 1)
                 A.pn[(long long)i * A.n + c] = (T)0;
         for (int j = 0; j < A.m; ++j) {
-            const int i = os[j];
-            const NodeDev<T> &nd = ns[i];
+            const int i = A.order[j];
+            const NodeDev<T> nd = A.nodes[i];
             const long long o = (long long)i * A.n + c;
             const T pt = A.pt[o];
             for (int k = 0; k < nd.nchild; ++k) {
-                const int ch = cs[nd.child_begin + k];
-                if (ns[ch].nparent > 1) {
+                const int ch = A.children[nd.child_begin + k];
+                if (A.nodes[ch].nparent > 1) {
                     T *pn = A.pn + (long long)ch * A.n + c;
-                    *pn = add(*pn, mul(ws[nd.child_begin + k], pt));
+                    *pn = add(*pn, mul(A.wchild[nd.child_begin + k], pt));
                 }
             }
             if (nd.nparent > 0 && nd.nchild > 0)
@@ -634,8 +610,8 @@ __global__ void k_dag_point(const HArgs<T> A, int nkids)
                 A.g[o] = A.inv_cc;
         }
         for (int j = A.m - 1; j >= 0; --j) {
-            const int i = os[j];
-            const NodeDev<T> &nd = ns[i];
+            const int i = A.order[j];
+            const NodeDev<T> nd = A.nodes[i];
             const long long o = (long long)i * A.n + c;
             if (nd.nchild == 0) {
                 const T x = add(sub(dag_in(A, nd, i, c), A.div[o]), dvd(A.u[o], A.cc));
@@ -646,11 +622,11 @@ __global__ void k_dag_point(const HArgs<T> A, int nkids)
             const T pto = A.pt[o];
             T g = A.g[o];
             for (int k = 0; k < nd.nchild; ++k) {
-                const int ch = cs[nd.child_begin + k];
+                const int ch = A.children[nd.child_begin + k];
                 const long long oc = (long long)ch * A.n + c;
                 const T uc = dvd(A.u[oc], A.cc);
-                if (ns[ch].nparent > 1) {
-                    const T w = ws[nd.child_begin + k];
+                if (A.nodes[ch].nparent > 1) {
+                    const T w = A.wchild[nd.child_begin + k];
                     const T e = sub(sub(add(add(A.div[oc], A.pt[oc]), mul(w, pto)), A.pn[oc]), uc);
                     g = add(g, mul(w, e));
                 } else {
@@ -661,8 +637,8 @@ __global__ void k_dag_point(const HArgs<T> A, int nkids)
             A.pt[o] = dvd(g, nd.wdiv);
         }
         for (int j = 0; j < A.m; ++j) {
-            const int i = os[j];
-            const NodeDev<T> &nd = ns[i];
+            const int i = A.order[j];
+            const NodeDev<T> nd = A.nodes[i];
             if (nd.nparent == 0)
                 continue;
             const long long o = (long long)i * A.n + c;
@@ -1055,17 +1031,13 @@ asets_status run_dag(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
         set_last_error("asets_dag_full_flow: out of device memory");
     } else if (e == cudaSuccess) {
         const int gp = h_grid(n, sms), gn = h_grid(n * (m - 1), sms);
-        const size_t smem_point = dag_smem_bytes<T>(m, (int)kids.size());
-        if (smem_point > 48 * 1024)
-            e = cudaFuncSetAttribute(k_dag_point<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem_point);
         k_dag_init<T><<<gp, kThreads, 0, st>>>(A);
         if (dirs)
             k_norm_dirs<T><<<h_grid(n * m, sms), kThreads, 0, st>>>(A);
         for (int it = 0; it < its && e == cudaSuccess; ++it) {
             k_dag_g<T><<<gn, kThreads, 0, st>>>(A);
             spatial_passes(A, gn, st, dirs);
-            k_dag_point<T><<<gp, kThreads, smem_point, st>>>(A, (int)kids.size());
+            k_dag_point<T><<<gp, kThreads, 0, st>>>(A);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess && dirs)
@@ -1146,12 +1118,6 @@ extern "C" ASETS_API asets_status asets_dag_run(
     std::vector<int> kids(children ? children : nullptr, children ? children + total : nullptr);
     if ((int)kids.size() != total) {
         set_last_error("asets_dag_full_flow: children missing");
-        return ASETS_ERR_INVALID_ARG;
-    }
-    // the per-pixel pass stages the graph in shared memory (up to 200 KB)
-    if ((precision == 8 ? dag_smem_bytes<double>(m, total) : dag_smem_bytes<float>(m, total)) >
-        200u * 1024u) {
-        set_last_error("asets_dag_full_flow: graph too large (node table above 200 KB)");
         return ASETS_ERR_INVALID_ARG;
     }
     for (int i = 0; i < m; ++i)
