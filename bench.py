@@ -609,7 +609,9 @@ def run_reference(args, rank, pg):
 
     cs, ct, alpha = synth.binary3d(seed=0, shape=SHAPE)
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    iters = 2  # per core per step: a bounded sample of the 200-iteration run
+    # per core per step: a bounded sample of the 200-iteration run, long
+    # enough that the per-call allocation and init do not dominate it
+    iters = 8
 
     def one(_):
         O.solve("binary", SHAPE, ct, alpha, cs=cs, max_it=iters, err_bound=0.0, cc=CC, steps=STEPS)
