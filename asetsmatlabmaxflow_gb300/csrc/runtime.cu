@@ -1440,7 +1440,9 @@ extern "C" ASETS_API asets_status asets_batch_add(asets_batch *b, asets_solver *
     return ASETS_OK;
 }
 
-// Per-item partial storage of a member sized for `items`.
+// Per-item partial storage of a member sized for `items`.  The member's
+// own item map (used when it is solved alone) must stay all zeros: a later
+// single solve may adopt the grown buffers.
 static asets_status ensure_items(asets_solver *s, int items)
 {
     if (items <= s->items_cap)
@@ -1449,6 +1451,7 @@ static asets_status ensure_items(asets_solver *s, int items)
     CU_TRY(cudaMalloc(&ptr, sizeof(int) * items));
     s->allocations.push_back(ptr);
     s->d_item_problem = static_cast<int *>(ptr);
+    CU_TRY(cudaMemsetAsync(s->d_item_problem, 0, sizeof(int) * items, s->ctx->stream));
     CU_TRY(cudaMalloc(&ptr, sizeof(double) * items));
     s->allocations.push_back(ptr);
     s->d_item_partials = static_cast<double *>(ptr);
@@ -1473,7 +1476,10 @@ static asets_status batch_layout(asets_batch *b, asets_batch::Group &g)
     for (size_t j = 0; j < g.idx.size(); ++j) {
         asets_solver *s = b->members[g.idx[j]];
         ProblemDesc d = s->desc;
-        // chunks of about 64 planes: the batch already fills the GPU
+        // chunks of about 64 planes: the batch already fills the GPU.  The
+        // batch's layout lives only in its own descriptor copy `d`: the
+        // member's descriptor keeps its single-solve layout, which a later
+        // solve of the member alone uploads as it is.
         d.zchunks = std::max(1, (s->ns + 32) / 64);
         StencilProblem sp;
         memset(&sp, 0, sizeof sp);
@@ -1488,9 +1494,6 @@ static asets_status batch_layout(asets_batch *b, asets_batch::Group &g)
         d.item_begin = (int)item_problem.size();
         d.n_items = items;
         d.item_partials = s->d_item_partials;
-        s->desc.zchunks = d.zchunks;
-        s->desc.n_items = items;
-        s->desc.item_begin = d.item_begin;
         item_problem.insert(item_problem.end(), items, (int)j);
         descs.push_back(d);
     }

@@ -147,3 +147,29 @@ def test_mixed_batch_with_labelled_members_equals_individual_solves(exact):
     b.close()
     for s in members:
         s.close()
+
+
+@pytest.mark.parametrize("tile_config", [0, 2])
+def test_member_solved_alone_after_a_batch(tile_config):
+    """A member keeps its own single-solve layout through a batch run: solved
+    alone afterwards (with the batch's kernel variant, or another one) it
+    gives exactly what the batch gave it."""
+    from asetsmatlabmaxflow_gb300 import native as N
+
+    ctx = N.Context.default()
+    solvers = []
+    for shape, cs, ct, alpha in _problems():
+        s = N.Solver(ctx, "binary", shape)
+        s.set_inputs(ct, alpha, cs)
+        solvers.append(s)
+    b = N.Batch(ctx)
+    for s in solvers:
+        b.add(s)
+    its = b.run(300, 1e-4, 0.3, 0.11, exact=True)
+    got = [s.get_u().copy() for s in solvers]
+    for s, it, u in zip(solvers, its, got):
+        assert s.run(300, 1e-4, 0.3, 0.11, exact=True, tile_config=tile_config) == it
+        np.testing.assert_array_equal(bits(s.get_u()), bits(u))
+    b.close()
+    for s in solvers:
+        s.close()
