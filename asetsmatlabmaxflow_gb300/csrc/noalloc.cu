@@ -12,9 +12,14 @@
 // one file-scope device array of fixed size.  It calls no cudaMalloc,
 // cudaFree or other allocating routine.
 //
-// That array is reserved on every GPU that loads the library, for the life
-// of the process: kNoallocScratchBytes (about 15 MiB).  Problems whose padded
-// volume exceeds kNoallocMaxCells voxels are rejected.
+// That array (kNoallocScratchBytes, about 15 MiB) is device memory of the
+// library's module: with CUDA's lazy module loading (the default) it is
+// reserved when the first call on a device looks up its address, and at
+// library load with CUDA_MODULE_LOADING=EAGER; from then on the device holds
+// it until the process exits.  A caller that hands the GPU to another
+// allocator makes one small call first (a 1 x 1 x 1 problem with maxIt 0
+// will do).  Problems whose padded volume exceeds kNoallocMaxCells voxels
+// are rejected.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -43,6 +48,7 @@ constexpr size_t kQueueBytes = 256;
 constexpr size_t kItemBytes = kMaxItems * (sizeof(int) + sizeof(double));
 constexpr size_t kNoallocScratchBytes =
     kNumFields * kFieldBytes + kControlBytes + kDescBytes + kQueueBytes + kItemBytes;
+constexpr int kLaunchChunk = 64;              // iterations queued between done-flag reads
 
 }  // namespace
 
@@ -108,7 +114,10 @@ asets_status setup_device(int dev, DeviceSetup **out)
         cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
         if (e != cudaSuccess) {
             cudaGetLastError();
-            return na_fail(ASETS_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+            // the lookup loads the module, which reserves the array
+            return na_fail(e == cudaErrorMemoryAllocation ? ASETS_ERR_OUT_OF_MEMORY
+                                                          : ASETS_ERR_CUDA,
+                           "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
         }
         int sms = 0;
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -128,6 +137,11 @@ asets_status setup_device(int dev, DeviceSetup **out)
     *out = &d;
     return ASETS_OK;
 }
+
+asets_status noalloc_solve(DeviceSetup &dv, const asets_options *opt, const float *alpha,
+                           const float *Cs, const float *Ct, int Nx, int Ny, int Nz,
+                           long long pitch, long long cells, int maxIt, float errBound, float cc,
+                           float steps, float *u, float *cvg, int *itNum, cudaStream_t sm);
 
 }  // namespace
 
@@ -159,7 +173,25 @@ extern "C" ASETS_API asets_status asets_binary_mf3d_noalloc(
         return st;
     std::lock_guard<std::mutex> call_lock(d->call_mu);
     cudaStream_t sm = static_cast<cudaStream_t>(stream);
+    st = noalloc_solve(*d, opt, alpha, Cs, Ct, Nx, Ny, Nz, pitch, cells, maxIt, errBound, cc,
+                       steps, u, cvg, itNum, sm);
+    if (st != ASETS_OK) {
+        // An error may leave this call's copies and kernels queued: let them
+        // finish before the next call reuses the scratch.
+        cudaStreamSynchronize(sm);
+        cudaGetLastError();
+    }
+    return st;
+}
 
+namespace {
+
+asets_status noalloc_solve(DeviceSetup &dv, const asets_options *opt, const float *alpha,
+                           const float *Cs, const float *Ct, int Nx, int Ny, int Nz,
+                           long long pitch, long long cells, int maxIt, float errBound, float cc,
+                           float steps, float *u, float *cvg, int *itNum, cudaStream_t sm)
+{
+    DeviceSetup *d = &dv;
     // carve the scratch
     unsigned char *base = d->scratch;
     auto field = [&](int i) { return reinterpret_cast<float *>(base + (size_t)i * kFieldBytes); };
@@ -272,7 +304,9 @@ extern "C" ASETS_API asets_status asets_binary_mf3d_noalloc(
                                 v->smem_bytes));
     int per_sm = 0;
     NA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, v->nt, v->smem_bytes));
-    const long long slots = (long long)d->num_sms * (per_sm > 0 ? per_sm : 1);
+    if (per_sm < 1)
+        return na_fail(ASETS_ERR_UNSUPPORTED, "the iteration kernel does not fit on an SM");
+    const long long slots = (long long)d->num_sms * per_sm;
     A.zchunks = choose_zchunks(p, *v, slots);
     const int items = problem_items(p, *v, A.zchunks);
     if (items > kMaxItems)
@@ -303,12 +337,23 @@ extern "C" ASETS_API asets_status asets_binary_mf3d_noalloc(
     if (grid < 1)
         grid = 1;
 
-    // All maxIt iterations are queued; once erriter meets errBound the
-    // remaining launches return at entry.
+    // Iterations are queued in chunks; after each chunk the host reads the
+    // control block's done flag and stops queueing once erriter has met
+    // errBound (a launch queued after that returns at entry).
     void *params[] = {&bargs};
-    for (int i = 0; i < maxIt; ++i)
-        NA_TRY(cudaLaunchKernel(v->fn, dim3((unsigned)grid), dim3(v->nt), params, v->smem_bytes,
-                                sm));
+    for (int i0 = 0; i0 < maxIt; i0 += kLaunchChunk) {
+        const int i1 = (maxIt - i0 < kLaunchChunk) ? maxIt : i0 + kLaunchChunk;
+        for (int i = i0; i < i1; ++i)
+            NA_TRY(cudaLaunchKernel(v->fn, dim3((unsigned)grid), dim3(v->nt), params,
+                                    v->smem_bytes, sm));
+        if (i1 < maxIt) {
+            int done = 0;
+            NA_TRY(cudaMemcpyAsync(&done, &ctl->done, sizeof done, cudaMemcpyDeviceToHost, sm));
+            NA_TRY(cudaStreamSynchronize(sm));
+            if (done)
+                break;
+        }
+    }
     IterControl out;
     NA_TRY(cudaMemcpyAsync(&out, ctl, sizeof out, cudaMemcpyDeviceToHost, sm));
     NA_TRY(cudaStreamSynchronize(sm));
@@ -322,3 +367,5 @@ extern "C" ASETS_API asets_status asets_binary_mf3d_noalloc(
     return ASETS_OK;
 #undef NA_TRY
 }
+
+}  // namespace

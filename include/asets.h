@@ -482,16 +482,21 @@ ASETS_API asets_status asets_alpha_contrast(asets_context *ctx, asets_memory whe
  * pointers (Matlab layout; cvg has maxIt entries), itNum is a host pointer,
  * and stream is a cudaStream_t (NULL: the default stream) on the current
  * device.  It calls no cudaMalloc/cudaFree or other allocating routine: its
- * scratch lives in one fixed device array of about 15 MiB that every GPU
- * loading the library reserves until the process exits.  Problems whose
- * padded volume (row pitch x Nx x Nz, the pitch being Ny rounded up to a
- * multiple of 32, or of 4 below 32 rows) exceeds 262144 voxels are rejected
- * with ASETS_ERR_INVALID_ARG.  The first call on a device looks up that
- * array's address; make it before any stream capture.  All calls on a device
+ * scratch lives in one fixed device array of about 15 MiB, device memory of
+ * the library's module.  Under CUDA's default lazy module loading that array
+ * is reserved by the first call on a device (which looks up its address),
+ * or at library load with CUDA_MODULE_LOADING=EAGER, and held until the
+ * process exits: a caller that later hands the GPU to another allocator
+ * makes one small call first (a 1x1x1 problem with maxIt 0), before that
+ * allocator reserves the device and before any stream capture.  If the
+ * first call cannot reserve it, it returns ASETS_ERR_OUT_OF_MEMORY.
+ * Problems whose padded volume (row pitch x Nx x Nz, the pitch being Ny
+ * rounded up to a multiple of 32, or of 4 below 32 rows) exceeds 262144
+ * voxels are rejected with ASETS_ERR_INVALID_ARG.  All calls on a device
  * share the array and keep the previous call's contents (the solve clears
  * what must start at zero); calls are serialised inside the library and each
- * waits for its GPU work before returning -- two calls whose GPU work
- * overlapped would race on the shared scratch.
+ * waits for its GPU work before returning, on success and on error -- two
+ * calls whose GPU work overlapped would race on the shared scratch.
  * ---------------------------------------------------------------------- */
 ASETS_API asets_status asets_binary_mf3d_noalloc(const asets_options *opt, const float *alpha,
                                                  const float *Cs, const float *Ct, int Nx,
