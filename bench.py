@@ -39,6 +39,20 @@ BYTES_PER_VOXEL_ITER = 60  # 6 state arrays x (read + write) x 4 B + 3 inputs x 
 WORKLOAD = "binary3d_256^3_200it"
 
 
+def workload_config(world: int) -> dict:
+    """The `config` of both arms' JSON lines (the same dict, so the two lines
+    name the same workload)."""
+    return {"workload": WORKLOAD, "model": "binary continuous max-flow 3D",
+            "shape": list(SHAPE), "iterations_per_step": ITERS, "cc": CC, "steps": STEPS,
+            "err_bound": 0.0, "parallelism": f"replicas{world}",
+            "l2": "working set ~1 GB per iteration, larger than L2; no flush",
+            "voronoi_cells": 40, "intensities": [0.25, 0.75], "noise": 0.2}
+
+
+def host_cores() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -290,7 +304,7 @@ def traffic_per_launch():
     return None
 
 
-def batch_run(ctx) -> dict:
+def batch_run(ctx, cpu: bool) -> dict:
     """Batched workload: 48 binary 2D (sides 128..1024) + 16 binary 3D (sides
     64..160) problems, alpha ~ U[0.2, 0.8], errBound 1e-4, one persistent
     launch per dimension and iteration, autotuned tile variant."""
@@ -313,6 +327,7 @@ def batch_run(ctx) -> dict:
     vox = sum(float(np.prod(p[0].shape)) * (i + 1) for p, i in zip(probs, its))
     out = {"workload": "48 binary 2D (128..1024 per side) + 16 binary 3D (64..160 per side), "
                        "errBound 1e-4, cc 0.3, steps 0.16",
+           "unit": "Gvoxel-iter/s",
            "problems": len(probs), "ms_to_errbound_all": st["ms"],
            "iterations_summed": st["iterations"], "max_iterations": max(its) + 1,
            "gvoxel_iter_per_s": vox / (st["ms"] * 1e-3) / 1e9,
@@ -321,10 +336,59 @@ def batch_run(ctx) -> dict:
     b.close()
     for s in solvers:
         s.close()
+    if cpu:
+        out["cpu_baseline"] = batch_cpu_baseline(probs, cc_, steps_)
     return out
 
 
-def configs_run(ctx) -> list:
+def batch_cpu_baseline(probs, cc_: float, steps_: float, iters: int = 20) -> dict:
+    """The batch on the host: every problem solved by the oracle (the
+    reference's C solver restated, bit-identical to it) for `iters`
+    iterations, one single-thread solve per host core at a time; aggregate
+    voxel-iterations per second over all cores."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+
+    cores = host_cores()
+
+    def one(p):
+        cs, ct, alpha = p
+        O.solve("binary", cs.shape, ct, alpha, cs=cs, max_it=iters, err_bound=0.0, cc=cc_,
+                steps=steps_)
+
+    O.lib()
+    order = sorted(probs, key=lambda p: -p[0].size)  # largest first: even finish
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=cores) as ex:
+        list(ex.map(one, order))
+    dt = time.perf_counter() - t0
+    vox = sum(float(p[0].size) for p in probs) * iters
+    return {"value": vox / dt / 1e9, "unit": "Gvoxel-iter/s", "cores": cores, "kind": "port",
+            "seconds": dt,
+            "sample": f"all {len(probs)} problems, {iters} iterations each incl. init, "
+                      f"{cores} concurrent single-thread solves (C restatement)"}
+
+
+def config_cpu_baseline(model, dims, L, inputs, steps_, iters) -> dict:
+    """One single-thread oracle solve of a `configs` workload, `iters`
+    iterations (init included); inputs are (Ct, alpha[, Cs])."""
+    from oracle import oracle as O
+
+    ct, alpha = inputs[0], inputs[1]
+    cs = inputs[2] if len(inputs) > 2 else None
+    t0 = time.perf_counter()
+    O.solve(model, dims, ct, alpha, cs=cs, nlab=L, max_it=iters, err_bound=0.0, cc=0.3,
+            steps=steps_)
+    dt = time.perf_counter() - t0
+    nvox = float(np.prod(dims))
+    return {"value": nvox * iters / dt / 1e9, "unit": "Gvoxel-iter/s", "cores": 1,
+            "kind": "port", "seconds": dt,
+            "sample": f"{iters} iterations incl. init, 1 thread, same input "
+                      "(C restatement, bit-identical to the reference C)"}
+
+
+def configs_run(ctx, cpu: bool) -> list:
     """The other workloads of the metric, each on its own solver: binary 2D
     256^2 (pars [256,256,300,1e-4,0.3,0.16]), Potts 3D 192^3 L=4 and
     Ishikawa 2D 1024^2 L=8 (cc 0.3, steps 0.11 / 0.16).  Per workload: 100
@@ -339,16 +403,17 @@ def configs_run(ctx) -> list:
     cs2, ct2, a2 = synth.binary2d(seed=0)
     ct3, a3 = synth.potts3d(seed=0)
     cti, ai = synth.ishikawa2d(seed=0)
-    # name, model, dims, labels, inputs, steps, maxIt, bytes per voxel-iteration
+    # name, model, dims, labels, inputs, steps, maxIt, bytes per voxel-iteration,
+    # iterations of the single-thread CPU sample
     table = (
-        ("binary2d_256^2", "binary", cs2.shape, 1, (ct2, a2, cs2), 0.16, 300, 52),
+        ("binary2d_256^2", "binary", cs2.shape, 1, (ct2, a2, cs2), 0.16, 300, 52, 300),
         ("potts3d_192^3_L4", "potts", ct3.shape[:3], ct3.shape[3], (ct3, a3), 0.11, 2000,
-         48 * ct3.shape[3] + 8),
+         48 * ct3.shape[3] + 8, 4),
         ("ishikawa2d_1024^2_L8", "ishikawa", cti.shape[:2], cti.shape[2], (cti, ai), 0.16, 2000,
-         (4 * cti.shape[2] - 3) * 8 + (2 * cti.shape[2] - 1) * 4),
+         (4 * cti.shape[2] - 3) * 8 + (2 * cti.shape[2] - 1) * 4, 20),
     )
     fixed = 100
-    for name, model, dims, L, inputs, steps_, max_it, bpv in table:
+    for name, model, dims, L, inputs, steps_, max_it, bpv, cpu_its in table:
         s = N.Solver(ctx, model, dims, L) if model != "binary" else N.Solver(ctx, model, dims)
         s.set_inputs(*inputs)
         nvox = int(np.prod(dims))
@@ -367,6 +432,9 @@ def configs_run(ctx) -> list:
                                   "peak_kind": peak_kind},
                      "err_bound": 1e-4, "max_it": max_it, "itnum": it,
                      "ms_to_errbound": conv_ms})
+        if cpu:
+            rows[-1]["cpu_baseline"] = config_cpu_baseline(model, dims, L, inputs, steps_,
+                                                            cpu_its)
         s.close()
     return rows
 
@@ -608,10 +676,11 @@ def run_reference(args, rank, pg):
     from oracle import oracle as O
 
     cs, ct, alpha = synth.binary3d(seed=0, shape=SHAPE)
-    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    # per core per step: a bounded sample of the 200-iteration run, long
-    # enough that the per-call allocation and init do not dominate it
-    iters = 8
+    cores = host_cores()
+    # per core per step: a bounded sample of the 200-iteration run; at 32
+    # iterations the per-call allocation and init (as in the reference's own
+    # call) are about 3% of it
+    iters = 32
 
     def one(_):
         O.solve("binary", SHAPE, ct, alpha, cs=cs, max_it=iters, err_bound=0.0, cc=CC, steps=STEPS)
@@ -632,7 +701,7 @@ def run_reference(args, rank, pg):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "shape": list(SHAPE), "cc": CC, "steps": STEPS},
+        "config": workload_config(args.gpus),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -741,8 +810,9 @@ def main():
     e2e_value = world * nvox * ITERS * args.steps / e2e_s / 1e9
     ok = bool(np.isfinite(h_u.numpy()).all())
 
-    batch = None if args.no_batch else batch_run(ctx)
-    configs = configs_run(ctx) if (rank == 0 and not args.no_configs) else None
+    cpu_on = rank == 0 and not args.no_cpu_baseline
+    batch = None if args.no_batch else batch_run(ctx, cpu_on)
+    configs = configs_run(ctx, cpu_on) if (rank == 0 and not args.no_configs) else None
     warm = warm_start_run(ctx, args.warm_seeds) if (rank == 0 and args.warm_seeds > 0) else None
     nxt = next_rows_run(ctx, stream, not args.no_cpu_baseline) \
         if (rank == 0 and not args.no_next) else None
@@ -757,11 +827,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "model": "binary continuous max-flow 3D",
-                       "shape": list(SHAPE), "iterations_per_step": ITERS, "cc": CC,
-                       "steps": STEPS, "err_bound": 0.0, "parallelism": f"replicas{world}",
-                       "l2": "working set ~1 GB per iteration, larger than L2; no flush",
-                       "voronoi_cells": 40, "intensities": [0.25, 0.75], "noise": 0.2},
+            "config": workload_config(world),
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": 3 * nvox * 4, "d2h_bytes_per_step": nvox * 4 + ITERS * 4},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -6,7 +6,9 @@ Produces
                                   (maxflow/asets*_mex.c), compiled from where
                                   they lie, against the package's mex host
                                   emulation (mex.h + libmexshim.so); only when
-                                  the reference tree is present.
+                                  the reference tree is present
+                                  ($ASETS_REFERENCE_DIR, or ../reference
+                                  beside the repository).
 
 Both are compiled with -ffp-contract=off: on x86-64 this is what gcc does
 anyway (no FMA without -mfma), and on aarch64 it stops gcc from fusing a*b+c,
@@ -25,7 +27,9 @@ HERE = Path(__file__).resolve().parent
 REPO = HERE.parent
 BUILD = HERE / "_build"
 REF_OUT = HERE / "_ref"
-REF_SRC = Path(os.environ.get("ASETS_REFERENCE_DIR", "/root/reference")) / "maxflow"
+# The reference tree: $ASETS_REFERENCE_DIR, else a checkout named `reference`
+# beside this repository.
+REF_SRC = Path(os.environ.get("ASETS_REFERENCE_DIR", REPO.parent / "reference")) / "maxflow"
 
 REF_SOLVERS = (
     "asetsBinaryMF2D_mex",
