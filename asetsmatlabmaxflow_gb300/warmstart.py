@@ -30,6 +30,7 @@ judges the warm labelling (label agreement).
 """
 from __future__ import annotations
 
+import json
 import time
 from dataclasses import dataclass, field
 from pathlib import Path
@@ -380,6 +381,103 @@ def evaluate_batched(net: N.WarmStartNet, cold_budget: int, seeds, *, level: int
             "agree_cold_mean": float(np.mean(agree)), "agree_cold_min": float(min(agree))}
 
 
+def potts_energy(ct, alpha_full, u, shape, L: int = LABELS) -> float:
+    """Relaxed Potts energy of a labelling function u (torch, Matlab layout,
+    label slowest), in float64: sum over labels and voxels of u_l Ct_l plus
+    alpha_l times the per-voxel gradient norm sqrt(0.5 * sum of the squared
+    differences across the voxel's 2*dim faces), the norm the solver's
+    projection bounds the flows with (|p| <= alpha,
+    maxflow/asetsPotts3D_mex.c:342-374); faces on the volume's border carry
+    no difference.  A one-hot u gives the discrete Potts energy of its
+    labelling."""
+    ny, nx, nz = shape
+    U = u.reshape(L, nz, nx, ny).double()
+    data = float((U * ct.reshape(L, nz, nx, ny).double()).sum())
+    g2 = U.new_zeros(U.shape)
+    for d in (1, 2, 3):
+        if U.shape[d] < 2:
+            continue
+        f2 = U.diff(dim=d) ** 2
+        n = U.shape[d]
+        g2.narrow(d, 0, n - 1).add_(f2)
+        g2.narrow(d, 1, n - 1).add_(f2)
+    tv = float((alpha_full.reshape(L, nz, nx, ny).double() * (0.5 * g2).sqrt()).sum())
+    return data + tv
+
+
+def one_hot(lab, n: int, L: int = LABELS):
+    """Labels (n,) -> a one-hot u in Matlab layout (label slowest)."""
+    import torch
+
+    return torch.nn.functional.one_hot(lab, L).T.reshape(-1).float()
+
+
+def diagnose(net: N.WarmStartNet, seeds, *, level: int = LEVELS - 1, run: Runner | None = None,
+             log=None) -> list[dict]:
+    """Per held-out problem: why the warm-started labelling differs from the
+    cold one.  Solves cold and warm (learned coarsest state, coarse to fine)
+    to errBound 1e-4 and to 1e-5, and reports for each of the four results
+    the relaxed Potts energy of u and the discrete energy of its argmax
+    labelling, with the label agreements, the smallest gap between two label
+    means, the share of voxels whose cold top-two u margin exceeds 0.1 and
+    the agreement on them, and the label pair that accounts for most of the
+    disagreement."""
+    import torch
+
+    own = run is None
+    run = run or Runner()
+    n, L = run.n, run.L
+    out = []
+    for sd in seeds:
+        means = synth.potts_warmstart_draws(sd)[0]
+        ct, a1, af = problem(sd)
+        run.load(ct, af)
+        lv = run.lv[level]
+        res = {}
+        for err, tag in ((EVAL_ERR, "4"), (TRAIN_ERR, "5")):
+            it_c = run.cold(err)
+            u_c = run.lv[0].read_state()[0].clone()
+            net.predict(lv.shape, lv.ct, lv.alpha, *lv.state)
+            it_w, _ = run.multilevel(err, MAX_IT, lv.state)
+            u_w = run.lv[0].read_state()[0].clone()
+            res[tag] = (it_c, u_c, it_w, u_w)
+        r = {"seed": int(sd), "alpha": float(a1[0]),
+             "means": [round(float(m), 4) for m in means],
+             "min_mean_gap": float(np.min(np.diff(np.sort(means))))}
+        labs = {}
+        for tag, (it_c, u_c, it_w, u_w) in res.items():
+            lc, lw = labels(u_c, n, L), labels(u_w, n, L)
+            labs["c" + tag], labs["w" + tag] = lc, lw
+            r[f"cold{tag}_it"], r[f"warm{tag}_it"] = int(it_c), int(it_w)
+            r[f"cold{tag}_E"] = potts_energy(ct, af, u_c, run.shape, L)
+            r[f"warm{tag}_E"] = potts_energy(ct, af, u_w, run.shape, L)
+            r[f"cold{tag}_Elab"] = potts_energy(ct, af, one_hot(lc, n, L), run.shape, L)
+            r[f"warm{tag}_Elab"] = potts_energy(ct, af, one_hot(lw, n, L), run.shape, L)
+            r[f"agree{tag}"] = float((lc == lw).float().mean())
+        r["cold4_vs_cold5"] = float((labs["c4"] == labs["c5"]).float().mean())
+        r["warm4_vs_cold5"] = float((labs["w4"] == labs["c5"]).float().mean())
+        top2 = res["4"][1].view(L, n).topk(2, dim=0).values
+        conf = (top2[0] - top2[1]) > 0.1
+        r["confident_share"] = float(conf.float().mean())
+        r["agree4_confident"] = float((labs["c4"] == labs["w4"])[conf].float().mean()) \
+            if bool(conf.any()) else float("nan")
+        diff = labs["c4"] != labs["w4"]
+        if bool(diff.any()):
+            pair = labs["c4"][diff] * L + labs["w4"][diff]
+            cnt = torch.bincount(pair, minlength=L * L)
+            k = int(cnt.argmax())
+            a, b = divmod(k, L)
+            r["top_pair"] = [a, b]
+            r["top_pair_share"] = float(cnt[k]) / float(diff.sum())
+            r["top_pair_gap"] = float(abs(means[a] - means[b]))
+        out.append(r)
+        if log:
+            log(json.dumps(r))
+    if own:
+        run.close()
+    return out
+
+
 def summarize(res: list[EvalResult]) -> dict:
     c_it = np.array([r.cold_it for r in res], float)
     w_it = np.array([r.warm_its[0] + (r.cold_it if r.fallback else 0) for r in res], float)
@@ -439,7 +537,6 @@ def _summary_1e5(res) -> dict:
 def main(argv=None):
     """python -m asetsmatlabmaxflow_gb300.warmstart --train N --eval M"""
     import argparse
-    import json
 
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", type=int, default=2000, help="training pairs (seeds 0..N-1)")
@@ -451,7 +548,17 @@ def main(argv=None):
     ap.add_argument("--no-tight", action="store_true")
     ap.add_argument("--eval-only", action="store_true")
     ap.add_argument("--results", type=Path, default=None, help="per-seed results (JSON)")
+    ap.add_argument("--diagnose", action="store_true",
+                    help="per-seed energies and agreements of cold and warm solves "
+                         "(committed weights)")
     a = ap.parse_args(argv)
+    if a.diagnose:
+        net, budget, level = load(path=a.out)
+        rows = diagnose(net, range(HELDOUT_SEED0, HELDOUT_SEED0 + a.eval), level=level,
+                        log=print)
+        if a.results:
+            a.results.write_text(json.dumps(rows, indent=1))
+        return
     if a.eval_only:
         net, budget, level = load(path=a.out)
     else:

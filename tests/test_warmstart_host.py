@@ -25,3 +25,37 @@ def test_summary_counts_fallback_iterations():
     assert s["coarsest_iters_learned_mean"] == 90 and s["coarsest_iters_cold_start_mean"] == 200
     assert abs(s["wall_ratio_cold_over_warm"] - 240 / 275) < 1e-12
     assert abs(s["wall_ratio_cold_over_multilevel"] - 4.0) < 1e-12
+
+
+def test_potts_energy_matches_a_direct_sum():
+    """The relaxed Potts energy used to compare warm and cold solutions, on a
+    small random u, against a loop over voxels and faces."""
+    import numpy as np
+    import torch
+
+    from asetsmatlabmaxflow_gb300 import warmstart as W
+
+    L, shape = 2, (3, 4, 2)
+    ny, nx, nz = shape
+    n = ny * nx * nz
+    g = np.random.default_rng(0)
+    u = torch.tensor(g.random(n * L), dtype=torch.float32)
+    ct = torch.tensor(g.random(n * L), dtype=torch.float32)
+    a = torch.full((n * L,), 0.3)
+    U = u.numpy().reshape(L, nz, nx, ny).astype(np.float64)
+    C = ct.numpy().reshape(L, nz, nx, ny)
+    tot = float((U * C).sum())
+    for l in range(L):
+        for z in range(nz):
+            for x in range(nx):
+                for y in range(ny):
+                    s = 0.0
+                    for dz, dx, dy in ((1, 0, 0), (0, 1, 0), (0, 0, 1)):
+                        for sg in (1, -1):
+                            zz, xx, yy = z + sg * dz, x + sg * dx, y + sg * dy
+                            if 0 <= zz < nz and 0 <= xx < nx and 0 <= yy < ny:
+                                s += (U[l, zz, xx, yy] - U[l, z, x, y]) ** 2
+                    tot += 0.3 * np.sqrt(0.5 * s)
+    assert abs(W.potts_energy(ct, a, u, shape, L) - tot) < 1e-9 * max(1.0, abs(tot))
+    oh = W.one_hot(torch.tensor([0, 1, 1]), 3, 2)
+    assert oh.tolist() == [1.0, 0.0, 0.0, 0.0, 1.0, 1.0]
