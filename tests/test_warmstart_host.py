@@ -41,7 +41,7 @@ def test_potts_energy_matches_a_direct_sum():
     g = np.random.default_rng(0)
     u = torch.tensor(g.random(n * L), dtype=torch.float32)
     ct = torch.tensor(g.random(n * L), dtype=torch.float32)
-    a = torch.full((n * L,), 0.3)
+    a = torch.full((n * L,), 0.25)
     U = u.numpy().reshape(L, nz, nx, ny).astype(np.float64)
     C = ct.numpy().reshape(L, nz, nx, ny)
     tot = float((U * C).sum())
@@ -55,7 +55,7 @@ def test_potts_energy_matches_a_direct_sum():
                             zz, xx, yy = z + sg * dz, x + sg * dx, y + sg * dy
                             if 0 <= zz < nz and 0 <= xx < nx and 0 <= yy < ny:
                                 s += (U[l, zz, xx, yy] - U[l, z, x, y]) ** 2
-                    tot += 0.3 * np.sqrt(0.5 * s)
+                    tot += 0.25 * np.sqrt(0.5 * s)
     assert abs(W.potts_energy(ct, a, u, shape, L) - tot) < 1e-9 * max(1.0, abs(tot))
     oh = W.one_hot(torch.tensor([0, 1, 1]), 3, 2)
     assert oh.tolist() == [1.0, 0.0, 0.0, 0.0, 1.0, 1.0]
