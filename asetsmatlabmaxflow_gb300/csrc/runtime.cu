@@ -16,8 +16,20 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "asets.h"
 #include "internal.h"
+
+// NVTX range for profilers (a no-op unless a tool is attached): solves,
+// batches, multilevel levels, autotuning and each CUDA-graph iteration chunk
+// show up on the timeline under these names.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 using namespace asets;
 
@@ -979,7 +991,10 @@ static asets_status run_chunks(asets_context *ctx, cudaGraphExec_t exec, int max
             if ((unsigned int)flags_h[chunk % 2] >= done_target)
                 break;
         }
-        CU_TRY(cudaGraphLaunch(exec, st));
+        {
+            NvtxRange r("asets iteration chunk");
+            CU_TRY(cudaGraphLaunch(exec, st));
+        }
         launched += kGraphIters;
         CU_TRY(cudaMemcpyAsync(&flags_h[chunk % 2], done_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
         CU_TRY(cudaEventRecord(flag_ev[chunk % 2], st));
@@ -1014,6 +1029,7 @@ static std::vector<std::pair<std::string, int>> g_solver_tune;
 static asets_status solver_autotune(asets_solver *s, int flags, float cc, float steps,
                                     int *tile_config)
 {
+    NvtxRange nv("asets autotune");
     const int exact = (flags & ASETS_FLAG_EXACT) ? 1 : 0;
     char key[128];
     snprintf(key, sizeof key, "model%d/%dx%dx%d/L%d/exact%d", (int)s->model, s->ny, s->nx, s->nz,
@@ -1068,6 +1084,7 @@ extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_
         return fail(ASETS_ERR_INVALID_ARG, "inputs not set");
     const int flags = opt ? opt->flags : 0;
     std::lock_guard<std::recursive_mutex> lock(s->ctx->mu);
+    NvtxRange nv("asets_solver_run");
     DeviceGuard guard(s->ctx->device);
     cudaStream_t st = s->ctx->stream;
     int tile_config = opt ? opt->tile_config : 0;
@@ -1301,6 +1318,7 @@ extern "C" ASETS_API asets_status asets_solver_run_multilevel(asets_solver *s,
         lv[k] = lv[k - 1]->coarse;
     s->ml_levels = 0;
     for (int k = built - 1; k >= 0; --k) {
+        NvtxRange nv("asets multilevel level");
         asets_solver *cur = lv[k];
         if (k < built - 1 && (st = ml_prolong(lv[k + 1], cur)) != ASETS_OK)
             return st;
@@ -1608,6 +1626,7 @@ static std::vector<std::pair<std::string, int>> g_tune_cache;
 
 static asets_status batch_autotune(asets_batch *b, int flags, float cc, float steps, int tile_config[4])
 {
+    NvtxRange nv("asets batch autotune");
     const int exact = (flags & ASETS_FLAG_EXACT) ? 1 : 0;
     for (int gi = 0; gi < 4; ++gi) {
         long long vox = 0;
@@ -1677,6 +1696,7 @@ extern "C" ASETS_API asets_status asets_batch_run(asets_batch *b, const asets_op
     const int flags = opt ? opt->flags : 0;
     std::lock_guard<std::recursive_mutex> lock(b->ctx->mu);
     DeviceGuard guard(b->ctx->device);
+    NvtxRange nv("asets_batch_run");
     cudaStream_t st = b->ctx->stream;
     // one kernel variant per dimension group (default: the first)
     const int tc0 = (opt && opt->tile_config > 0) ? opt->tile_config : 1;
