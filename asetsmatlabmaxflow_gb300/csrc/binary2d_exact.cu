@@ -1,11 +1,13 @@
 // Compiled instances of the fused iteration kernel for the binary model (ps/pt/u
-// epilogue), 2D tiles 224-row, 56-row; EXACT projection, built with the reference's
+// epilogue), 2D tiles 240-row (two rows per thread), 224-row, 56-row; EXACT projection, built with the reference's
 // float arithmetic (no FMA contraction, no flush to zero).
 #include "variants.cuh"
 
 namespace asets {
 
 static const StencilVariant kVariants[] = {
+    // two rows per thread, 240-row tiles, 6 stages, unrolled by 4
+    make_variant<2, 4, 6, EPI_BINARY, true, 4, 4, 2>(),
     make_variant<2, 8, 4, EPI_BINARY, true>(),
     make_variant<2, 2, 4, EPI_BINARY, true>(),
 };

@@ -109,31 +109,124 @@ __device__ __forceinline__ void tma_prefetch_desc(const CUtensorMap *map)
 template <bool EXACT>
 struct Proj;
 
+// The reference's norm rounded to float, fpt = (float)sqrt(0.5 * s) with s
+// the double sum of the N squared face flows in order, computed in float.
+// The exact sum of squares is formed as an unevaluated pair hi + lo (each
+// square split exactly by FMA, the sums by TwoSum -- Knuth's error-free
+// addition -- with the error terms added into lo; |hi + lo - S| <= 2^-40 S
+// for N <= 6), renormalised so that |lo| <= ulp(hi)/2.  Then
+// y0 = RN(sqrt(hi/2)) lies within one ulp of sqrt(S/2), its residual
+// hi/2 - y0^2 is exact under FMA, and d ~ sqrt(S/2) - y0 to within 2^-17 of
+// an ulp of y0, which picks y0 or a neighbour.  The double computation lies
+// within 4 * 2^-53 (relative) of sqrt(S/2), so both round to the same float
+// unless sqrt(S/2) is within 2^-12 of half a spacing of a rounding midpoint
+// (below a power of two the spacing halves); then, and for sums outside
+// [2^-60, 2^120], it returns false and the caller takes the double path.
+// About 2^-12 of the evaluations near capacity do.
+template <int N>
+__device__ __forceinline__ bool ref_norm_f32(const float (&f)[N], float &out)
+{
+    float hi = __fmul_rn(f[0], f[0]);
+    float lo = __fmaf_rn(f[0], f[0], -hi);
+#pragma unroll
+    for (int i = 1; i < N; ++i) {
+        const float ph = __fmul_rn(f[i], f[i]);
+        const float pl = __fmaf_rn(f[i], f[i], -ph);
+        const float sum = __fadd_rn(hi, ph);
+        const float bv = __fsub_rn(sum, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bv)), __fsub_rn(ph, bv));
+        hi = sum;
+        lo = __fadd_rn(lo, __fadd_rn(pl, err));
+    }
+    if (!(hi >= 0x1p-60f && hi <= 0x1p120f))
+        return false;
+    {
+        // renormalise (Fast2Sum, exact as |hi| >= |lo|)
+        const float s2 = __fadd_rn(hi, lo);
+        lo = __fsub_rn(lo, __fsub_rn(s2, hi));
+        hi = s2;
+    }
+    const float h2 = __fmul_rn(hi, 0.5f);
+    const float y0 = __fsqrt_rn(h2);
+    const float r = __fadd_rn(__fmaf_rn(-y0, y0, h2), __fmul_rn(lo, 0.5f));
+    const float d = __fmul_rn(__fmul_rn(r, 0.5f), __frcp_rn(y0));
+    const int yb = __float_as_int(y0);
+    const float up = __int_as_float(yb + 1);
+    // half the spacing to the neighbour on d's side
+    float hs = __fmul_rn(__fsub_rn(up, y0), 0.5f);
+    if (d < 0.0f && (yb & 0x7fffff) == 0)
+        hs = __fmul_rn(hs, 0.5f);
+    const float ad = fabsf(d);
+    if (fabsf(__fsub_rn(ad, hs)) <= __fmul_rn(hs, 0x1p-12f))
+        return false;  // too close to a midpoint to decide in float
+    out = (ad < hs) ? y0 : __int_as_float(d > 0.0f ? yb + 1 : yb - 1);
+    return true;
+}
+
+// The reference's fpt from its own double computation (the undecided
+// cases of ref_norm_f32).  Not inlined, so that the compiler cannot hoist its
+// conversions and double additions out of the rare branch that needs them.
+template <int N>
+__device__ __noinline__ float ref_norm_f64(const float *f)
+{
+    double s = (double)f[0] * (double)f[0];
+    for (int i = 1; i < N; ++i)
+        s = s + (double)f[i] * (double)f[i];
+    return (float)__dsqrt_rn(s * 0.5);
+}
+
 template <>
 struct Proj<true> {
+    // Most voxels are far inside the constraint |p| <= alpha, where the
+    // reference's factor is exactly 1 (fpt <= alpha).  A float sum of the
+    // squares (relative error below 7 * 2^-24) decides that case: if
+    // 0.5 * s * (1 + 2^-16) < alpha^2 in float, the double |p| of the
+    // reference is below alpha as well (the margin exceeds both sums'
+    // rounding), so its float fpt is <= alpha and the factor is 1.  The
+    // other voxels -- the flow at or near its capacity -- get the
+    // reference's float fpt from ref_norm_f32, or in the rare undecidable
+    // cases from the reference's own double computation: the same bits as
+    // the reference, mostly at FP32 cost.
+    __device__ __forceinline__ static bool surely_inside(float s, float alpha)
+    {
+        const float lhs = __fmul_rn(__fmul_rn(s, 0.5f), 1.0f + 0x1p-16f);
+        return lhs < __fmul_rn(alpha, alpha);
+    }
+    template <int N>
+    __device__ __forceinline__ static float factor(const float (&f)[N], float alpha)
+    {
+        float sf = __fmul_rn(f[0], f[0]);
+#pragma unroll
+        for (int i = 1; i < N; ++i)
+            sf = __fmaf_rn(f[i], f[i], sf);
+        // All faces zero: fpt = 0 is not above alpha >= 0, so the factor is 1.
+        // This is also every cell outside the volume (zero flows and zero
+        // alpha from the tile loads' out-of-range fill).
+        if (sf == 0.0f && alpha >= 0.0f)
+            return 1.0f;
+        if (surely_inside(sf, alpha))
+            return 1.0f;
+        float fpt;
+        if (!ref_norm_f32<N>(f, fpt))
+            fpt = ref_norm_f64<N>(f);
+        return finish(fpt, alpha);
+    }
     // faces in the reference's summation order
     __device__ __forceinline__ static float gk(float f0, float f1, float f2, float f3, float alpha)
     {
-        double s = (double)f0 * (double)f0;
-        s = s + (double)f1 * (double)f1;
-        s = s + (double)f2 * (double)f2;
-        s = s + (double)f3 * (double)f3;
-        return finish(s, alpha);
+        const float f[4] = {f0, f1, f2, f3};
+        return factor<4>(f, alpha);
     }
     __device__ __forceinline__ static float gk(float f0, float f1, float f2, float f3, float f4,
                                                float f5, float alpha)
     {
-        double s = (double)f0 * (double)f0;
-        s = s + (double)f1 * (double)f1;
-        s = s + (double)f2 * (double)f2;
-        s = s + (double)f3 * (double)f3;
-        s = s + (double)f4 * (double)f4;
-        s = s + (double)f5 * (double)f5;
-        return finish(s, alpha);
+        const float f[6] = {f0, f1, f2, f3, f4, f5};
+        return factor<6>(f, alpha);
     }
-    __device__ __forceinline__ static float finish(double s, float alpha)
+    // fpt -> 1 / (fpt / alpha) when fpt > alpha, else 1, in float as the
+    // reference (maxflow/asetsBinaryMF3D_mex.c:317-331)
+    __device__ __forceinline__ static float finish(float fpt, float alpha)
     {
-        float fpt = (float)__dsqrt_rn(s * 0.5);
         fpt = (fpt > alpha) ? __fdiv_rn(fpt, alpha) : 1.0f;
         return __fdiv_rn(1.0f, fpt);
     }

@@ -1378,6 +1378,7 @@ struct asets_batch {
     std::vector<asets_solver *> members;
     struct Group {
         std::vector<int> idx;  // members of this group
+        std::vector<int> live; // members in the current layout (not yet retired)
         const StencilVariant *v = nullptr;
         ProblemDesc *d_desc = nullptr;
         int desc_cap = 0;
@@ -1389,6 +1390,10 @@ struct asets_batch {
         int tile_config = 0;
     } groups[4];  // [0] binary 2D, [1] binary 3D, [2] labelled 2D, [3] labelled 3D
     unsigned int *d_done = nullptr;
+    IterControl **d_ctls = nullptr;  // every member's control block
+    int *d_member_done = nullptr;    // gathered done flags
+    int *h_member_done = nullptr;    // pinned copy
+    int ctls_cap = 0;
     ChunkGraph graph;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, flag_ev[2] = {nullptr, nullptr};
     std::vector<void *> allocations;
@@ -1438,6 +1443,8 @@ extern "C" ASETS_API void asets_batch_destroy(asets_batch *b)
     b->graph.reset();
     for (void *p : b->allocations)
         cudaFree(p);
+    if (b->h_member_done)
+        cudaFreeHost(b->h_member_done);
     for (cudaEvent_t e : {b->ev0, b->ev1, b->flag_ev[0], b->flag_ev[1]})
         if (e)
             cudaEventDestroy(e);
@@ -1484,28 +1491,79 @@ static asets_status batch_buffer(asets_batch *b, void **p, size_t bytes)
     return ASETS_OK;
 }
 
-// Lay out one group's descriptors and item map for a run.
+static StencilProblem item_geometry(const asets_solver *s)
+{
+    StencilProblem sp;
+    memset(&sp, 0, sizeof sp);
+    sp.nr = s->nr;
+    sp.nc = s->nc;
+    sp.ns = s->ns;
+    sp.flow_labels = s->flow_labels;
+    return sp;
+}
+
+// Stream-axis chunk counts for the problems of one launch: one common chunk
+// length (planes per item) for all of them, the one with the best
+// (wave fill of `slots` resident blocks) x (useful planes / swept planes,
+// each chunk sweeping 4 warm-up planes).  Many live problems keep long
+// chunks; a few left iterating (the tail of a batch) get short ones, so
+// their items still spread over every SM.
+static std::vector<int> choose_batch_chunks(const std::vector<asets_solver *> &live,
+                                            const StencilVariant &v, long long slots)
+{
+    static const int kLengths[] = {8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256, 512, 1024, 4096};
+    std::vector<int> best(live.size(), 1), cur(live.size(), 1);
+    double best_eff = -1.0;
+    for (int len : kLengths) {
+        long long items = 0;
+        double useful = 0.0, swept = 0.0;
+        for (size_t j = 0; j < live.size(); ++j) {
+            const asets_solver *s = live[j];
+            const int max_k = std::max(1, s->ns / 8);
+            const int k = std::min(max_k, std::max(1, (s->ns + len / 2) / len));
+            cur[j] = k;
+            const long long it = problem_items(item_geometry(s), v, k);
+            items += it;
+            useful += (double)it / k * s->ns;
+            swept += (double)it / k * (s->ns + 4.0 * k);
+        }
+        if (items < 1)
+            continue;
+        const long long waves = (items + slots - 1) / slots;
+        const double eff = ((double)items / (double)(waves * slots)) * (useful / swept);
+        if (eff > best_eff + 1e-9) {
+            best_eff = eff;
+            best = cur;
+        }
+    }
+    return best;
+}
+
+// Lay out one group's descriptors and item map for a run, over the members
+// in g.live (all of the group's members at the start of a run; the ones
+// still iterating when the batch re-lays itself out).
 static asets_status batch_layout(asets_batch *b, asets_batch::Group &g)
 {
-    if (g.idx.empty())
+    if (g.live.empty())
         return ASETS_OK;
+    int per_sm = 0;
+    CU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g.v->fn, g.v->nt,
+                                                         g.v->smem_bytes));
+    const long long slots = (long long)b->ctx->num_sms * std::max(per_sm, 1);
+    std::vector<asets_solver *> live;
+    for (int i : g.live)
+        live.push_back(b->members[i]);
+    const std::vector<int> zc = choose_batch_chunks(live, *g.v, slots);
     std::vector<ProblemDesc> descs;
     std::vector<int> item_problem;
-    for (size_t j = 0; j < g.idx.size(); ++j) {
-        asets_solver *s = b->members[g.idx[j]];
-        ProblemDesc d = s->desc;
-        // chunks of about 64 planes: the batch already fills the GPU.  The
-        // batch's layout lives only in its own descriptor copy `d`: the
+    for (size_t j = 0; j < live.size(); ++j) {
+        asets_solver *s = live[j];
+        // The batch's layout lives only in its own descriptor copy `d`: the
         // member's descriptor keeps its single-solve layout, which a later
         // solve of the member alone uploads as it is.
-        d.zchunks = std::max(1, (s->ns + 32) / 64);
-        StencilProblem sp;
-        memset(&sp, 0, sizeof sp);
-        sp.nr = s->nr;
-        sp.nc = s->nc;
-        sp.ns = s->ns;
-        sp.flow_labels = s->flow_labels;
-        const int items = problem_items(sp, *g.v, d.zchunks);
+        ProblemDesc d = s->desc;
+        d.zchunks = zc[j];
+        const int items = problem_items(item_geometry(s), *g.v, d.zchunks);
         asets_status st = ensure_items(s, items);
         if (st != ASETS_OK)
             return st;
@@ -1537,10 +1595,6 @@ static asets_status batch_layout(asets_batch *b, asets_batch::Group &g)
     CU_TRY(cudaMemcpyAsync(g.d_item_problem, item_problem.data(), sizeof(int) * item_problem.size(),
                            cudaMemcpyHostToDevice, st));
     CU_TRY(cudaStreamSynchronize(st));  // host vectors go out of scope
-    int per_sm = 0;
-    CU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g.v->fn, g.v->nt,
-                                                         g.v->smem_bytes));
-    const long long slots = (long long)b->ctx->num_sms * std::max(per_sm, 1);
     g.grid = (int)std::min<long long>((long long)item_problem.size(), slots);
     g.bargs.probs = g.d_desc;
     g.bargs.item_problem = g.d_item_problem;
@@ -1554,7 +1608,7 @@ static cudaError_t batch_launch_iteration(asets_batch *b)
 {
     for (int gi = 0; gi < 4; ++gi) {
         auto &g = b->groups[gi];
-        if (g.idx.empty())
+        if (g.live.empty())
             continue;
         void *params[] = {&g.bargs};
         cudaError_t e = cudaLaunchKernel(g.v->fn, dim3(g.grid), dim3(g.v->nt), params,
@@ -1565,7 +1619,7 @@ static cudaError_t batch_launch_iteration(asets_batch *b)
             continue;
         // labelled models: each problem's label kernel closes its iteration
         // (it returns at once for a finished problem) and counts it when done
-        for (int i : g.idx) {
+        for (int i : g.live) {
             asets_solver *s = b->members[i];
             LabelArgs la = label_args(s);
             la.done_count = b->d_done;
@@ -1601,7 +1655,32 @@ static asets_status batch_prepare(asets_batch *b, int flags, const int tile_conf
     }
     cudaStream_t st = b->ctx->stream;
     CU_TRY(cudaMemsetAsync(b->d_done, 0, kBatchCounters * sizeof(unsigned int), st));
+    const int nm = (int)b->members.size();
+    if (nm > b->ctls_cap) {
+        void *p = nullptr;
+        asets_status s2 = batch_buffer(b, &p, sizeof(IterControl *) * nm);
+        if (s2 != ASETS_OK)
+            return s2;
+        b->d_ctls = static_cast<IterControl **>(p);
+        if ((s2 = batch_buffer(b, &p, sizeof(int) * nm)) != ASETS_OK)
+            return s2;
+        b->d_member_done = static_cast<int *>(p);
+        if (b->h_member_done)
+            cudaFreeHost(b->h_member_done);
+        b->h_member_done = nullptr;
+        CU_TRY(cudaMallocHost(&b->h_member_done, sizeof(int) * nm));
+        b->ctls_cap = nm;
+    }
+    {
+        std::vector<IterControl *> ctls(nm);
+        for (int i = 0; i < nm; ++i)
+            ctls[i] = b->members[i]->ctl;
+        CU_TRY(cudaMemcpyAsync(b->d_ctls, ctls.data(), sizeof(IterControl *) * nm,
+                               cudaMemcpyHostToDevice, st));
+        CU_TRY(cudaStreamSynchronize(st));
+    }
     for (auto &g : b->groups) {
+        g.live = g.idx;
         asets_status s2 = batch_layout(b, g);
         if (s2 != ASETS_OK)
             return s2;
@@ -1609,14 +1688,101 @@ static asets_status batch_prepare(asets_batch *b, int flags, const int tile_conf
     return ASETS_OK;
 }
 
-static asets_status batch_execute(asets_batch *b, int maxIt, int *chunks)
+__global__ void gather_done_kernel(IterControl *const *ctls, int n, int *out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = *(const volatile int *)&ctls[i]->done;
+}
+
+// After members have retired: drop them from the layout of their group and
+// re-choose the live members' chunk counts (choose_batch_chunks), so that
+// the items of the problems still iterating cover the GPU again.  The
+// stream is drained first (the descriptors are rewritten).  *changed tells
+// whether a layout changed (the iteration chunk must be captured anew).
+static asets_status batch_relayout(asets_batch *b, bool *changed)
+{
+    *changed = false;
+    cudaStream_t st = b->ctx->stream;
+    const int nm = (int)b->members.size();
+    gather_done_kernel<<<1, 256, 0, st>>>(b->d_ctls, nm, b->d_member_done);
+    CU_TRY(cudaGetLastError());
+    CU_TRY(cudaMemcpyAsync(b->h_member_done, b->d_member_done, sizeof(int) * nm,
+                           cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    for (auto &g : b->groups) {
+        std::vector<int> live;
+        for (int i : g.live)
+            if (!b->h_member_done[i])
+                live.push_back(i);
+        if (live.size() == g.live.size())
+            continue;
+        g.live = live;
+        asets_status s2 = batch_layout(b, g);
+        if (s2 != ASETS_OK)
+            return s2;
+        *changed = true;
+    }
+    return ASETS_OK;
+}
+
+// Kernel launches of one iteration of the current layout: the flow pass of
+// each group, plus the label kernel of each live labelled member.
+static int batch_launches_per_iter(const asets_batch *b)
+{
+    int n = 0;
+    for (int gi = 0; gi < 4; ++gi)
+        if (!b->groups[gi].live.empty())
+            n += 1 + (gi >= 2 ? (int)b->groups[gi].live.size() : 0);
+    return n;
+}
+
+// Replay iteration chunks (as run_chunks) until every member is done or
+// maxIt launches are queued.  Whenever the done count read back has grown,
+// the retired members leave the layout (batch_relayout).  *chunks: chunks
+// replayed; *launches (may be NULL): the kernel launches they held.
+static asets_status batch_execute(asets_batch *b, int maxIt, int *chunks, int *launches)
 {
     cudaStream_t st = b->ctx->stream;
     asets_status ss = capture_chunk(b->graph, st, [&] { return batch_launch_iteration(b); });
     if (ss != ASETS_OK)
         return ss;
-    return run_chunks(b->ctx, b->graph.exec, maxIt, b->d_done, (unsigned int)b->members.size(),
-                      b->flag_ev, chunks);
+    const unsigned int target = (unsigned int)b->members.size();
+    int *flags_h = b->ctx->pinned_flags;
+    unsigned int seen = 0;
+    int launched = 0, chunk = 0, kernels = 0;
+    while (launched < maxIt) {
+        if (chunk >= 2) {
+            CU_TRY(cudaEventSynchronize(b->flag_ev[chunk % 2]));
+            const unsigned int done = (unsigned int)flags_h[chunk % 2];
+            if (done >= target)
+                break;
+            if (done > seen) {
+                seen = done;
+                bool changed = false;
+                if ((ss = batch_relayout(b, &changed)) != ASETS_OK)
+                    return ss;
+                if (changed) {
+                    ss = capture_chunk(b->graph, st, [&] { return batch_launch_iteration(b); });
+                    if (ss != ASETS_OK)
+                        return ss;
+                }
+            }
+        }
+        {
+            NvtxRange r("asets batch iteration chunk");
+            CU_TRY(cudaGraphLaunch(b->graph.exec, st));
+        }
+        launched += kGraphIters;
+        kernels += kGraphIters * batch_launches_per_iter(b);
+        CU_TRY(cudaMemcpyAsync(&flags_h[chunk % 2], b->d_done, sizeof(int),
+                               cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaEventRecord(b->flag_ev[chunk % 2], st));
+        ++chunk;
+    }
+    *chunks = chunk;
+    if (launches)
+        *launches = kernels;
+    return ASETS_OK;
 }
 
 // Tile configuration per dimension group, chosen by timing each candidate
@@ -1664,7 +1830,7 @@ static asets_status batch_autotune(asets_batch *b, int flags, float cc, float st
                 return st;
             int chunks = 0;
             CU_TRY(cudaEventRecord(b->ev0, b->ctx->stream));
-            st = batch_execute(b, kGraphIters, &chunks);
+            st = batch_execute(b, kGraphIters, &chunks, nullptr);
             if (st != ASETS_OK)
                 return st;
             CU_TRY(cudaEventRecord(b->ev1, b->ctx->stream));
@@ -1710,9 +1876,9 @@ extern "C" ASETS_API asets_status asets_batch_run(asets_batch *b, const asets_op
     if (ss != ASETS_OK)
         return ss;
     CU_TRY(cudaEventRecord(b->ev0, st));
-    int chunks = 0;
+    int chunks = 0, launches = 0;
     if (maxIt > 0) {
-        ss = batch_execute(b, maxIt, &chunks);
+        ss = batch_execute(b, maxIt, &chunks, &launches);
         if (ss != ASETS_OK)
             return ss;
     }
@@ -1725,11 +1891,7 @@ extern "C" ASETS_API asets_status asets_batch_run(asets_batch *b, const asets_op
     float ms = 0.f;
     CU_TRY(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
     b->last_ms = ms;
-    int per_iter = 0;  // flow passes, plus the labelled members' label kernels
-    for (int gi = 0; gi < 4; ++gi)
-        if (!b->groups[gi].idx.empty())
-            per_iter += 1 + (gi >= 2 ? (int)b->groups[gi].idx.size() : 0);
-    b->last_launches = chunks * kGraphIters * per_iter;
+    b->last_launches = launches;  // flow passes, plus the labelled members' label kernels
     b->groups[0].tile_config = tile_config[0];
     b->groups[1].tile_config = tile_config[1];
     for (size_t i = 0; i < b->members.size(); ++i) {

@@ -32,6 +32,35 @@ def test_reciprocal_division_is_correctly_rounded_for_all_dividends(div_lib, d):
     assert m.value == 0, f"{m.value} mismatches, first dividend bits {f.value:#010x}"
 
 
+@pytest.fixture(scope="module")
+def norm_lib(tmp_path_factory):
+    from asetsmatlabmaxflow_gb300 import build
+
+    out = tmp_path_factory.mktemp("normcheck") / "libnormcheck.so"
+    subprocess.run([build.nvcc(), *build.ARCH, *build.NVCC_FLAGS, f"-I{build.CSRC}",
+                    f"-I{build.INCLUDE}", "-shared", "-o", str(out),
+                    str(ROOT / "tests" / "cuda" / "norm_check.cu")], check=True)
+    lib = ctypes.CDLL(str(out))
+    lib.norm_check.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong,
+                               ctypes.POINTER(ctypes.c_ulonglong)]
+    lib.norm_check.restype = ctypes.c_int
+    return lib
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("nfaces", [4, 6])
+def test_exact_projection_factor_equals_the_double_computation(norm_lib, nfaces, mode):
+    """The EXACT kernels' projection factor (float pre-check, the double norm
+    reproduced in float, double only where float cannot decide) is bit for
+    bit the reference's double computation, on 2^25 seeded cases per mode:
+    unit-range flows, a wide exponent range, one dominant face, few-bit
+    values (half of these with the capacity within a few ulps of the norm),
+    and norms within a few ulps of a capacity of exactly 1 or 0.5."""
+    m = ctypes.c_ulonglong(0)
+    assert norm_lib.norm_check(nfaces, mode, 1 << 25, ctypes.byref(m)) == 0
+    assert m.value == 0, f"{m.value} mismatches"
+
+
 def test_bounded_wait_times_out_and_context_survives():
     """A device-side wait on a barrier that nothing completes gives up after
     its budget, the host gets ASETS_ERR_TIMEOUT, and the next solve on the
