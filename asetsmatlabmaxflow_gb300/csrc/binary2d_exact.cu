@@ -10,6 +10,8 @@ static const StencilVariant kVariants[] = {
     make_variant<2, 4, 6, EPI_BINARY, true, 4, 4, 2>(),
     make_variant<2, 8, 4, EPI_BINARY, true>(),
     make_variant<2, 2, 4, EPI_BINARY, true>(),
+    // two iterations per pass, 224-row tiles (fixed-iteration runs)
+    make_variant_t2<4, 5, true, 3, 4>(),
 };
 
 const StencilVariant *binary2d_exact_variants(int *count)

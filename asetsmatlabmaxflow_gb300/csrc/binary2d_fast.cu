@@ -13,6 +13,8 @@ static const StencilVariant kVariants[] = {
     make_variant<2, 8, 4, EPI_BINARY, false, 4, 4>(),       // 224-row tiles
     make_variant<2, 2, 4, EPI_BINARY, false>(),             // 56-row tiles (short columns)
     make_variant<2, 4, 4, EPI_BINARY, false, 4, 4, 2>(),
+    // two iterations per pass, 224-row tiles (fixed-iteration runs)
+    make_variant_t2<4, 5, false, 3, 4>(),
 };
 
 const StencilVariant *binary2d_fast_variants(int *count)

@@ -17,9 +17,12 @@ struct StencilVariant {
     int dim, epi, exact;
     int tr, tc, nt, nstage;  // tile rows/cols, threads, TMA ring depth
     int smem_bytes;          // dynamic shared memory per block
-    int box_rows;            // halo box rows (tr + 8)
+    int box_rows;            // halo box rows (tr + 8; tr + 12 for two iterations per pass)
     int box_cols;            // halo box columns for slots other than SL_BC
     int box_cols_bc;         // halo box columns of the SL_BC slot
+    int tile_box_rows;       // rows of the binary tile boxes (tr; tr + 8 from row r0-4
+                             // for two iterations per pass)
+    int temporal;            // ALM iterations per launch (1, or 2: stencil2d_t2.cuh)
     const void *fn;
 };
 

@@ -26,7 +26,8 @@ struct IterControl {
     float err_bound;
     float denom;        // cvg = (float)erru / denom
     int alpha_bad;      // set by the validation pass
-    int pad[5];
+    int rollback;       // two-iteration pass: the solve ended at its first iteration
+    int pad[4];
 };
 
 // Stage slots: which field each TMA box holds.

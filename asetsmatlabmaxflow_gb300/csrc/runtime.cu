@@ -487,7 +487,8 @@ static asets_status setup_kernel(asets_solver *s, int exact, int tile_config)
         s->allocations.push_back(ptr);
         s->d_item_problem = static_cast<int *>(ptr);
         CU_TRY(cudaMemsetAsync(s->d_item_problem, 0, sizeof(int) * items, s->ctx->stream));
-        CU_TRY(cudaMalloc(&ptr, sizeof(double) * items));
+        // two erriter partials per item (a two-iteration pass)
+        CU_TRY(cudaMalloc(&ptr, sizeof(double) * 2 * items));
         s->allocations.push_back(ptr);
         s->d_item_partials = static_cast<double *>(ptr);
         s->items_cap = items;
@@ -980,7 +981,7 @@ static asets_status capture_chunk(ChunkGraph &g, cudaStream_t st, LaunchOne laun
 // queueing chunk c the host looks at the flag copied after chunk c-2.
 static asets_status run_chunks(asets_context *ctx, cudaGraphExec_t exec, int maxIt,
                                const unsigned int *done_dev, unsigned int done_target,
-                               cudaEvent_t flag_ev[2], int *chunks_out)
+                               cudaEvent_t flag_ev[2], int *chunks_out, int iters_per_launch = 1)
 {
     cudaStream_t st = ctx->stream;
     int *flags_h = ctx->pinned_flags;
@@ -995,7 +996,7 @@ static asets_status run_chunks(asets_context *ctx, cudaGraphExec_t exec, int max
             NvtxRange r("asets iteration chunk");
             CU_TRY(cudaGraphLaunch(exec, st));
         }
-        launched += kGraphIters;
+        launched += kGraphIters * iters_per_launch;
         CU_TRY(cudaMemcpyAsync(&flags_h[chunk % 2], done_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
         CU_TRY(cudaEventRecord(flag_ev[chunk % 2], st));
         ++chunk;
@@ -1012,8 +1013,16 @@ static asets_status finish_run(asets_solver *s, const IterControl &out, int *itN
         return fail(ASETS_ERR_TIMEOUT, "a device-side wait for a TMA load timed out");
     if (maxIt > 0 && !out.done)
         return fail(ASETS_ERR_CUDA, "iteration loop ended without completion (iter=%d)", out.iter);
-    s->final_parity = (s->model == ASETS_BINARY) ? ((out.last_iter + 1) & 1) : 0;
-    s->flow_parity = (out.last_iter + 1) & 1;
+    if (maxIt > 0 && out.rollback)
+        return fail(ASETS_ERR_UNSUPPORTED, "the two-iteration pass ended the solve at its first "
+                    "iteration (errBound met, or an odd maxIt); use it for fixed, even iteration "
+                    "counts");
+    // the state after iteration k is in parity (k & 1), or, with two
+    // iterations per pass, in the parity of the number of passes
+    const int ran = out.last_iter + 1;
+    const int parity = (s->variant && s->variant->temporal == 2) ? ((ran >> 1) & 1) : (ran & 1);
+    s->final_parity = (s->model == ASETS_BINARY) ? parity : 0;
+    s->flow_parity = parity;
     if (itNum)
         *itNum = (maxIt == 0) ? 0 : out.it_num;
     return ASETS_OK;
@@ -1044,10 +1053,13 @@ static asets_status solver_autotune(asets_solver *s, int flags, float cc, float 
     }
     cudaStream_t st = s->ctx->stream;
     int n = 0;
-    stencil_variants(s->dim, s->model == ASETS_BINARY ? EPI_BINARY : EPI_DIV, exact, &n);
+    const StencilVariant *tab =
+        stencil_variants(s->dim, s->model == ASETS_BINARY ? EPI_BINARY : EPI_DIV, exact, &n);
     int best = 1;
     float best_ms = 1e30f;
     for (int cand = 1; cand <= n; ++cand) {
+        if (tab[cand - 1].temporal != 1)
+            continue;  // the two-iteration pass serves fixed iteration counts only
         asets_status ss = prepare_run(s, flags, cand, kGraphIters, 0.0f, cc, steps);
         if (ss != ASETS_OK)
             return ss;
@@ -1110,7 +1122,7 @@ extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_
     CU_TRY(cudaEventRecord(s->ev0, st));
     int chunks = 0;
     ss = run_chunks(s->ctx, s->graph.exec, maxIt, reinterpret_cast<const unsigned int *>(&s->ctl->done),
-                    1u, s->flag_ev, &chunks);
+                    1u, s->flag_ev, &chunks, s->variant->temporal);
     if (ss != ASETS_OK)
         return ss;
     CU_TRY(cudaEventRecord(s->ev1, st));
@@ -1477,7 +1489,7 @@ static asets_status ensure_items(asets_solver *s, int items)
     s->allocations.push_back(ptr);
     s->d_item_problem = static_cast<int *>(ptr);
     CU_TRY(cudaMemsetAsync(s->d_item_problem, 0, sizeof(int) * items, s->ctx->stream));
-    CU_TRY(cudaMalloc(&ptr, sizeof(double) * items));
+    CU_TRY(cudaMalloc(&ptr, sizeof(double) * 2 * items));
     s->allocations.push_back(ptr);
     s->d_item_partials = static_cast<double *>(ptr);
     s->items_cap = items;
@@ -1649,6 +1661,8 @@ static asets_status batch_prepare(asets_batch *b, int flags, const int tile_conf
         asets_status st = prepare_run(s, flags, tile_config[gi], maxIt, errBound, cc, steps);
         if (st != ASETS_OK)
             return st;
+        if (s->variant->temporal != 1)
+            return fail(ASETS_ERR_UNSUPPORTED, "batches run one iteration per launch");
         b->groups[gi].idx.push_back((int)i);
         b->groups[gi].v = s->variant;
         b->groups[gi].tile_config = tile_config[gi];
@@ -1819,10 +1833,13 @@ static asets_status batch_autotune(asets_batch *b, int flags, float cc, float st
                 continue;
         }
         int n = 0;
-        stencil_variants((gi & 1) ? 3 : 2, gi >= 2 ? EPI_DIV : EPI_BINARY, exact, &n);
+        const StencilVariant *tab =
+            stencil_variants((gi & 1) ? 3 : 2, gi >= 2 ? EPI_DIV : EPI_BINARY, exact, &n);
         int best = 1;
         float best_ms = 1e30f;
         for (int cand = 1; cand <= n; ++cand) {
+            if (tab[cand - 1].temporal != 1)
+                continue;  // batches run one iteration per launch
             int tc[4] = {tile_config[0], tile_config[1], tile_config[2], tile_config[3]};
             tc[gi] = cand;
             asets_status st = batch_prepare(b, flags, tc, kGraphIters, 0.0f, cc, steps);

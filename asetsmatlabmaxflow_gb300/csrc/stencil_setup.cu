@@ -43,7 +43,8 @@ int build_problem_desc(EncodeTiledFn fn, const StencilVariant &v, const StencilP
             float *tsrc[NUM_TILE_SLOTS] = {p.src[par][1], p.src[par][2], const_cast<float *>(p.cs),
                                            const_cast<float *>(p.ct)};
             for (int ts = 0; ts < NUM_TILE_SLOTS; ++ts) {
-                int r = encode(fn, &A->tile[par][ts], tsrc[ts], p, 1, v.tr, v.tc);
+                int r = encode(fn, &A->tile[par][ts], tsrc[ts], p, 1,
+                               v.tile_box_rows > 0 ? v.tile_box_rows : v.tr, v.tc);
                 if (r)
                     return r;
             }

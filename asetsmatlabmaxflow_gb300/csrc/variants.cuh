@@ -3,6 +3,7 @@
 
 #include "internal.h"
 #include "stencil2_kernel.cuh"
+#include "stencil2d_t2.cuh"
 
 namespace asets {
 
@@ -23,7 +24,32 @@ StencilVariant make_variant()
     v.box_rows = G::LR;
     v.box_cols = G::LC;
     v.box_cols_bc = G::LC_BC;
+    v.tile_box_rows = G::TR;
+    v.temporal = 1;
     v.fn = reinterpret_cast<const void *>(&stencil_col_kernel<DIM, NW, NSTAGE, EPI, EXACT, MINB, UNROLL, CELLS, LATE>);
+    return v;
+}
+
+// The binary 2D kernel with two iterations per pass (stencil2d_t2.cuh).
+template <int NW, int NSTAGE, bool EXACT, int MINB, int UNROLL>
+StencilVariant make_variant_t2()
+{
+    using G = T2Geom<NW>;
+    StencilVariant v;
+    v.dim = 2;
+    v.epi = EPI_BINARY;
+    v.exact = EXACT ? 1 : 0;
+    v.tr = G::TR;
+    v.tc = 1;
+    v.nt = G::NT;
+    v.nstage = NSTAGE;
+    v.smem_bytes = G::template smem_bytes<NSTAGE>();
+    v.box_rows = G::LR;
+    v.box_cols = 1;
+    v.box_cols_bc = 1;
+    v.tile_box_rows = G::TB;
+    v.temporal = 2;
+    v.fn = reinterpret_cast<const void *>(&stencil2d_t2_kernel<NW, NSTAGE, EXACT, MINB, UNROLL>);
     return v;
 }
 
