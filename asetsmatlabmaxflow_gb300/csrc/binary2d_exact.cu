@@ -1,5 +1,6 @@
 // Compiled instances of the fused iteration kernel for the binary model (ps/pt/u
-// epilogue), 2D tiles 240-row (two rows per thread), 224-row, 56-row; EXACT projection, built with the reference's
+// epilogue), 2D tiles 240-row (two rows per thread), 224-row, 56-row, and two
+// iterations per pass with 224-row tiles; EXACT projection, built with the reference's
 // float arithmetic (no FMA contraction, no flush to zero).
 #include "variants.cuh"
 
@@ -10,7 +11,7 @@ static const StencilVariant kVariants[] = {
     make_variant<2, 4, 6, EPI_BINARY, true, 4, 4, 2>(),
     make_variant<2, 8, 4, EPI_BINARY, true>(),
     make_variant<2, 2, 4, EPI_BINARY, true>(),
-    // two iterations per pass, 224-row tiles (fixed-iteration runs)
+    // two iterations per pass, 224-row tiles
     make_variant_t2<4, 5, true, 3, 4>(),
 };
 

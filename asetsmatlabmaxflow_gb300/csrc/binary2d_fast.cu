@@ -1,20 +1,22 @@
-// Compiled instances of the fused iteration kernel for the binary model (ps/pt/u
-// epilogue), 2D tiles 240-row (two rows per thread), 224-row, 56-row; fast
-// projection, built with FMA contraction and flush to zero (held to the parity
-// tolerance, not bit-exactness).
+// Compiled instances of the fused iteration kernels for the binary model (ps/pt/u
+// epilogue), 2D: two iterations per pass with 224-row tiles (default), one
+// iteration per pass with 240-row (two rows per thread), 224-row and 56-row
+// tiles; fast projection, built with FMA contraction and flush to zero (held
+// to the parity tolerance, not bit-exactness).
 #include "variants.cuh"
 
 namespace asets {
 
 static const StencilVariant kVariants[] = {
-    // default: two rows per thread, 240-row tiles, 6 stages, the plane loop
-    // unrolled by 4
+    // default: two iterations per pass (stencil2d_t2.cuh), 224-row tiles,
+    // five stages, the plane loop unrolled by 4
+    make_variant_t2<4, 5, false, 3, 4>(),
+    // one iteration per pass: two rows per thread, 240-row tiles, 6 stages,
+    // the plane loop unrolled by 4
     make_variant<2, 4, 6, EPI_BINARY, false, 4, 4, 2>(),
     make_variant<2, 8, 4, EPI_BINARY, false, 4, 4>(),       // 224-row tiles
     make_variant<2, 2, 4, EPI_BINARY, false>(),             // 56-row tiles (short columns)
     make_variant<2, 4, 4, EPI_BINARY, false, 4, 4, 2>(),
-    // two iterations per pass, 224-row tiles (fixed-iteration runs)
-    make_variant_t2<4, 5, false, 3, 4>(),
 };
 
 const StencilVariant *binary2d_fast_variants(int *count)

@@ -154,6 +154,7 @@ struct asets_solver {
     int grid = 0;
     ProblemDesc desc;                  // host copy, uploaded at each run
     ProblemDesc *d_desc = nullptr;
+    ProblemDesc *d_desc_replay = nullptr;  // one-iteration re-run after a two-iteration pass
     int *d_item_problem = nullptr;
     double *d_item_partials = nullptr;
     unsigned int *d_queue = nullptr;
@@ -394,14 +395,9 @@ static const StencilVariant *pick_variant(const asets_solver *s, int exact, int 
     return match[0];
 }
 
-// Build the kernel arguments (TMA maps for both parities, destinations).
-static asets_status setup_kernel(asets_solver *s, int exact, int tile_config)
+// The solver's buffers as the iteration kernel sees them (both parities).
+static StencilProblem stencil_problem_of(const asets_solver *s)
 {
-    const StencilVariant *v = pick_variant(s, exact, tile_config);
-    if (!v)
-        return fail(ASETS_ERR_UNSUPPORTED, "no kernel variant for this configuration");
-    if (s->variant == v)
-        return ASETS_OK;
     const bool binary = (s->model == ASETS_BINARY);
     StencilProblem p;
     memset(&p, 0, sizeof p);
@@ -455,6 +451,18 @@ static asets_status setup_kernel(asets_solver *s, int exact, int tile_config)
     p.alpha_labels = s->alpha_labels;
     p.cs = s->cs;
     p.ct = s->ct;
+    return p;
+}
+
+// Build the kernel arguments (TMA maps for both parities, destinations).
+static asets_status setup_kernel(asets_solver *s, int exact, int tile_config)
+{
+    const StencilVariant *v = pick_variant(s, exact, tile_config);
+    if (!v)
+        return fail(ASETS_ERR_UNSUPPORTED, "no kernel variant for this configuration");
+    if (s->variant == v)
+        return ASETS_OK;
+    const StencilProblem p = stencil_problem_of(s);
     ProblemDesc &A = s->desc;
     int r = build_problem_desc(s->ctx->encode, *v, p, &A);
     if (r)
@@ -883,13 +891,14 @@ static asets_status prepare_run(asets_solver *s, int flags, int tile_config, int
     asets_status ss = setup_kernel(s, exact, tile_config);
     if (ss != ASETS_OK)
         return ss;
-    if (maxIt > s->cvg_cap) {
+    if (maxIt + 1 > s->cvg_cap) {
+        // one spare slot past maxIt: the erriter of a roll-back re-run
         float *p = nullptr;
-        ss = dalloc(s, &p, (size_t)maxIt);
+        ss = dalloc(s, &p, (size_t)maxIt + 1);
         if (ss != ASETS_OK)
             return ss;
         s->cvg = p;
-        s->cvg_cap = maxIt;
+        s->cvg_cap = maxIt + 1;
     }
     ProblemDesc &A = s->desc;
     A.cvg = s->cvg;
@@ -1013,18 +1022,110 @@ static asets_status finish_run(asets_solver *s, const IterControl &out, int *itN
         return fail(ASETS_ERR_TIMEOUT, "a device-side wait for a TMA load timed out");
     if (maxIt > 0 && !out.done)
         return fail(ASETS_ERR_CUDA, "iteration loop ended without completion (iter=%d)", out.iter);
-    if (maxIt > 0 && out.rollback)
-        return fail(ASETS_ERR_UNSUPPORTED, "the two-iteration pass ended the solve at its first "
-                    "iteration (errBound met, or an odd maxIt); use it for fixed, even iteration "
-                    "counts");
-    // the state after iteration k is in parity (k & 1), or, with two
-    // iterations per pass, in the parity of the number of passes
-    const int ran = out.last_iter + 1;
-    const int parity = (s->variant && s->variant->temporal == 2) ? ((ran >> 1) & 1) : (ran & 1);
+    // The state after iteration k is in parity (k & 1).  With two
+    // iterations per pass a pass starting at iteration it (even) reads
+    // parity (it/2) & 1 and leaves its result -- or, after a roll-back, the
+    // re-run first iteration's -- in the other one.
+    const int parity = (s->variant && s->variant->temporal == 2)
+                           ? (((out.last_iter >> 1) & 1) ^ 1)
+                           : ((out.last_iter + 1) & 1);
     s->final_parity = (s->model == ASETS_BINARY) ? parity : 0;
     s->flow_parity = parity;
     if (itNum)
         *itNum = (maxIt == 0) ? 0 : out.it_num;
+    return ASETS_OK;
+}
+
+static asets_status ensure_items(asets_solver *s, int items);
+
+// A two-iteration pass whose first iteration ended the solve (erriter met
+// errBound there, or maxIt was reached) has stored the second iteration's
+// state; the result is the first's.  Re-run that iteration with the
+// one-iteration kernel from the state before the pass, still in the pass's
+// source parity: when that parity is 1 the descriptor's parity halves are
+// swapped, so that the kernel (which reads parity it & 1 = 0 for an even
+// iteration) reads it and writes the other.  The re-run's erriter goes to a
+// spare cvg slot and its control block is put back to the pass's decision,
+// so cvg, itNum and the stopping iteration are those of the pass.
+static asets_status replay_first_of_pass(asets_solver *s, const IterControl &out)
+{
+    const int it = out.last_iter;
+    const int p = (it >> 1) & 1;
+    int n = 0;
+    const StencilVariant *tab = stencil_variants(s->dim, EPI_BINARY, s->variant->exact, &n);
+    const StencilVariant *v = nullptr;
+    for (int i = 0; i < n && !v; ++i)
+        if (tab[i].temporal == 1)
+            v = &tab[i];
+    if (!v)
+        return fail(ASETS_ERR_UNSUPPORTED, "no one-iteration kernel variant to re-run with");
+    const StencilProblem sp = stencil_problem_of(s);
+    ProblemDesc D;
+    int r = build_problem_desc(s->ctx->encode, *v, sp, &D);
+    if (r)
+        return fail(ASETS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", r);
+    CU_TRY(cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                v->smem_bytes));
+    int per_sm = 0;
+    CU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, v->nt, v->smem_bytes));
+    if (per_sm < 1)
+        return fail(ASETS_ERR_UNSUPPORTED, "stencil kernel does not fit on an SM");
+    const long long slots = (long long)s->ctx->num_sms * per_sm;
+    D.zchunks = choose_zchunks(sp, *v, slots);
+    const int items = problem_items(sp, *v, D.zchunks);
+    asets_status st = ensure_items(s, items);
+    if (st != ASETS_OK)
+        return st;
+    D.item_begin = 0;
+    D.n_items = items;
+    D.ctl = s->ctl;
+    D.item_partials = s->d_item_partials;
+    D.cvg = s->cvg + (s->last_max_it - it);  // cvg[it] of the re-run: the spare slot cvg[maxIt]
+    D.cc = s->desc.cc;
+    D.inv_cc = s->desc.inv_cc;
+    D.steps = s->desc.steps;
+    if (p == 1) {
+        std::swap(D.halo[0], D.halo[1]);
+        std::swap(D.tile[0], D.tile[1]);
+        std::swap(D.dst_b[0], D.dst_b[1]);
+        std::swap(D.dst_s[0], D.dst_s[1]);
+    }
+    cudaStream_t stm = s->ctx->stream;
+    if (!s->d_desc_replay) {
+        void *ptr = nullptr;
+        CU_TRY(cudaMalloc(&ptr, sizeof(ProblemDesc)));
+        s->allocations.push_back(ptr);
+        s->d_desc_replay = static_cast<ProblemDesc *>(ptr);
+    }
+    CU_TRY(cudaMemcpyAsync(s->d_desc_replay, &D, sizeof D, cudaMemcpyHostToDevice, stm));
+    IterControl c = out;
+    c.iter = it;
+    c.done = 0;
+    c.max_it = it + 1;
+    c.err_bound = -1.0f;  // never met: the re-run ends by maxIt
+    c.ticket = 0;
+    c.error = 0;
+    c.rollback = 0;
+    CU_TRY(cudaMemcpyAsync(s->ctl, &c, sizeof c, cudaMemcpyHostToDevice, stm));
+    BatchArgs ba;
+    ba.probs = s->d_desc_replay;
+    ba.item_problem = s->d_item_problem;
+    ba.total_items = items;
+    ba.queue = s->d_queue;
+    ba.done_count = s->d_queue + 2;
+    void *params[] = {&ba};
+    const long long grid = std::max<long long>(1, std::min<long long>(items, slots));
+    CU_TRY(cudaLaunchKernel(v->fn, dim3((unsigned)grid), dim3(v->nt), params, v->smem_bytes, stm));
+    IterControl chk;
+    CU_TRY(cudaMemcpyAsync(&chk, s->ctl, sizeof chk, cudaMemcpyDeviceToHost, stm));
+    CU_TRY(cudaStreamSynchronize(stm));
+    if (chk.error & DEV_ERR_TIMEOUT)
+        return fail(ASETS_ERR_TIMEOUT, "a device-side wait for a TMA load timed out");
+    if (!chk.done || chk.last_iter != it)
+        return fail(ASETS_ERR_CUDA, "re-run of iteration %d did not complete", it);
+    IterControl back = out;  // the pass's decision stands
+    CU_TRY(cudaMemcpyAsync(s->ctl, &back, sizeof back, cudaMemcpyHostToDevice, stm));
+    CU_TRY(cudaStreamSynchronize(stm));
     return ASETS_OK;
 }
 
@@ -1058,9 +1159,9 @@ static asets_status solver_autotune(asets_solver *s, int flags, float cc, float 
     int best = 1;
     float best_ms = 1e30f;
     for (int cand = 1; cand <= n; ++cand) {
-        if (tab[cand - 1].temporal != 1)
-            continue;  // the two-iteration pass serves fixed iteration counts only
-        asets_status ss = prepare_run(s, flags, cand, kGraphIters, 0.0f, cc, steps);
+        // one chunk of launches: kGraphIters x (iterations per launch) iterations
+        const int per_launch = tab[cand - 1].temporal;
+        asets_status ss = prepare_run(s, flags, cand, kGraphIters * per_launch, 0.0f, cc, steps);
         if (ss != ASETS_OK)
             return ss;
         ss = capture_chunk(s->graph, st, [&] { return launch_iteration(s); });
@@ -1072,6 +1173,7 @@ static asets_status solver_autotune(asets_solver *s, int flags, float cc, float 
         CU_TRY(cudaEventSynchronize(s->ev1));
         float ms = 0.f;
         CU_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+        ms /= (float)per_launch;  // per kGraphIters iterations
         if (ms < best_ms) {
             best_ms = ms;
             best = cand;
@@ -1129,10 +1231,19 @@ extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_
     IterControl out;
     CU_TRY(cudaMemcpyAsync(&out, s->ctl, sizeof out, cudaMemcpyDeviceToHost, st));
     CU_TRY(cudaStreamSynchronize(st));
+    int replays = 0;
+    if (maxIt > 0 && out.done && out.rollback && !(out.error & DEV_ERR_TIMEOUT)) {
+        ss = replay_first_of_pass(s, out);
+        if (ss != ASETS_OK)
+            return ss;
+        replays = 1;
+        CU_TRY(cudaEventRecord(s->ev1, st));  // the re-run counts into the solve's time
+        CU_TRY(cudaEventSynchronize(s->ev1));
+    }
     float ms = 0.f;
     CU_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
     s->last_ms = ms;
-    s->last_launches = chunks * kGraphIters * (s->model == ASETS_BINARY ? 1 : 2);
+    s->last_launches = chunks * kGraphIters * (s->model == ASETS_BINARY ? 1 : 2) + replays;
     s->last_iters = (maxIt == 0) ? 0 : out.last_iter + 1;
     return finish_run(s, out, itNum);
 }
@@ -1661,8 +1772,6 @@ static asets_status batch_prepare(asets_batch *b, int flags, const int tile_conf
         asets_status st = prepare_run(s, flags, tile_config[gi], maxIt, errBound, cc, steps);
         if (st != ASETS_OK)
             return st;
-        if (s->variant->temporal != 1)
-            return fail(ASETS_ERR_UNSUPPORTED, "batches run one iteration per launch");
         b->groups[gi].idx.push_back((int)i);
         b->groups[gi].v = s->variant;
         b->groups[gi].tile_config = tile_config[gi];
@@ -1838,16 +1947,17 @@ static asets_status batch_autotune(asets_batch *b, int flags, float cc, float st
         int best = 1;
         float best_ms = 1e30f;
         for (int cand = 1; cand <= n; ++cand) {
-            if (tab[cand - 1].temporal != 1)
-                continue;  // batches run one iteration per launch
             int tc[4] = {tile_config[0], tile_config[1], tile_config[2], tile_config[3]};
             tc[gi] = cand;
-            asets_status st = batch_prepare(b, flags, tc, kGraphIters, 0.0f, cc, steps);
+            // 2 x kGraphIters iterations of every member: two chunks of one
+            // iteration per launch, or one of two (the second chunk's
+            // launches then return at entry)
+            asets_status st = batch_prepare(b, flags, tc, 2 * kGraphIters, 0.0f, cc, steps);
             if (st != ASETS_OK)
                 return st;
             int chunks = 0;
             CU_TRY(cudaEventRecord(b->ev0, b->ctx->stream));
-            st = batch_execute(b, kGraphIters, &chunks, nullptr);
+            st = batch_execute(b, 2 * kGraphIters, &chunks, nullptr);
             if (st != ASETS_OK)
                 return st;
             CU_TRY(cudaEventRecord(b->ev1, b->ctx->stream));
@@ -1905,10 +2015,25 @@ extern "C" ASETS_API asets_status asets_batch_run(asets_batch *b, const asets_op
         CU_TRY(cudaMemcpyAsync(&outs[i], b->members[i]->ctl, sizeof(IterControl),
                                cudaMemcpyDeviceToHost, st));
     CU_TRY(cudaStreamSynchronize(st));
+    // members whose two-iteration pass ended at its first iteration
+    int replays = 0;
+    for (size_t i = 0; i < b->members.size(); ++i) {
+        asets_solver *s = b->members[i];
+        if (maxIt > 0 && outs[i].done && outs[i].rollback && !(outs[i].error & DEV_ERR_TIMEOUT)) {
+            asets_status rs = replay_first_of_pass(s, outs[i]);
+            if (rs != ASETS_OK)
+                return rs;
+            ++replays;
+        }
+    }
+    if (replays) {
+        CU_TRY(cudaEventRecord(b->ev1, st));  // the re-runs count into the batch's time
+        CU_TRY(cudaEventSynchronize(b->ev1));
+    }
     float ms = 0.f;
     CU_TRY(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
     b->last_ms = ms;
-    b->last_launches = launches;  // flow passes, plus the labelled members' label kernels
+    b->last_launches = launches + replays;  // flow passes, label kernels, re-runs
     b->groups[0].tile_config = tile_config[0];
     b->groups[1].tile_config = tile_config[1];
     for (size_t i = 0; i < b->members.size(); ++i) {
