@@ -10,6 +10,7 @@
 
 #include "asets.h"
 #include "internal.h"
+#include "wgrad_tc.cuh"
 
 using namespace asets;
 
@@ -198,71 +199,6 @@ __global__ void loss_kernel(const float *out, const float *tgt, __nv_bfloat16 *g
         atomicAdd(loss, acc * scale);
 }
 
-// dW[t][ci][co] += sum_v a[v + off_t][ci] * g[v][co], bias grad sum_v g[v][co].
-// One block per SM walks 128-voxel rows; thread (t, ci) keeps its 16 outputs
-// in registers across rows.
-constexpr int kWgThreads = 448;  // 432 (tap, channel) pairs + 16 bias lanes
-constexpr int kWgSmem = (9 * 130 * 16 + 128 * 16) * 4;
-__global__ void __launch_bounds__(kWgThreads, 1)
-    wgrad_kernel(const __nv_bfloat16 *a, const __nv_bfloat16 *g, float *dw, float *db, int ny,
-                 int nx, int nz)
-{
-    extern __shared__ float wg_smem[];
-    float(*sa)[130][16] = reinterpret_cast<float(*)[130][16]>(wg_smem);       // [9][130][16]
-    float(*sg)[16] = reinterpret_cast<float(*)[16]>(wg_smem + 9 * 130 * 16);  // [128][16]
-    const int tid = threadIdx.x;
-    const int t = tid / 16, ci = tid % 16;  // valid for tid < 432
-    const int dz = t / 9, dx = (t / 3) % 3, dy = t % 3;
-    float acc[16];
-#pragma unroll
-    for (int c = 0; c < 16; ++c)
-        acc[c] = 0.f;
-    const int ytiles = (ny + 127) / 128;
-    const int ntiles = ytiles * nx * nz;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int yt = tile % ytiles, rest = tile / ytiles;
-        const int x = rest % nx, z = rest / nx;
-        const int y0 = yt * 128;
-        __syncthreads();
-        for (int i = tid; i < 9 * 130 * 16; i += kWgThreads) {
-            const int c = i % 16, vy = (i / 16) % 130, row = i / (16 * 130);
-            const int zz = z + row / 3 - 1, xx = x + row % 3 - 1, yy = y0 + vy - 1;
-            float f = 0.f;
-            if (zz >= 0 && zz < nz && xx >= 0 && xx < nx && yy >= 0 && yy < ny)
-                f = __bfloat162float(a[(((long long)zz * nx + xx) * ny + yy) * 16 + c]);
-            sa[row][vy][c] = f;
-        }
-        for (int i = tid; i < 128 * 16; i += kWgThreads) {
-            const int c = i % 16, vy = i / 16, yy = y0 + vy;
-            sg[vy][c] = (yy < ny) ? __bfloat162float(g[(((long long)z * nx + x) * ny + yy) * 16 + c])
-                                  : 0.f;
-        }
-        __syncthreads();
-        if (tid < 432) {
-            const int row = dz * 3 + dx;
-            for (int v = 0; v < 128; ++v) {
-                const float av = sa[row][v + dy][ci];
-#pragma unroll
-                for (int c = 0; c < 16; ++c)
-                    acc[c] = fmaf(av, sg[v][c], acc[c]);
-            }
-        } else {
-            const int c = tid - 432;  // bias lanes
-            float s = 0.f;
-            for (int v = 0; v < 128; ++v)
-                s += sg[v][c];
-            acc[0] += s;
-        }
-    }
-    if (tid < 432) {
-#pragma unroll
-        for (int c = 0; c < 16; ++c)
-            atomicAdd(&dw[(t * 16 + ci) * 16 + c], acc[c]);
-    } else {
-        atomicAdd(&db[tid - 432], acc[0]);
-    }
-}
-
 // Adam on the FP32 master parameters; clears the gradients.
 __global__ void adam_kernel(float *p, float *m, float *v, float *grad, int n, float lr, float b1,
                             float b2, float eps, float c1, float c2)
@@ -310,6 +246,7 @@ struct asets_wsnet {
     __nv_bfloat16 *gout = nullptr;                // [2][v][16] gradient of the output
     float *out = nullptr, *tgt = nullptr;         // [2][v][16]
     float *part = nullptr;                        // [v][16] first half of a summed dgrad
+    float *wg_partial = nullptr;                  // [SMs][28][16][16] weight-gradient partials
     int step = 0;
 };
 
@@ -359,11 +296,11 @@ extern "C" ASETS_API asets_status asets_wsnet_create(asets_context *ctx, int nLa
             return fail_free(ws_fail(ASETS_ERR_OUT_OF_MEMORY, "warm-start net: out of memory"));
     if (cudaMallocAsync((void **)&n->w16, kBlocks * kW * 2, st) != cudaSuccess ||
         cudaMallocAsync((void **)&n->loss, 4, st) != cudaSuccess ||
-        cudaMallocAsync((void **)&n->err, 4, st) != cudaSuccess)
+        cudaMallocAsync((void **)&n->err, 4, st) != cudaSuccess ||
+        cudaMallocAsync((void **)&n->wg_partial,
+                        (size_t)context_num_sms(ctx) * kWgtTaps * 256 * sizeof(float), st) !=
+            cudaSuccess)
         return fail_free(ws_fail(ASETS_ERR_OUT_OF_MEMORY, "warm-start net: out of memory"));
-    if (cudaFuncSetAttribute(wgrad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kWgSmem) !=
-        cudaSuccess)
-        return fail_free(ws_fail(ASETS_ERR_CUDA, "warm-start net: shared memory attribute"));
     // He-normal initial weights from a seeded generator (Box-Muller on a
     // 64-bit LCG), zero biases; weights of unused channels stay zero.
     std::vector<float> h(kParams, 0.f);
@@ -407,7 +344,7 @@ extern "C" ASETS_API void asets_wsnet_destroy(asets_wsnet *n)
     cudaStream_t st = context_stream(n->ctx);
     void *ps[] = {n->params, n->grads,   n->m,       n->v,    n->w16,  n->loss,
                   n->err,    n->x0,      n->act[0],  n->act[1], n->act[2], n->gbuf[0],
-                  n->gbuf[1], n->gout,   n->out,     n->tgt,  n->part};
+                  n->gbuf[1], n->gout,   n->out,     n->tgt,  n->part, n->wg_partial};
     for (void *p : ps)
         if (p)
             cudaFreeAsync(p, st);
@@ -534,9 +471,8 @@ static asets_status ws_backward(asets_wsnet *n, int Ny, int Nx, int Nz, const fl
     // flip(g3, W3) + flip(g4, W4), masked by the ReLU of act[2]
     for (int b = 3; b < kBlocks; ++b) {
         float *gw = n->grads + (size_t)b * (kW + 16);
-        wgrad_kernel<<<sms, kWgThreads, kWgSmem, st>>>(n->act[2], n->gout + (size_t)(b - 3) * vox * 16,
-                                                        gw, gw + kW, Ny, Nx, Nz);
-        WS_TRY(cudaGetLastError());
+        WS_TRY(launch_wgrad_tc(enc, n->act[2], n->gout + (size_t)(b - 3) * vox * 16, gw, gw + kW,
+                               Ny, Nx, Nz, n->wg_partial, sms, n->err, st));
     }
     {
         ConvLaunch c = conv_of(n, 3, n->gout, n->part, Ny, Nx, Nz);
@@ -554,8 +490,8 @@ static asets_status ws_backward(asets_wsnet *n, int Ny, int Nx, int Nz, const fl
     int cur = 0;
     for (int l = 2; l >= 0; --l) {
         float *gw = n->grads + (size_t)l * (kW + 16);
-        wgrad_kernel<<<sms, kWgThreads, kWgSmem, st>>>(ins[l], n->gbuf[cur], gw, gw + kW, Ny, Nx, Nz);
-        WS_TRY(cudaGetLastError());
+        WS_TRY(launch_wgrad_tc(enc, ins[l], n->gbuf[cur], gw, gw + kW, Ny, Nx, Nz, n->wg_partial,
+                               sms, n->err, st));
         if (l == 0)
             break;
         ConvLaunch c = conv_of(n, l, n->gbuf[cur], n->gbuf[cur ^ 1], Ny, Nx, Nz);
