@@ -11,7 +11,8 @@
 // the no-swizzle K-major layout in which a tap's A operand is a plain offset.
 //
 // The same kernel computes the data gradient: with `flip` the taps are
-// mirrored and the weight matrix transposed.  The epilogue adds the bias and
+// mirrored and the weight matrix transposed.  The weight gradient is a
+// separate tcgen05 kernel (wgrad_tc.cuh).  The epilogue adds the bias and
 // an optional FP32 addend (a second convolution's result), then applies ReLU
 // and an optional mask (the ReLU derivative of the layer below).
 #include <cuda_bf16.h>
@@ -23,7 +24,9 @@
 
 namespace asets {
 
-constexpr int kConvThreads = 128;            // 4 warps: TMEM lanes 0..127
+constexpr int kConvThreads = 192;            // warp 0: TMA, warp 1: MMA, warps 2-5: epilogue
+constexpr int kConvStages = 4;               // TMA ring depth
+constexpr int kConvAcc = 8;                  // TMEM accumulators (16 FP32 columns each)
 constexpr int kConvRows = 9;                 // (dz, dx) neighbour rows
 constexpr int kConvVox = 130;                // y-1 .. y+128
 constexpr int kConvHalfBytes = kConvVox * 16;           // 8 channels x 2 B per voxel
@@ -33,7 +36,7 @@ constexpr int kConvStageStride = (kConvStageBytes + 127) / 128 * 128;
 constexpr int kConvTapBytes = 2 * 16 * 16;              // B operand of one tap
 constexpr int kConvWBytes = 27 * kConvTapBytes;         // 13,824 B
 // + 32 KB: operand descriptors can only address inside the allocation
-constexpr int kConvSmem = 2 * kConvStageStride + kConvWBytes + 128 + 32768;
+constexpr int kConvSmem = kConvStages * kConvStageStride + kConvWBytes + 128 + 32768;
 
 struct ConvTcArgs {
     CUtensorMap act;           // 5D view (8 ch, y, half, x, z) of the BF16 input
@@ -47,28 +50,42 @@ struct ConvTcArgs {
     int relu, out_fp32, flip;
 };
 
+// Warp-specialised: warp 0 (one lane) keeps a ring of kConvStages tile
+// stages loading, warp 1 (one lane) issues each tile's 27 MMAs into one of
+// kConvAcc TMEM accumulators as soon as its stage and accumulator are free
+// and commits them to the stage's "empty" and the accumulator's "full"
+// barrier, and warps 2-5 (TMEM lane quarters 2, 3, 0, 1) drain full
+// accumulators through the epilogue and hand them back.  No role waits on
+// another's per-tile round trip, so the tensor core sees a steady stream
+// of MMAs.  Every wait is bounded; a timeout raises the shared abort flag,
+// every role leaves its loop, the producer waits (bounded) for its copies
+// in flight and the MMA lane for its last commit before TMEM is freed.
 __global__ void __launch_bounds__(kConvThreads, 1) conv3_tc_kernel(const __grid_constant__ ConvTcArgs A)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ uint64_t full_bar[2], mma_bar[2];
+    __shared__ uint64_t full_bar[kConvStages], empty_bar[kConvStages];
+    __shared__ uint64_t accf_bar[kConvAcc], acce_bar[kConvAcc];
     __shared__ uint32_t s_tmem;
     __shared__ int s_abort;
     unsigned char *smem = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~static_cast<uintptr_t>(127));
-    unsigned char *stage[2] = {smem, smem + kConvStageStride};
-    unsigned char *wsm = smem + 2 * kConvStageStride;
+    unsigned char *wsm = smem + kConvStages * kConvStageStride;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     if (tid == 0) {
         s_abort = 0;
-        for (int i = 0; i < 2; ++i) {
+        for (int i = 0; i < kConvStages; ++i) {
             mbar_init(&full_bar[i], 1);
-            mbar_init(&mma_bar[i], 1);
+            mbar_init(&empty_bar[i], 1);
+        }
+        for (int i = 0; i < kConvAcc; ++i) {
+            mbar_init(&accf_bar[i], 1);
+            mbar_init(&acce_bar[i], 4);  // one arrival per epilogue warp
         }
         mbar_fence_init();
     }
-    if (warp == 0)
-        tmem_alloc(&s_tmem, 32);  // two 16-column FP32 accumulators
+    if (warp == 1)
+        tmem_alloc(&s_tmem, kConvAcc * 16);
 
     // B operands: tap t as [k half][n][8 k] (core matrices of 8 n x 8 k)
     for (int i = tid; i < 27 * 16 * 16; i += kConvThreads) {
@@ -83,130 +100,149 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv3_tc_kernel(const __grid_
     tc_fence_after_sync();
     const uint32_t tmem = s_tmem;
 
-    float bias[16];
-#pragma unroll
-    for (int c = 0; c < 16; ++c)
-        bias[c] = A.bias ? __ldg(A.bias + c) : 0.f;
-
     const int ntiles = A.ytiles * A.nx * A.nz;
-    const uint32_t idesc = umma_idesc_bf16_f32(128, 16);
-    auto issue = [&](int tile, int st) {
-        const int yt = tile % A.ytiles, rest = tile / A.ytiles;
-        const int x = rest % A.nx, z = rest / A.nx;
-        mbar_arrive_expect_tx(&full_bar[st], kConvStageBytes);
-        tma_load_5d(stage[st], &A.act, 0, yt * 128 - 1, 0, x - 1, z - 1, &full_bar[st]);
-    };
-    if (tid == 0) {
-        if ((int)blockIdx.x < ntiles)
-            issue(blockIdx.x, 0);
-        if ((int)(blockIdx.x + gridDim.x) < ntiles)
-            issue(blockIdx.x + gridDim.x, 1);
-    }
+    const int mine = ((int)blockIdx.x < ntiles) ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
 
-    int j = 0;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++j) {
-        const int st = j & 1;
-        const uint32_t ph = (j >> 1) & 1;
-        bool ok = true;
-        if (tid == 0) {
-            ok = mbar_wait_bounded(&full_bar[st], ph, &s_abort);
-            if (ok) {
+    if (warp == 0) {
+        // ---- producer
+        int issued = 0;
+        if (lane == 0) {
+            for (int j = 0; j < mine; ++j) {
+                const int st = j % kConvStages;
+                if (j >= kConvStages &&
+                    !mbar_wait_bounded(&empty_bar[st], ((j / kConvStages) - 1) & 1, &s_abort))
+                    break;
+                const int tile = blockIdx.x + j * gridDim.x;
+                const int yt = tile % A.ytiles, rest = tile / A.ytiles;
+                const int x = rest % A.nx, z = rest / A.nx;
+                mbar_arrive_expect_tx(&full_bar[st], kConvStageBytes);
+                tma_load_5d(smem + st * kConvStageStride, &A.act, 0, yt * 128 - 1, 0, x - 1, z - 1,
+                            &full_bar[st]);
+                ++issued;
+            }
+            if (s_abort) {
+                // drain the copies in flight of this CTA (bounded)
+                volatile int drain_flag = 0;
+                for (int j = issued > kConvStages ? issued - kConvStages : 0; j < issued; ++j)
+                    mbar_wait_bounded(&full_bar[j % kConvStages], (j / kConvStages) & 1,
+                                      (int *)&drain_flag);
+            }
+        }
+    } else if (warp == 1) {
+        // ---- MMA issue
+        if (lane == 0) {
+            const uint32_t idesc = umma_idesc_bf16_f32(128, 16);
+            const uint32_t b0 = smem_addr(wsm);
+            int done = 0;
+            for (int j = 0; j < mine; ++j) {
+                const int st = j % kConvStages, slot = j % kConvAcc;
+                if (!mbar_wait_bounded(&full_bar[st], (j / kConvStages) & 1, &s_abort))
+                    break;
+                if (j >= kConvAcc &&
+                    !mbar_wait_bounded(&acce_bar[slot], ((j / kConvAcc) - 1) & 1, &s_abort))
+                    break;
                 tc_fence_after_sync();
-                const uint32_t a0 = smem_addr(stage[st]);
-                const uint32_t b0 = smem_addr(wsm);
+                const uint32_t a0 = smem_addr(smem + st * kConvStageStride);
                 for (int t = 0; t < 27; ++t) {
                     const int dz = t / 9, dx = (t / 3) % 3, dy = t % 3;
                     const uint32_t a = a0 + (dz * 3 + dx) * kConvRowBytes + dy * 16;
                     const uint64_t ad = umma_smem_desc(a, kConvHalfBytes, 128);
                     const uint64_t bd = umma_smem_desc(b0 + t * kConvTapBytes, 256, 128);
-                    umma_bf16(tmem + st * 16, ad, bd, idesc, t > 0 ? 1u : 0u);
+                    umma_bf16(tmem + slot * 16, ad, bd, idesc, t > 0 ? 1u : 0u);
                 }
-                umma_commit(&mma_bar[st]);
-                ok = mbar_wait_bounded(&mma_bar[st], ph, &s_abort);
+                umma_commit(&empty_bar[st]);
+                umma_commit(&accf_bar[slot]);
+                done = j + 1;
+            }
+            if (s_abort && done > 0) {
+                // the last committed MMAs finish before TMEM is freed (bounded)
+                volatile int drain_flag = 0;
+                const int j = done - 1;
+                mbar_wait_bounded(&accf_bar[j % kConvAcc], (j / kConvAcc) & 1, (int *)&drain_flag);
             }
         }
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0)
-                atomicOr(A.err, 1);
-            break;
-        }
-        tc_fence_after_sync();
-        float acc[16];
-        tmem_load16(tmem + ((uint32_t)(32 * warp) << 16) + st * 16, acc);
-        const int yt = tile % A.ytiles, rest = tile / A.ytiles;
-        const int x = rest % A.nx, z = rest / A.nx;
-        const int y = yt * 128 + 32 * warp + lane;
-        if (y < A.ny) {
-            const long long v = ((long long)z * A.nx + x) * A.ny + y;
-            float o[16];
+    } else {
+        // ---- epilogue: warp w reads TMEM lanes 32 * (w % 4) .. + 31
+        const int q = warp & 3;
+        float bias[16];
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
-                o[c] = acc[c] + bias[c];
-            }
-            if (A.addend) {
-                const float4 *ap = reinterpret_cast<const float4 *>(A.addend + v * 16);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const float4 a4 = __ldg(ap + q);
-                    o[4 * q] += a4.x;
-                    o[4 * q + 1] += a4.y;
-                    o[4 * q + 2] += a4.z;
-                    o[4 * q + 3] += a4.w;
-                }
-            }
-            if (A.relu) {
+        for (int c = 0; c < 16; ++c)
+            bias[c] = A.bias ? __ldg(A.bias + c) : 0.f;
+        for (int j = 0; j < mine; ++j) {
+            const int slot = j % kConvAcc;
+            if (!mbar_wait_bounded(&accf_bar[slot], (j / kConvAcc) & 1, &s_abort))
+                break;
+            tc_fence_after_sync();
+            float acc[16];
+            tmem_load16(tmem + ((uint32_t)(32 * q) << 16) + slot * 16, acc);
+            tc_fence_before_sync();
+            __syncwarp();
+            if (lane == 0)
+                asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&acce_bar[slot]))
+                             : "memory");
+            const int tile = blockIdx.x + j * gridDim.x;
+            const int yt = tile % A.ytiles, rest = tile / A.ytiles;
+            const int x = rest % A.nx, z = rest / A.nx;
+            const int y = yt * 128 + 32 * q + lane;
+            if (y < A.ny) {
+                const long long v = ((long long)z * A.nx + x) * A.ny + y;
+                float o[16];
 #pragma unroll
                 for (int c = 0; c < 16; ++c)
-                    o[c] = fmaxf(o[c], 0.f);
-            }
-            if (A.mask) {
-                const uint4 *mp = reinterpret_cast<const uint4 *>(A.mask + v * 16);
-                const uint4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
-                const __nv_bfloat16 *mb0 = reinterpret_cast<const __nv_bfloat16 *>(&m0);
-                const __nv_bfloat16 *mb1 = reinterpret_cast<const __nv_bfloat16 *>(&m1);
+                    o[c] = acc[c] + bias[c];
+                if (A.addend) {
+                    const float4 *ap = reinterpret_cast<const float4 *>(A.addend + v * 16);
 #pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    if (!(__bfloat162float(mb0[c]) > 0.f))
-                        o[c] = 0.f;
-                    if (!(__bfloat162float(mb1[c]) > 0.f))
-                        o[8 + c] = 0.f;
+                    for (int k = 0; k < 4; ++k) {
+                        const float4 a4 = __ldg(ap + k);
+                        o[4 * k] += a4.x;
+                        o[4 * k + 1] += a4.y;
+                        o[4 * k + 2] += a4.z;
+                        o[4 * k + 3] += a4.w;
+                    }
+                }
+                if (A.relu) {
+#pragma unroll
+                    for (int c = 0; c < 16; ++c)
+                        o[c] = fmaxf(o[c], 0.f);
+                }
+                if (A.mask) {
+                    const uint4 *mp = reinterpret_cast<const uint4 *>(A.mask + v * 16);
+                    const uint4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
+                    const __nv_bfloat16 *mb0 = reinterpret_cast<const __nv_bfloat16 *>(&m0);
+                    const __nv_bfloat16 *mb1 = reinterpret_cast<const __nv_bfloat16 *>(&m1);
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) {
+                        if (!(__bfloat162float(mb0[c]) > 0.f))
+                            o[c] = 0.f;
+                        if (!(__bfloat162float(mb1[c]) > 0.f))
+                            o[8 + c] = 0.f;
+                    }
+                }
+                if (A.out_fp32) {
+                    float4 *op = reinterpret_cast<float4 *>(static_cast<float *>(A.out) + v * 16);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        op[k] = make_float4(o[4 * k], o[4 * k + 1], o[4 * k + 2], o[4 * k + 3]);
+                } else {
+                    __align__(16) __nv_bfloat16 ob[16];
+#pragma unroll
+                    for (int c = 0; c < 16; ++c)
+                        ob[c] = __float2bfloat16_rn(o[c]);
+                    uint4 *op = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(A.out) + v * 16);
+                    op[0] = reinterpret_cast<const uint4 *>(ob)[0];
+                    op[1] = reinterpret_cast<const uint4 *>(ob)[1];
                 }
             }
-            if (A.out_fp32) {
-                float4 *op = reinterpret_cast<float4 *>(static_cast<float *>(A.out) + v * 16);
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    op[q] = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
-            } else {
-                __align__(16) __nv_bfloat16 ob[16];
-#pragma unroll
-                for (int c = 0; c < 16; ++c)
-                    ob[c] = __float2bfloat16_rn(o[c]);
-                uint4 *op = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(A.out) + v * 16);
-                op[0] = reinterpret_cast<const uint4 *>(ob)[0];
-                op[1] = reinterpret_cast<const uint4 *>(ob)[1];
-            }
-        }
-        tc_fence_before_sync();
-        __syncthreads();  // stage st and accumulator st are free again
-        if (tid == 0 && tile + 2 * (int)gridDim.x < ntiles)
-            issue(tile + 2 * gridDim.x, st);
-    }
-    __syncthreads();
-    if (tid == 0) {
-        // drain copies still in flight after an early exit (bounded)
-        s_abort = 0;
-        for (int i = 0; i < 2; ++i) {
-            const int jj = j + i;
-            const int t2 = blockIdx.x + jj * gridDim.x;
-            if (t2 < ntiles && jj >= 0)
-                mbar_wait_bounded(&full_bar[jj & 1], (jj >> 1) & 1, &s_abort);
         }
     }
+    tc_fence_before_sync();
     __syncthreads();
     tc_fence_after_sync();
-    if (warp == 0)
-        tmem_dealloc(tmem, 32);
+    if (tid == 0 && s_abort)
+        atomicOr(A.err, 1);
+    if (warp == 1)
+        tmem_dealloc(tmem, kConvAcc * 16);
 }
 
 int conv_smem_bytes() { return kConvSmem; }
