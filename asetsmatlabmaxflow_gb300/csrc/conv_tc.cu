@@ -48,6 +48,7 @@ struct ConvTcArgs {
     int *err;
     int ny, nx, nz, ytiles;
     int relu, out_fp32, flip;
+    int hp_in, hp_out;         // half-planar BF16 input (and mask) / output
 };
 
 // Warp-specialised: warp 0 (one lane) keeps a ring of kConvStages tile
@@ -206,9 +207,13 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv3_tc_kernel(const __grid_
                     for (int c = 0; c < 16; ++c)
                         o[c] = fmaxf(o[c], 0.f);
                 }
+                // element offsets of the voxel's two channel halves in the input layout
+                const long long zx = (long long)z * A.nx + x;
+                const long long h0 = A.hp_in ? (zx * 2) * A.ny * 8 + (long long)y * 8 : v * 16;
+                const long long h1 = A.hp_in ? h0 + (long long)A.ny * 8 : v * 16 + 8;
                 if (A.mask) {
-                    const uint4 *mp = reinterpret_cast<const uint4 *>(A.mask + v * 16);
-                    const uint4 m0 = __ldg(mp), m1 = __ldg(mp + 1);
+                    const uint4 m0 = __ldg(reinterpret_cast<const uint4 *>(A.mask + h0));
+                    const uint4 m1 = __ldg(reinterpret_cast<const uint4 *>(A.mask + h1));
                     const __nv_bfloat16 *mb0 = reinterpret_cast<const __nv_bfloat16 *>(&m0);
                     const __nv_bfloat16 *mb1 = reinterpret_cast<const __nv_bfloat16 *>(&m1);
 #pragma unroll
@@ -229,9 +234,11 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv3_tc_kernel(const __grid_
 #pragma unroll
                     for (int c = 0; c < 16; ++c)
                         ob[c] = __float2bfloat16_rn(o[c]);
-                    uint4 *op = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(A.out) + v * 16);
-                    op[0] = reinterpret_cast<const uint4 *>(ob)[0];
-                    op[1] = reinterpret_cast<const uint4 *>(ob)[1];
+                    __nv_bfloat16 *ob0 = static_cast<__nv_bfloat16 *>(A.out);
+                    const long long o0 = A.hp_out ? (zx * 2) * A.ny * 8 + (long long)y * 8 : v * 16;
+                    const long long o1 = A.hp_out ? o0 + (long long)A.ny * 8 : v * 16 + 8;
+                    *reinterpret_cast<uint4 *>(ob0 + o0) = reinterpret_cast<const uint4 *>(ob)[0];
+                    *reinterpret_cast<uint4 *>(ob0 + o1) = reinterpret_cast<const uint4 *>(ob)[1];
                 }
             }
         }
@@ -252,9 +259,11 @@ cudaError_t launch_conv3_tc(EncodeTiledFn encode, const ConvLaunch &c, int num_s
 {
     ConvTcArgs A;
     memset(&A, 0, sizeof A);
-    // channels-last [z][x][y][16] BF16 seen as (8 ch, y, half, x, z)
+    // the BF16 input seen as (8 ch, y, half, x, z): channels-last
+    // [z][x][y][16] or half-planar [z][x][half][y][8]
     cuuint64_t dims[5] = {8, (cuuint64_t)c.ny, 2, (cuuint64_t)c.nx, (cuuint64_t)c.nz};
-    cuuint64_t strides[4] = {32, 16, (cuuint64_t)32 * c.ny, (cuuint64_t)32 * c.ny * c.nx};
+    cuuint64_t strides[4] = {c.hp_in ? 16ull : 32ull, c.hp_in ? (cuuint64_t)16 * c.ny : 16ull,
+                             (cuuint64_t)32 * c.ny, (cuuint64_t)32 * c.ny * c.nx};
     cuuint32_t box[5] = {8, kConvVox, 2, 3, 3};
     cuuint32_t estr[5] = {1, 1, 1, 1, 1};
     CUresult r = encode(&A.act, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(c.x), dims,
@@ -276,6 +285,8 @@ cudaError_t launch_conv3_tc(EncodeTiledFn encode, const ConvLaunch &c, int num_s
     A.relu = c.relu;
     A.out_fp32 = c.out_fp32;
     A.flip = c.flip;
+    A.hp_in = c.hp_in;
+    A.hp_out = c.hp_out;
     cudaError_t e = cudaFuncSetAttribute(conv3_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          kConvSmem);
     if (e != cudaSuccess)

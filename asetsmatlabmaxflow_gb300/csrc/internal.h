@@ -155,6 +155,12 @@ struct ConvLaunch {
     void *y;             // BF16 or FP32 [v][16]
     int ny, nx, nz;
     int relu, out_fp32, flip;
+    // BF16 activation layouts: 0 channels-last [z][x][y][16]; 1 half-planar
+    // [z][x][channel half][y][8] (each (z, x) row of a channel half one
+    // contiguous run, so the convolution's row loads are long bursts).  `x`
+    // and `mask` follow hp_in, a BF16 `y` hp_out; FP32 arrays are always
+    // channels-last.
+    int hp_in = 0, hp_out = 0;
 };
 cudaError_t launch_conv3_tc(EncodeTiledFn encode, const ConvLaunch &c, int num_sms,
                             cudaStream_t st, int *d_err);

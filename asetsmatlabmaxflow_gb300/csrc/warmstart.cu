@@ -101,8 +101,10 @@ constexpr int kW = 27 * 16 * 16;  // weights of one block
 constexpr int kParams = kBlocks * (kW + 16);
 constexpr int kOut = 32;          // output channels (two blocks of 16)
 
+// (Ct_1..Ct_L, alpha) -> the BF16 input of the first layer, half-planar
+// ([z][x][half][y][8], the layout of every BF16 activation of the net).
 __global__ void pack_input_kernel(const float *ct, const float *alpha, __nv_bfloat16 *x,
-                                  long long n, int L)
+                                  long long n, int L, int ny)
 {
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
          g += (long long)gridDim.x * blockDim.x) {
@@ -115,9 +117,10 @@ __global__ void pack_input_kernel(const float *ct, const float *alpha, __nv_bflo
                 f = alpha[g];
             v[c] = __float2bfloat16_rn(f);
         }
-        uint4 *o = reinterpret_cast<uint4 *>(x + g * 16);
-        o[0] = reinterpret_cast<const uint4 *>(v)[0];
-        o[1] = reinterpret_cast<const uint4 *>(v)[1];
+        const long long zx = g / ny, y = g % ny;
+        *reinterpret_cast<uint4 *>(x + (zx * 2) * ny * 8 + y * 8) = reinterpret_cast<const uint4 *>(v)[0];
+        *reinterpret_cast<uint4 *>(x + (zx * 2 + 1) * ny * 8 + y * 8) =
+            reinterpret_cast<const uint4 *>(v)[1];
     }
 }
 
@@ -177,10 +180,10 @@ __global__ void unpack_output_kernel(const float *out, NetIO io, long long n, in
 }
 
 // Mean squared error over the 5L+1 used output channels; writes the
-// gradient w.r.t. the output (BF16, same [2][n][16] layout) and accumulates
-// the loss.
+// gradient w.r.t. the output (BF16, per 16-channel block half-planar like
+// the activations: [2][z][x][half][y][8]) and accumulates the loss.
 __global__ void loss_kernel(const float *out, const float *tgt, __nv_bfloat16 *g, long long n,
-                            int used, float scale, float *loss)
+                            int used, float scale, float *loss, int ny)
 {
     float acc = 0.f;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < 2 * n * 16;
@@ -191,7 +194,10 @@ __global__ void loss_kernel(const float *out, const float *tgt, __nv_bfloat16 *g
             d = out[i] - tgt[i];
             acc += d * d;
         }
-        g[i] = __float2bfloat16_rn(2.f * d * scale);
+        const long long blk = i / (n * 16), v = (i / 16) % n, cc = i & 15;
+        const long long zx = v / ny, y = v % ny;
+        g[blk * n * 16 + (zx * 2 + cc / 8) * ny * 8 + y * 8 + (cc & 7)] =
+            __float2bfloat16_rn(2.f * d * scale);
     }
     for (int o = 16; o > 0; o >>= 1)
         acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -385,6 +391,8 @@ static ConvLaunch conv_of(asets_wsnet *n, int b, const void *x, void *y, int Ny,
     c.ny = Ny;
     c.nx = Nx;
     c.nz = Nz;
+    c.hp_in = 1;   // the net's BF16 activations are half-planar
+    c.hp_out = 1;
     return c;
 }
 
@@ -399,7 +407,7 @@ static asets_status ws_forward(asets_wsnet *n, int Ny, int Nx, int Nz, const flo
     cudaStream_t st = context_stream(n->ctx);
     const int sms = context_num_sms(n->ctx);
     EncodeTiledFn enc = context_encoder(n->ctx);
-    pack_input_kernel<<<blocks_for(vox, 256, sms), 256, 0, st>>>(ct, alpha, n->x0, vox, n->L);
+    pack_input_kernel<<<blocks_for(vox, 256, sms), 256, 0, st>>>(ct, alpha, n->x0, vox, n->L, Ny);
     WS_TRY(cudaGetLastError());
     WS_TRY(cudaMemsetAsync(n->err, 0, 4, st));
     const void *in = n->x0;
@@ -465,14 +473,14 @@ static asets_status ws_backward(asets_wsnet *n, int Ny, int Nx, int Nz, const fl
     const int used = 5 * n->L + 1;
     const float scale = 1.0f / (float)((double)vox * used);
     loss_kernel<<<blocks_for(vox * 32, 256, sms), 256, 0, st>>>(n->out, n->tgt, n->gout, vox, used,
-                                                                scale, n->loss);
+                                                                scale, n->loss, Ny);
     WS_TRY(cudaGetLastError());
     // output blocks 3 and 4: weight gradients, then the data gradient
     // flip(g3, W3) + flip(g4, W4), masked by the ReLU of act[2]
     for (int b = 3; b < kBlocks; ++b) {
         float *gw = n->grads + (size_t)b * (kW + 16);
         WS_TRY(launch_wgrad_tc(enc, n->act[2], n->gout + (size_t)(b - 3) * vox * 16, gw, gw + kW,
-                               Ny, Nx, Nz, n->wg_partial, sms, n->err, st));
+                               Ny, Nx, Nz, n->wg_partial, sms, n->err, st, 1));
     }
     {
         ConvLaunch c = conv_of(n, 3, n->gout, n->part, Ny, Nx, Nz);
@@ -491,7 +499,7 @@ static asets_status ws_backward(asets_wsnet *n, int Ny, int Nx, int Nz, const fl
     for (int l = 2; l >= 0; --l) {
         float *gw = n->grads + (size_t)l * (kW + 16);
         WS_TRY(launch_wgrad_tc(enc, ins[l], n->gbuf[cur], gw, gw + kW, Ny, Nx, Nz, n->wg_partial,
-                               sms, n->err, st));
+                               sms, n->err, st, 1));
         if (l == 0)
             break;
         ConvLaunch c = conv_of(n, l, n->gbuf[cur], n->gbuf[cur ^ 1], Ny, Nx, Nz);

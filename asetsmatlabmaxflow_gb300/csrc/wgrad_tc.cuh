@@ -201,16 +201,18 @@ __global__ void wgrad_tc_reduce_kernel(const float *partial, int nblocks, float 
 }
 
 // Tensor maps of the two operands, the launch, the reduction.  `partial`
-// holds num_sms x 28 x 256 floats.
+// holds num_sms x 28 x 256 floats.  `hp`: both BF16 arrays half-planar
+// ([z][x][half][y][8]) instead of channels-last ([z][x][y][16]).
 inline cudaError_t launch_wgrad_tc(EncodeTiledFn encode, const __nv_bfloat16 *act,
                                    const __nv_bfloat16 *grad, float *dw, float *db, int ny, int nx,
                                    int nz, float *partial, int num_sms, int *d_err,
-                                   cudaStream_t st)
+                                   cudaStream_t st, int hp = 0)
 {
     WgradTcArgs A;
     memset(&A, 0, sizeof A);
     cuuint64_t dims[5] = {8, (cuuint64_t)ny, 2, (cuuint64_t)nx, (cuuint64_t)nz};
-    cuuint64_t strides[4] = {32, 16, (cuuint64_t)32 * ny, (cuuint64_t)32 * ny * nx};
+    cuuint64_t strides[4] = {hp ? 16ull : 32ull, hp ? (cuuint64_t)16 * ny : 16ull,
+                             (cuuint64_t)32 * ny, (cuuint64_t)32 * ny * nx};
     cuuint32_t box_a[5] = {8, 130, 2, 3, 3};
     cuuint32_t box_g[5] = {8, 128, 2, 1, 1};
     cuuint32_t estr[5] = {1, 1, 1, 1, 1};
