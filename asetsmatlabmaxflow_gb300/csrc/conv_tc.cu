@@ -28,11 +28,11 @@ constexpr int kConvThreads = 192;            // warp 0: TMA, warp 1: MMA, warps 
 constexpr int kConvStages = 4;               // TMA ring depth
 constexpr int kConvAcc = 8;                  // TMEM accumulators (16 FP32 columns each)
 constexpr int kConvRows = 9;                 // (dz, dx) neighbour rows
-constexpr int kConvVox = 130;                // y-1 .. y+128
-constexpr int kConvHalfBytes = kConvVox * 16;           // 8 channels x 2 B per voxel
-constexpr int kConvRowBytes = 2 * kConvHalfBytes;       // both channel halves
-constexpr int kConvStageBytes = kConvRows * kConvRowBytes;   // 37,440 B delivered by TMA
-constexpr int kConvStageStride = (kConvStageBytes + 127) / 128 * 128;
+// Staged voxels per row: channels-last input y-1 .. y+128 (130, loaded in
+// 16-byte runs); half-planar input y-8 .. y+135 (144 = 18 groups of 8
+// voxels, loaded in 128-byte runs from rows padded to a multiple of 8).
+constexpr int kConvVoxCL = 130, kConvVoxHP = 144;
+constexpr int kConvStageStride = (kConvRows * 2 * kConvVoxHP * 16 + 127) / 128 * 128;  // 41,472
 constexpr int kConvTapBytes = 2 * 16 * 16;              // B operand of one tap
 constexpr int kConvWBytes = 27 * kConvTapBytes;         // 13,824 B
 // + 32 KB: operand descriptors can only address inside the allocation
@@ -49,6 +49,9 @@ struct ConvTcArgs {
     int ny, nx, nz, ytiles;
     int relu, out_fp32, flip;
     int hp_in, hp_out;         // half-planar BF16 input (and mask) / output
+    int ypad;                  // half-planar row length (ny rounded up to 8)
+    int half_bytes, row_bytes, stage_bytes;  // staged layout: [row][half][voxel][8]
+    int vox_base;              // staged voxel of y - 1 is vox_base - 1 (1 or 8)
 };
 
 // Warp-specialised: warp 0 (one lane) keeps a ring of kConvStages tile
@@ -116,9 +119,13 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv3_tc_kernel(const __grid_
                 const int tile = blockIdx.x + j * gridDim.x;
                 const int yt = tile % A.ytiles, rest = tile / A.ytiles;
                 const int x = rest % A.nx, z = rest / A.nx;
-                mbar_arrive_expect_tx(&full_bar[st], kConvStageBytes);
-                tma_load_5d(smem + st * kConvStageStride, &A.act, 0, yt * 128 - 1, 0, x - 1, z - 1,
-                            &full_bar[st]);
+                mbar_arrive_expect_tx(&full_bar[st], A.stage_bytes);
+                if (A.hp_in)  // 18 groups of 8 voxels from y - 8
+                    tma_load_5d(smem + st * kConvStageStride, &A.act, 0, yt * 16 - 1, 0, x - 1,
+                                z - 1, &full_bar[st]);
+                else
+                    tma_load_5d(smem + st * kConvStageStride, &A.act, 0, yt * 128 - 1, 0, x - 1,
+                                z - 1, &full_bar[st]);
                 ++issued;
             }
             if (s_abort) {
@@ -143,11 +150,12 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv3_tc_kernel(const __grid_
                     !mbar_wait_bounded(&acce_bar[slot], ((j / kConvAcc) - 1) & 1, &s_abort))
                     break;
                 tc_fence_after_sync();
-                const uint32_t a0 = smem_addr(smem + st * kConvStageStride);
+                const uint32_t a0 =
+                    smem_addr(smem + st * kConvStageStride) + (A.vox_base - 1) * 16;
                 for (int t = 0; t < 27; ++t) {
                     const int dz = t / 9, dx = (t / 3) % 3, dy = t % 3;
-                    const uint32_t a = a0 + (dz * 3 + dx) * kConvRowBytes + dy * 16;
-                    const uint64_t ad = umma_smem_desc(a, kConvHalfBytes, 128);
+                    const uint32_t a = a0 + (dz * 3 + dx) * A.row_bytes + dy * 16;
+                    const uint64_t ad = umma_smem_desc(a, A.half_bytes, 128);
                     const uint64_t bd = umma_smem_desc(b0 + t * kConvTapBytes, 256, 128);
                     umma_bf16(tmem + slot * 16, ad, bd, idesc, t > 0 ? 1u : 0u);
                 }
@@ -209,8 +217,8 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv3_tc_kernel(const __grid_
                 }
                 // element offsets of the voxel's two channel halves in the input layout
                 const long long zx = (long long)z * A.nx + x;
-                const long long h0 = A.hp_in ? (zx * 2) * A.ny * 8 + (long long)y * 8 : v * 16;
-                const long long h1 = A.hp_in ? h0 + (long long)A.ny * 8 : v * 16 + 8;
+                const long long h0 = A.hp_in ? (zx * 2) * A.ypad * 8 + (long long)y * 8 : v * 16;
+                const long long h1 = A.hp_in ? h0 + (long long)A.ypad * 8 : v * 16 + 8;
                 if (A.mask) {
                     const uint4 m0 = __ldg(reinterpret_cast<const uint4 *>(A.mask + h0));
                     const uint4 m1 = __ldg(reinterpret_cast<const uint4 *>(A.mask + h1));
@@ -235,8 +243,8 @@ __global__ void __launch_bounds__(kConvThreads, 1) conv3_tc_kernel(const __grid_
                     for (int c = 0; c < 16; ++c)
                         ob[c] = __float2bfloat16_rn(o[c]);
                     __nv_bfloat16 *ob0 = static_cast<__nv_bfloat16 *>(A.out);
-                    const long long o0 = A.hp_out ? (zx * 2) * A.ny * 8 + (long long)y * 8 : v * 16;
-                    const long long o1 = A.hp_out ? o0 + (long long)A.ny * 8 : v * 16 + 8;
+                    const long long o0 = A.hp_out ? (zx * 2) * A.ypad * 8 + (long long)y * 8 : v * 16;
+                    const long long o1 = A.hp_out ? o0 + (long long)A.ypad * 8 : v * 16 + 8;
                     *reinterpret_cast<uint4 *>(ob0 + o0) = reinterpret_cast<const uint4 *>(ob)[0];
                     *reinterpret_cast<uint4 *>(ob0 + o1) = reinterpret_cast<const uint4 *>(ob)[1];
                 }
@@ -259,12 +267,28 @@ cudaError_t launch_conv3_tc(EncodeTiledFn encode, const ConvLaunch &c, int num_s
 {
     ConvTcArgs A;
     memset(&A, 0, sizeof A);
-    // the BF16 input seen as (8 ch, y, half, x, z): channels-last
-    // [z][x][y][16] or half-planar [z][x][half][y][8]
-    cuuint64_t dims[5] = {8, (cuuint64_t)c.ny, 2, (cuuint64_t)c.nx, (cuuint64_t)c.nz};
-    cuuint64_t strides[4] = {c.hp_in ? 16ull : 32ull, c.hp_in ? (cuuint64_t)16 * c.ny : 16ull,
-                             (cuuint64_t)32 * c.ny, (cuuint64_t)32 * c.ny * c.nx};
-    cuuint32_t box[5] = {8, kConvVox, 2, 3, 3};
+    // The BF16 input as (8 ch, y, half, x, z) for channels-last
+    // [z][x][y][16]; half-planar [z][x][half][ypad][8] as (64 = 8 voxels x 8
+    // ch, ypad/8 groups, half, x, z), whose 128-byte inner box is one burst.
+    const int ypad = (c.ny + 7) / 8 * 8;
+    cuuint64_t dims[5], strides[4];
+    cuuint32_t box[5];
+    if (c.hp_in) {
+        const cuuint64_t d[5] = {64, (cuuint64_t)ypad / 8, 2, (cuuint64_t)c.nx, (cuuint64_t)c.nz};
+        const cuuint64_t s[4] = {128, (cuuint64_t)16 * ypad, (cuuint64_t)32 * ypad,
+                                 (cuuint64_t)32 * ypad * c.nx};
+        const cuuint32_t b[5] = {64, kConvVoxHP / 8, 2, 3, 3};
+        memcpy(dims, d, sizeof d);
+        memcpy(strides, s, sizeof s);
+        memcpy(box, b, sizeof b);
+    } else {
+        const cuuint64_t d[5] = {8, (cuuint64_t)c.ny, 2, (cuuint64_t)c.nx, (cuuint64_t)c.nz};
+        const cuuint64_t s[4] = {32, 16, (cuuint64_t)32 * c.ny, (cuuint64_t)32 * c.ny * c.nx};
+        const cuuint32_t b[5] = {8, kConvVoxCL, 2, 3, 3};
+        memcpy(dims, d, sizeof d);
+        memcpy(strides, s, sizeof s);
+        memcpy(box, b, sizeof b);
+    }
     cuuint32_t estr[5] = {1, 1, 1, 1, 1};
     CUresult r = encode(&A.act, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void *>(c.x), dims,
                         strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -287,6 +311,12 @@ cudaError_t launch_conv3_tc(EncodeTiledFn encode, const ConvLaunch &c, int num_s
     A.flip = c.flip;
     A.hp_in = c.hp_in;
     A.hp_out = c.hp_out;
+    A.ypad = ypad;
+    const int vox = c.hp_in ? kConvVoxHP : kConvVoxCL;
+    A.half_bytes = vox * 16;
+    A.row_bytes = 2 * vox * 16;
+    A.stage_bytes = kConvRows * A.row_bytes;
+    A.vox_base = c.hp_in ? 8 : 1;
     cudaError_t e = cudaFuncSetAttribute(conv3_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          kConvSmem);
     if (e != cudaSuccess)

@@ -102,7 +102,7 @@ constexpr int kParams = kBlocks * (kW + 16);
 constexpr int kOut = 32;          // output channels (two blocks of 16)
 
 // (Ct_1..Ct_L, alpha) -> the BF16 input of the first layer, half-planar
-// ([z][x][half][y][8], the layout of every BF16 activation of the net).
+// ([z][x][half][ypad][8], the layout of every BF16 activation of the net).
 __global__ void pack_input_kernel(const float *ct, const float *alpha, __nv_bfloat16 *x,
                                   long long n, int L, int ny)
 {
@@ -117,9 +117,9 @@ __global__ void pack_input_kernel(const float *ct, const float *alpha, __nv_bflo
                 f = alpha[g];
             v[c] = __float2bfloat16_rn(f);
         }
-        const long long zx = g / ny, y = g % ny;
-        *reinterpret_cast<uint4 *>(x + (zx * 2) * ny * 8 + y * 8) = reinterpret_cast<const uint4 *>(v)[0];
-        *reinterpret_cast<uint4 *>(x + (zx * 2 + 1) * ny * 8 + y * 8) =
+        const long long zx = g / ny, y = g % ny, yp = (ny + 7) / 8 * 8;
+        *reinterpret_cast<uint4 *>(x + (zx * 2) * yp * 8 + y * 8) = reinterpret_cast<const uint4 *>(v)[0];
+        *reinterpret_cast<uint4 *>(x + (zx * 2 + 1) * yp * 8 + y * 8) =
             reinterpret_cast<const uint4 *>(v)[1];
     }
 }
@@ -181,7 +181,7 @@ __global__ void unpack_output_kernel(const float *out, NetIO io, long long n, in
 
 // Mean squared error over the 5L+1 used output channels; writes the
 // gradient w.r.t. the output (BF16, per 16-channel block half-planar like
-// the activations: [2][z][x][half][y][8]) and accumulates the loss.
+// the activations: [2][z][x][half][ypad][8]) and accumulates the loss.
 __global__ void loss_kernel(const float *out, const float *tgt, __nv_bfloat16 *g, long long n,
                             int used, float scale, float *loss, int ny)
 {
@@ -195,8 +195,9 @@ __global__ void loss_kernel(const float *out, const float *tgt, __nv_bfloat16 *g
             acc += d * d;
         }
         const long long blk = i / (n * 16), v = (i / 16) % n, cc = i & 15;
-        const long long zx = v / ny, y = v % ny;
-        g[blk * n * 16 + (zx * 2 + cc / 8) * ny * 8 + y * 8 + (cc & 7)] =
+        const long long zx = v / ny, y = v % ny, yp = (ny + 7) / 8 * 8;
+        const long long pn = yp * (n / ny);  // padded voxels of one 16-channel block
+        g[blk * pn * 16 + (zx * 2 + cc / 8) * yp * 8 + y * 8 + (cc & 7)] =
             __float2bfloat16_rn(2.f * d * scale);
     }
     for (int o = 16; o > 0; o >>= 1)
@@ -246,7 +247,8 @@ struct asets_wsnet {
     __nv_bfloat16 *w16 = nullptr;
     float *loss = nullptr;
     int *err = nullptr;
-    long long vox_cap = 0;
+    long long vox_cap = 0, pvox_cap = 0;
+    int shape[3] = {0, 0, 0};         // volume the half-planar padding was cleared for
     __nv_bfloat16 *x0 = nullptr, *act[3] = {nullptr, nullptr, nullptr};
     __nv_bfloat16 *gbuf[2] = {nullptr, nullptr};  // [v][16] gradients of hidden layers
     __nv_bfloat16 *gout = nullptr;                // [2][v][16] gradient of the output
@@ -256,11 +258,29 @@ struct asets_wsnet {
     int step = 0;
 };
 
-static asets_status ws_reserve(asets_wsnet *n, long long vox)
+// Buffers for a Ny x Nx x Nz volume.  The BF16 activations and gradients
+// are half-planar with rows padded to ypad = Ny rounded up to 8 voxels
+// (pvox = ypad * Nx * Nz per 16-channel block); the convolutions read the
+// padding, so it must be zero: every buffer is cleared when the shape
+// changes (the kernels write real voxels only).
+static asets_status ws_reserve(asets_wsnet *n, int Ny, int Nx, int Nz)
 {
-    if (vox <= n->vox_cap)
-        return ASETS_OK;
+    const long long vox = (long long)Ny * Nx * Nz;
+    const long long pvox = (long long)((Ny + 7) / 8 * 8) * Nx * Nz;
     cudaStream_t st = context_stream(n->ctx);
+    const bool same = (Ny == n->shape[0] && Nx == n->shape[1] && Nz == n->shape[2]);
+    if (vox <= n->vox_cap && pvox <= n->pvox_cap) {
+        if (!same) {
+            __nv_bfloat16 *hp[] = {n->x0, n->act[0], n->act[1], n->act[2], n->gbuf[0], n->gbuf[1]};
+            for (__nv_bfloat16 *b : hp)
+                WS_TRY(cudaMemsetAsync(b, 0, (size_t)pvox * 32, st));
+            WS_TRY(cudaMemsetAsync(n->gout, 0, (size_t)pvox * 64, st));
+            n->shape[0] = Ny;
+            n->shape[1] = Nx;
+            n->shape[2] = Nz;
+        }
+        return ASETS_OK;
+    }
     void **bufs[] = {(void **)&n->x0,      (void **)&n->act[0], (void **)&n->act[1],
                      (void **)&n->act[2],  (void **)&n->gbuf[0], (void **)&n->gbuf[1],
                      (void **)&n->gout,    (void **)&n->out,    (void **)&n->tgt,
@@ -271,11 +291,19 @@ static asets_status ws_reserve(asets_wsnet *n, long long vox)
             *b = nullptr;
         }
     n->vox_cap = 0;
-    const size_t b16 = (size_t)vox * 16 * sizeof(__nv_bfloat16), f32 = (size_t)vox * 16 * 4;
+    n->pvox_cap = 0;
+    const size_t b16 = (size_t)pvox * 16 * sizeof(__nv_bfloat16), f32 = (size_t)vox * 16 * 4;
     const size_t sizes[] = {b16, b16, b16, b16, b16, b16, 2 * b16, 2 * f32, 2 * f32, f32};
-    for (int i = 0; i < 10; ++i)
+    for (int i = 0; i < 10; ++i) {
         WS_TRY(cudaMallocAsync(bufs[i], sizes[i], st));
+        if (i < 7)
+            WS_TRY(cudaMemsetAsync(*bufs[i], 0, sizes[i], st));
+    }
     n->vox_cap = vox;
+    n->pvox_cap = pvox;
+    n->shape[0] = Ny;
+    n->shape[1] = Nx;
+    n->shape[2] = Nz;
     return ASETS_OK;
 }
 
@@ -401,7 +429,7 @@ static asets_status ws_forward(asets_wsnet *n, int Ny, int Nx, int Nz, const flo
                                const float *alpha)
 {
     const long long vox = (long long)Ny * Nx * Nz;
-    asets_status s = ws_reserve(n, vox);
+    asets_status s = ws_reserve(n, Ny, Nx, Nz);
     if (s != ASETS_OK)
         return s;
     cudaStream_t st = context_stream(n->ctx);
@@ -465,6 +493,7 @@ static asets_status ws_backward(asets_wsnet *n, int Ny, int Nx, int Nz, const fl
     if (s != ASETS_OK)
         return s;
     const long long vox = (long long)Ny * Nx * Nz;
+    const long long pvox = (long long)((Ny + 7) / 8 * 8) * Nx * Nz;  // a padded half-planar block
     cudaStream_t st = context_stream(n->ctx);
     const int sms = context_num_sms(n->ctx);
     EncodeTiledFn enc = context_encoder(n->ctx);
@@ -479,7 +508,7 @@ static asets_status ws_backward(asets_wsnet *n, int Ny, int Nx, int Nz, const fl
     // flip(g3, W3) + flip(g4, W4), masked by the ReLU of act[2]
     for (int b = 3; b < kBlocks; ++b) {
         float *gw = n->grads + (size_t)b * (kW + 16);
-        WS_TRY(launch_wgrad_tc(enc, n->act[2], n->gout + (size_t)(b - 3) * vox * 16, gw, gw + kW,
+        WS_TRY(launch_wgrad_tc(enc, n->act[2], n->gout + (size_t)(b - 3) * pvox * 16, gw, gw + kW,
                                Ny, Nx, Nz, n->wg_partial, sms, n->err, st, 1));
     }
     {
@@ -487,7 +516,7 @@ static asets_status ws_backward(asets_wsnet *n, int Ny, int Nx, int Nz, const fl
         c.flip = 1;
         c.out_fp32 = 1;
         WS_TRY(launch_conv3_tc(enc, c, sms, st, n->err));
-        ConvLaunch d = conv_of(n, 4, n->gout + (size_t)vox * 16, n->gbuf[0], Ny, Nx, Nz);
+        ConvLaunch d = conv_of(n, 4, n->gout + (size_t)pvox * 16, n->gbuf[0], Ny, Nx, Nz);
         d.flip = 1;
         d.addend = n->part;
         d.mask = n->act[2];

@@ -37,10 +37,9 @@ namespace asets {
 constexpr int kWgtThreads = 128;
 constexpr int kWgtStages = 3;
 constexpr int kWgtTaps = 28;                               // 27 taps + bias
-constexpr int kWgtActBytes = 9 * 2 * 130 * 16;             // 37,440: 3x3 rows, y-1..y+128
-constexpr int kWgtActStride = (kWgtActBytes + 127) / 128 * 128;
-constexpr int kWgtActHalf = 130 * 16;                      // bytes between channel halves
-constexpr int kWgtActRow = 2 * kWgtActHalf;
+// staged activation rows: 130 voxels y-1 .. y+128 (channels-last input) or
+// 144 voxels y-8 .. y+135 (half-planar input, 128-byte loads), as in conv_tc.cu
+constexpr int kWgtActStride = (9 * 2 * 144 * 16 + 127) / 128 * 128;  // 41,472
 constexpr int kWgtGradBytes = 2 * 128 * 16;                // [half][128 voxels][8 co]
 constexpr int kWgtOnesBytes = 512;                         // [2 halves][16 voxels][8] ones
 // gradient stages first: an M = 128 A operand reads 16 core-matrix rows
@@ -53,11 +52,13 @@ static_assert(kWgtGradOff + (kWgtStages - 1) * kWgtGradBytes + 16 * 2048 <= kWgt
               "the padded A operand must stay inside the shared memory");
 
 struct WgradTcArgs {
-    CUtensorMap act;     // 5D view (8 ch, y, half, x, z) of the BF16 input, box {8,130,2,3,3}
-    CUtensorMap grad;    // same view of the BF16 output gradient, box {8,128,2,1,1}
+    CUtensorMap act;     // the BF16 input, staged 3x3 rows as [row][half][voxel][8]
+    CUtensorMap grad;    // the BF16 output gradient, staged [half][128 voxels][8]
     float *partial;      // [gridDim.x][28][16 ci][16 co]
     int *err;
     int ny, nx, nz, ytiles;
+    int hp;                                  // half-planar operands
+    int act_half, act_row, act_bytes, vox_base;
 };
 
 __global__ void __launch_bounds__(kWgtThreads, 1)
@@ -100,11 +101,11 @@ __global__ void __launch_bounds__(kWgtThreads, 1)
         const int st = j % kWgtStages;
         const int yt = tile % A.ytiles, rest = tile / A.ytiles;
         const int x = rest % A.nx, z = rest / A.nx;
-        mbar_arrive_expect_tx(&full_bar[st], kWgtActBytes + kWgtGradBytes);
-        tma_load_5d(smem + kWgtActOff + st * kWgtActStride, &A.act, 0, yt * 128 - 1, 0, x - 1, z - 1,
-                    &full_bar[st]);
-        tma_load_5d(smem + kWgtGradOff + st * kWgtGradBytes, &A.grad, 0, yt * 128, 0, x, z,
-                    &full_bar[st]);
+        mbar_arrive_expect_tx(&full_bar[st], A.act_bytes + kWgtGradBytes);
+        tma_load_5d(smem + kWgtActOff + st * kWgtActStride, &A.act, 0,
+                    A.hp ? yt * 16 - 1 : yt * 128 - 1, 0, x - 1, z - 1, &full_bar[st]);
+        tma_load_5d(smem + kWgtGradOff + st * kWgtGradBytes, &A.grad, 0, A.hp ? yt * 16 : yt * 128,
+                    0, x, z, &full_bar[st]);
     };
 
     bool ok = true;
@@ -121,7 +122,8 @@ __global__ void __launch_bounds__(kWgtThreads, 1)
                 break;
             tc_fence_after_sync();
             const uint32_t g0 = smem_addr(smem + kWgtGradOff + st * kWgtGradBytes);
-            const uint32_t a0 = smem_addr(smem + kWgtActOff + st * kWgtActStride);
+            const uint32_t a0 =
+                smem_addr(smem + kWgtActOff + st * kWgtActStride) + (A.vox_base - 1) * 16;
             for (int ks = 0; ks < 8; ++ks) {  // 16 voxels per MMA
                 // A: co x voxels, core matrices 8 voxels x 8 co; K step 128 B, M step 2,048 B
                 const uint64_t ad = umma_smem_desc(g0 + ks * 256, 128, 2048);
@@ -129,8 +131,8 @@ __global__ void __launch_bounds__(kWgtThreads, 1)
                 for (int t = 0; t < 27; ++t) {
                     const int dz = t / 9, dx = (t / 3) % 3, dy = t % 3;
                     // B: ci x voxels of the tap's row, shifted by dy; N step: channel half
-                    const uint32_t b = a0 + (dz * 3 + dx) * kWgtActRow + (dy + 16 * ks) * 16;
-                    const uint64_t bd = umma_smem_desc(b, 128, kWgtActHalf);
+                    const uint32_t b = a0 + (dz * 3 + dx) * A.act_row + (dy + 16 * ks) * 16;
+                    const uint64_t bd = umma_smem_desc(b, 128, A.act_half);
                     umma_bf16(tmem + t * 16, ad, bd, idesc, acc);
                 }
                 umma_bf16(tmem + 27 * 16, ad, umma_smem_desc(ones, 128, 256), idesc, acc);
@@ -210,11 +212,23 @@ inline cudaError_t launch_wgrad_tc(EncodeTiledFn encode, const __nv_bfloat16 *ac
 {
     WgradTcArgs A;
     memset(&A, 0, sizeof A);
+    const int ypad = (ny + 7) / 8 * 8;
+    // channels-last: (8 ch, y, half, x, z); half-planar [z][x][half][ypad][8]:
+    // (8 voxels x 8 ch, ypad / 8, half, x, z)
     cuuint64_t dims[5] = {8, (cuuint64_t)ny, 2, (cuuint64_t)nx, (cuuint64_t)nz};
-    cuuint64_t strides[4] = {hp ? 16ull : 32ull, hp ? (cuuint64_t)16 * ny : 16ull,
-                             (cuuint64_t)32 * ny, (cuuint64_t)32 * ny * nx};
+    cuuint64_t strides[4] = {32, 16, (cuuint64_t)32 * ny, (cuuint64_t)32 * ny * nx};
     cuuint32_t box_a[5] = {8, 130, 2, 3, 3};
     cuuint32_t box_g[5] = {8, 128, 2, 1, 1};
+    if (hp) {
+        const cuuint64_t d[5] = {64, (cuuint64_t)ypad / 8, 2, (cuuint64_t)nx, (cuuint64_t)nz};
+        const cuuint64_t s[4] = {128, (cuuint64_t)16 * ypad, (cuuint64_t)32 * ypad,
+                                 (cuuint64_t)32 * ypad * nx};
+        const cuuint32_t ba[5] = {64, 18, 2, 3, 3}, bg[5] = {64, 16, 2, 1, 1};
+        memcpy(dims, d, sizeof d);
+        memcpy(strides, s, sizeof s);
+        memcpy(box_a, ba, sizeof ba);
+        memcpy(box_g, bg, sizeof bg);
+    }
     cuuint32_t estr[5] = {1, 1, 1, 1, 1};
     CUresult r = encode(&A.act, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<__nv_bfloat16 *>(act),
                         dims, strides, box_a, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -233,6 +247,12 @@ inline cudaError_t launch_wgrad_tc(EncodeTiledFn encode, const __nv_bfloat16 *ac
     A.nx = nx;
     A.nz = nz;
     A.ytiles = (ny + 127) / 128;
+    A.hp = hp;
+    const int vox = hp ? 144 : 130;
+    A.act_half = vox * 16;
+    A.act_row = 2 * vox * 16;
+    A.act_bytes = 9 * A.act_row;
+    A.vox_base = hp ? 8 : 1;
     cudaError_t e = cudaFuncSetAttribute(wgrad_tc_kernel,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, kWgtSmem);
     if (e != cudaSuccess)

@@ -11,9 +11,20 @@
 
 #include "wgrad_tc.cuh"
 
+// element index of (z, x, y, channel c): channels-last, or half-planar with
+// rows padded to ypad
+__device__ __forceinline__ long long at(int hp, int ny, int nx, int z, int x, int y, int c)
+{
+    const long long zx = (long long)z * nx + x;
+    if (!hp)
+        return (zx * ny + y) * 16 + c;
+    const long long yp = (ny + 7) / 8 * 8;
+    return (zx * 2 + c / 8) * yp * 8 + (long long)y * 8 + (c & 7);
+}
+
 // reference: one thread per (tap, ci, co) or bias co, summing over all voxels in double
 __global__ void wgrad_ref_kernel(const __nv_bfloat16 *a, const __nv_bfloat16 *g, int ny, int nx,
-                                 int nz, double *dw, double *dabs)
+                                 int nz, int hp, double *dw, double *dabs)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 27 * 256 + 16)
@@ -25,13 +36,12 @@ __global__ void wgrad_ref_kernel(const __nv_bfloat16 *a, const __nv_bfloat16 *g,
     for (int z = 0; z < nz; ++z)
         for (int x = 0; x < nx; ++x)
             for (int y = 0; y < ny; ++y) {
-                const double gv = __bfloat162float(g[(((long long)z * nx + x) * ny + y) * 16 + co]);
+                const double gv = __bfloat162float(g[at(hp, ny, nx, z, x, y, co)]);
                 double av = 1.0;
                 if (!bias) {
                     const int zz = z + dz, xx = x + dx, yy = y + dy;
                     av = (zz >= 0 && zz < nz && xx >= 0 && xx < nx && yy >= 0 && yy < ny)
-                             ? (double)__bfloat162float(
-                                   a[(((long long)zz * nx + xx) * ny + yy) * 16 + ci])
+                             ? (double)__bfloat162float(a[at(hp, ny, nx, zz, xx, yy, ci)])
                              : 0.0;
                 }
                 s += av * gv;
@@ -53,8 +63,20 @@ __global__ void fill_kernel(__nv_bfloat16 *p, long long n, unsigned long long se
     }
 }
 
-// Returns 0 and the largest |got - ref| / (sum |a*g| + 1e-30) over all outputs.
-extern "C" __attribute__((visibility("default"))) int wgrad_check(int ny, int nx, int nz,
+// the padding voxels of a half-planar array are zero
+__global__ void zero_pad_kernel(__nv_bfloat16 *p, int ny, int nx, int nz)
+{
+    const long long yp = (ny + 7) / 8 * 8;
+    const long long n = yp * nx * nz * 16;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        if ((i / 8) % yp >= ny)
+            p[i] = __float2bfloat16_rn(0.f);
+}
+
+// Returns 0 and the largest |got - ref| / (sum |a*g| + 1e-30) over all
+// outputs; hp: both operands half-planar with padded rows.
+extern "C" __attribute__((visibility("default"))) int wgrad_check(int ny, int nx, int nz, int hp,
                                                                   double *worst_out)
 {
     void *fn = nullptr;
@@ -65,7 +87,7 @@ extern "C" __attribute__((visibility("default"))) int wgrad_check(int ny, int nx
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long vox = (long long)ny * nx * nz;
+    const long long vox = (long long)((ny + 7) / 8 * 8) * nx * nz;  // with padding
     __nv_bfloat16 *a = nullptr, *g = nullptr;
     float *dw = nullptr, *partial = nullptr;
     double *ref = nullptr, *rabs = nullptr;
@@ -77,12 +99,16 @@ extern "C" __attribute__((visibility("default"))) int wgrad_check(int ny, int nx
         return 2;
     fill_kernel<<<256, 256>>>(a, vox * 16, 11);
     fill_kernel<<<256, 256>>>(g, vox * 16, 29);
+    if (hp) {
+        zero_pad_kernel<<<256, 256>>>(a, ny, nx, nz);
+        zero_pad_kernel<<<256, 256>>>(g, ny, nx, nz);
+    }
     cudaMemset(dw, 0, (27 * 256 + 16) * 4);
     cudaMemset(err, 0, 4);
     if (asets::launch_wgrad_tc(reinterpret_cast<asets::EncodeTiledFn>(fn), a, g, dw, dw + 27 * 256,
-                               ny, nx, nz, partial, sms, err, 0) != cudaSuccess)
+                               ny, nx, nz, partial, sms, err, 0, hp) != cudaSuccess)
         return 3;
-    wgrad_ref_kernel<<<(27 * 256 + 16 + 127) / 128, 128>>>(a, g, ny, nx, nz, ref, rabs);
+    wgrad_ref_kernel<<<(27 * 256 + 16 + 127) / 128, 128>>>(a, g, ny, nx, nz, hp, ref, rabs);
     if (cudaDeviceSynchronize() != cudaSuccess)
         return 4;
     int herr = 0;

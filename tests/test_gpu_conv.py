@@ -87,19 +87,21 @@ def wgrad_lib(tmp_path_factory):
                     f"-I{build.INCLUDE}", "-shared", "-o", str(out),
                     str(root / "tests" / "cuda" / "wgrad_check.cu"), "-lcuda"], check=True)
     lib = ctypes.CDLL(str(out))
-    lib.wgrad_check.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+    lib.wgrad_check.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                 ctypes.POINTER(ctypes.c_double)]
     lib.wgrad_check.restype = ctypes.c_int
     return lib
 
 
+@pytest.mark.parametrize("hp", [0, 1])
 @pytest.mark.parametrize("dims", [(150, 3, 3), (128, 4, 5), (260, 2, 2), (37, 6, 3)])
-def test_tensor_core_weight_gradient_matches_double_reference(wgrad_lib, dims):
+def test_tensor_core_weight_gradient_matches_double_reference(wgrad_lib, dims, hp):
     """The tcgen05 weight and bias gradients (voxels as the GEMM's K, both
     operands MN-major) against a double-precision sum over the same BF16
-    values: error within 1e-5 of the sum of |a * g| (FP32 accumulation)."""
+    values, for channels-last and for padded half-planar operands: error
+    within 1e-5 of the sum of |a * g| (FP32 accumulation)."""
     import ctypes
 
     worst = ctypes.c_double(1.0)
-    assert wgrad_lib.wgrad_check(*dims, ctypes.byref(worst)) == 0
+    assert wgrad_lib.wgrad_check(*dims, hp, ctypes.byref(worst)) == 0
     assert worst.value < 1e-5, worst.value
