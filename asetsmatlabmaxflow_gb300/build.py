@@ -19,9 +19,14 @@ PKG = Path(__file__).resolve().parent
 REPO = PKG.parent
 CSRC = PKG / "csrc"
 MEX_DIR = PKG / "mex"
-LIB = PKG / "lib"
-OBJ = PKG / "_build"
 INCLUDE = REPO / "include"
+# ASETS_BOUNDS_CHECK=1 builds the debug flavour (-DASETS_BOUNDS_CHECK: the
+# iteration kernels check every store and shared-memory index and report a
+# violation as an error instead of making the access) into lib_check/;
+# native.py loads it when ASETS_LIB_DIR points there.
+BOUNDS_CHECK = os.environ.get("ASETS_BOUNDS_CHECK", "0") not in ("", "0")
+LIB = PKG / ("lib_check" if BOUNDS_CHECK else "lib")
+OBJ = PKG / ("_build_check" if BOUNDS_CHECK else "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -36,6 +41,9 @@ NVCC_FLAGS = [
 # bit-exactness: they may contract a*b+c into FMA and flush denormals.
 FAST_FLAGS = [f for f in NVCC_FLAGS if f not in ("-ftz=false", "--fmad=false")] + [
     "-ftz=true", "--fmad=true"]
+if BOUNDS_CHECK:
+    NVCC_FLAGS = NVCC_FLAGS + ["-DASETS_BOUNDS_CHECK"]
+    FAST_FLAGS = FAST_FLAGS + ["-DASETS_BOUNDS_CHECK"]
 
 CU_SOURCES = (
     "runtime.cu",

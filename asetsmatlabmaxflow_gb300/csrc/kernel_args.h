@@ -9,6 +9,7 @@ namespace asets {
 // Bits of IterControl::error.
 enum DeviceError : int {
     DEV_ERR_TIMEOUT = 1,  // an mbarrier wait exceeded its budget
+    DEV_ERR_BOUNDS = 2,   // bounds-check build: a store or shared-memory index out of range
 };
 
 // Per-solve control block in device memory.  Every iteration launch reads
@@ -72,6 +73,7 @@ struct ProblemDesc {
     int tiles_r, tiles_c;
     int zchunks;                           // stream-axis chunks per tile
     int item_begin, n_items;               // this problem's items in the launch
+    long long dst_elems;                   // elements of each destination array (bounds checks)
     int lab_mul[NUM_SLOTS];
     int lab_add[NUM_SLOTS];
     float cc, inv_cc, steps;

@@ -1020,6 +1020,9 @@ static asets_status finish_run(asets_solver *s, const IterControl &out, int *itN
     const int maxIt = s->last_max_it;
     if (out.error & DEV_ERR_TIMEOUT)
         return fail(ASETS_ERR_TIMEOUT, "a device-side wait for a TMA load timed out");
+    if (out.error & DEV_ERR_BOUNDS)
+        return fail(ASETS_ERR_CUDA, "an out-of-range store or shared-memory index was caught "
+                    "(bounds-check build)");
     if (maxIt > 0 && !out.done)
         return fail(ASETS_ERR_CUDA, "iteration loop ended without completion (iter=%d)", out.iter);
     // The state after iteration k is in parity (k & 1).  With two

@@ -130,6 +130,43 @@ __device__ __forceinline__ void st_cells_if(float *__restrict__ p, const float (
         p[0] = v[0];
     }
 }
+// st_cells_if at element offset `off` of a destination array of the
+// problem.  The bounds-check build (-DASETS_BOUNDS_CHECK) first checks that
+// every stored cell lies inside the array (P.dst_elems elements) and
+// otherwise records DEV_ERR_BOUNDS and stores nothing.
+template <int CELLS>
+__device__ __forceinline__ void st_dst(float *__restrict__ base, unsigned int off,
+                                       const float (&v)[CELLS], const bool (&ok)[CELLS],
+                                       const ProblemDesc &P)
+{
+#ifdef ASETS_BOUNDS_CHECK
+    int last = -1;
+#pragma unroll
+    for (int j = 0; j < CELLS; ++j)
+        if (ok[j])
+            last = j;
+    if (last >= 0 && (long long)off + last >= P.dst_elems) {
+        atomicOr(&P.ctl->error, DEV_ERR_BOUNDS);
+        return;
+    }
+#endif
+    st_cells_if<CELLS>(base + off, v, ok);
+}
+
+// Bounds-check build: record DEV_ERR_BOUNDS when a shared-memory index of
+// the thread is outside [0, limit).
+__device__ __forceinline__ void check_index(long long idx, long long limit, const ProblemDesc &P)
+{
+#ifdef ASETS_BOUNDS_CHECK
+    if (idx < 0 || idx >= limit)
+        atomicOr(&P.ctl->error, DEV_ERR_BOUNDS);
+#else
+    (void)idx;
+    (void)limit;
+    (void)P;
+#endif
+}
+
 // value of the row above (r-1) / below (r+1) each cell: inside the thread,
 // or through one warp shuffle for the first / last cell
 template <int CELLS>
@@ -383,6 +420,16 @@ __global__ void __launch_bounds__(32 * NW, MINB)
         // element offsets fit 32 bits: solves are limited to 2^31 - 1 voxel-labels
         const unsigned int col_off = (unsigned int)(lab_off + (long long)c * P.pitch + r);
         const unsigned int plane_stride = (unsigned int)P.plane_stride;
+        // halo-box reads si .. si+C (the row face below the last cell), in 3D
+        // the column faces of the next column si+LR .. si+LR+C-1; tile-box
+        // reads ti .. ti+C-1; shared-plane reads gi .. gi+C-1
+        check_index(si + C, G::LR * G::LC, P);
+        if constexpr (DIM == 3)
+            check_index(si + G::LR + C - 1, G::LR * G::LC_BC, P);
+        if (is_tile[0])
+            check_index(ti + C - 1, G::tile_floats(), P);
+        if constexpr (DIM == 3)
+            check_index(gi + C - 1, NT * C, P);
         float *__restrict__ d_bs = P.dst_b[par][SL_BS];
         float *__restrict__ d_br = P.dst_b[par][SL_BR];
         float *__restrict__ d_bc = P.dst_b[par][SL_BC];
@@ -559,7 +606,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                     bssn[j] = keep_if<EXACT>(((g2[j] + g2prev[j]) * 0.5f) * bsprev[j],
                                              inplane[j] && spb_in, spb_f);
                 if (sp >= s_begin && sp < s_end)
-                    st_cells_if<C>(d_bs + col_off + (unsigned int)sp * plane_stride, bssn, is_tile);
+                    st_dst<C>(d_bs, col_off + (unsigned int)sp * plane_stride, bssn, is_tile, P);
 #pragma unroll
                 for (int j = 0; j < C; ++j) {
                     bss_old[j] = bss_cur[j];
@@ -605,9 +652,9 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                 if (is_tile[0]) {
                     if (sp >= s_begin && sp < s_end) {
                         const unsigned int o = col_off + (unsigned int)sp * plane_stride;
-                        st_cells_if<C>(d_br + o, brr, is_tile);
+                        st_dst<C>(d_br, o, brr, is_tile, P);
                         if constexpr (DIM == 3)
-                            st_cells_if<C>(d_bc + o, bcc, is_tile);
+                            st_dst<C>(d_bc, o, bcc, is_tile, P);
                     }
                     const int so = s - 2;
                     if (so >= s_begin && so < s_end) {
@@ -640,11 +687,11 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                                 pt_o[j] = pt_n;
                                 u_o[j] = u[j] - e;
                             }
-                            st_cells_if<C>(d_s0 + o, ps_o, is_tile);
-                            st_cells_if<C>(d_s1 + o, pt_o, is_tile);
-                            st_cells_if<C>(d_s2 + o, u_o, is_tile);
+                            st_dst<C>(d_s0, o, ps_o, is_tile, P);
+                            st_dst<C>(d_s1, o, pt_o, is_tile, P);
+                            st_dst<C>(d_s2, o, u_o, is_tile, P);
                         } else {
-                            st_cells_if<C>(d_s0 + o, dv, is_tile);
+                            st_dst<C>(d_s0, o, dv, is_tile, P);
                         }
                     }
                 }

@@ -240,6 +240,9 @@ __global__ void __launch_bounds__(32 * NW, MINB)
             out_b[j] = rows_b && inplane[j];
         const unsigned int col_off = (unsigned int)r;   // + plane * plane_stride
         const unsigned int plane_stride = (unsigned int)P.plane_stride;
+        // halo-box reads rho .. rho+2, tile-box reads rho .. rho+1
+        check_index(rho + 2, G::LR, P);
+        check_index(rho + 1, G::TB, P);
         // B writes the pass's result into the other parity
         float *__restrict__ d_bs = P.dst_b[par][SL_BS];
         float *__restrict__ d_br = P.dst_b[par][SL_BR];
@@ -435,8 +438,8 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                     bssnB[j] = keep_if<EXACT>(((g2B[j] + g2prevB[j]) * 0.5f) * bsprevB[j],
                                               inplane[j] && qpb_in, qpb_f);
                 if (qp - 1 >= s_begin && qp - 1 < s_end)
-                    st_cells_if<C>(d_bs + col_off + (unsigned int)(qp - 1) * plane_stride, bssnB,
-                                   out_b);
+                    st_dst<C>(d_bs, col_off + (unsigned int)(qp - 1) * plane_stride, bssnB, out_b,
+                              P);
 #pragma unroll
                 for (int j = 0; j < C; ++j) {
                     bss_oldB[j] = bss_curB[j];
@@ -459,8 +462,7 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                     dnB[j] = brr1B - brrB[j];
                 }
                 if (qp - 1 >= s_begin && qp - 1 < s_end)
-                    st_cells_if<C>(d_br + col_off + (unsigned int)(qp - 1) * plane_stride, brrB,
-                                   out_b);
+                    st_dst<C>(d_br, col_off + (unsigned int)(qp - 1) * plane_stride, brrB, out_b, P);
                 const int so = qp - 2;
                 if (so >= s_begin && so < s_end) {
                     float ps_o[C], pt_o[C], u_o[C];
@@ -481,9 +483,9 @@ __global__ void __launch_bounds__(32 * NW, MINB)
                         u_o[j] = a_u[1][j] - e;
                     }
                     const unsigned int o = col_off + (unsigned int)so * plane_stride;
-                    st_cells_if<C>(d_s0 + o, ps_o, out_b);
-                    st_cells_if<C>(d_s1 + o, pt_o, out_b);
-                    st_cells_if<C>(d_s2 + o, u_o, out_b);
+                    st_dst<C>(d_s0, o, ps_o, out_b, P);
+                    st_dst<C>(d_s1, o, pt_o, out_b, P);
+                    st_dst<C>(d_s2, o, u_o, out_b, P);
                 }
 #pragma unroll
                 for (int j = 0; j < C; ++j) {

@@ -59,6 +59,7 @@ int build_problem_desc(EncodeTiledFn fn, const StencilVariant &v, const StencilP
         A->lab_add[s] = p.lab_add[s];
     }
     A->pitch = p.pitch;
+    A->dst_elems = p.cells * (p.flow_labels > 0 ? p.flow_labels : 1);
     A->plane_stride = p.plane;
     A->label_stride = p.cells;
     A->nr = p.nr;

@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+from pathlib import Path
 
 import numpy as np
 
@@ -50,7 +51,10 @@ class Options(ctypes.Structure):
 
 _lib = None
 
-LIB_PATH = _build.LIB / "libasetscuda.so"
+# ASETS_LIB_DIR selects another in-tree build (the bounds-check flavour in
+# lib_check/); the default is the release build in lib/.
+LIB_PATH = Path(os.environ["ASETS_LIB_DIR"]) / "libasetscuda.so" if os.environ.get(
+    "ASETS_LIB_DIR") else _build.LIB / "libasetscuda.so"
 
 # name -> (restype, argtypes)
 _SIGS = {
