@@ -57,6 +57,10 @@ CU_SOURCES = (
     "flow3d_exact.cu",
     "flow2d_fast.cu",
     "flow2d_exact.cu",
+    "potts2d_fused_fast.cu",
+    "potts2d_fused_exact.cu",
+    "ishikawa2d_fused_fast.cu",
+    "ishikawa2d_fused_exact.cu",
     "label_kernels.cu",
     "noalloc.cu",
     "conv_tc.cu",

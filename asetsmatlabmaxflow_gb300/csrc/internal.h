@@ -12,7 +12,11 @@ struct asets_context;
 namespace asets {
 
 // ---------------------------------------------------------------- stencil
-// One compiled instance of stencil_iteration_kernel.
+// Label extent of the TMA boxes: one label (the label is the item's), or
+// all labels of the array (stencil2d_labels_kernel).
+enum LabelBoxes : int { LB_ONE = 0, LB_ALL = 1 };
+
+// One compiled instance of an iteration kernel.
 struct StencilVariant {
     int dim, epi, exact;
     int tr, tc, nt, nstage;  // tile rows/cols, threads, TMA ring depth
@@ -24,6 +28,8 @@ struct StencilVariant {
                              // for two iterations per pass)
     int temporal;            // ALM iterations per launch (1, or 2: stencil2d_t2.cuh)
     const void *fn;
+    int label_boxes = LB_ONE;
+    int ct_box_rows = 0;     // rows of the Ct box of the one-pass multi-label kernel (0: none)
 };
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -43,7 +49,8 @@ struct StencilProblem {
     int lab_mul[NUM_SLOTS], lab_add[NUM_SLOTS];
     float *alpha;
     int alpha_labels;
-    const float *cs, *ct;        // binary capacities
+    const float *cs, *ct;        // binary capacities; Ct of the one-pass multi-label kernel
+    int ct_labels;
     float *dst_s[2][3];          // binary: new ps/pt/u; labelled: [.][0] = divergence
 };
 
@@ -75,6 +82,24 @@ inline const StencilVariant *stencil_variants(int dim, int epi, int exact, int *
                                  : (exact ? flow3d_exact_variants(count) : flow3d_fast_variants(count));
     return epi == EPI_BINARY ? (exact ? binary2d_exact_variants(count) : binary2d_fast_variants(count))
                              : (exact ? flow2d_exact_variants(count) : flow2d_fast_variants(count));
+}
+
+// The one-pass multi-label 2D kernels (stencil2d_labels.cuh) for a label
+// count: Potts 1-8 labels, Ishikawa 2-9; `which` numbers the kernels of one
+// label count from 0 (null past the last, or outside the range).
+const StencilVariant *potts2d_fused_fast_variant(int nlab, int which);
+const StencilVariant *potts2d_fused_exact_variant(int nlab, int which);
+const StencilVariant *ishikawa2d_fused_fast_variant(int nlab, int which);
+const StencilVariant *ishikawa2d_fused_exact_variant(int nlab, int which);
+// model: 1 Potts, 2 Ishikawa
+inline const StencilVariant *fused2d_variant(int model, int nlab, int exact, int which = 0)
+{
+    if (model == 1)
+        return exact ? potts2d_fused_exact_variant(nlab, which) : potts2d_fused_fast_variant(nlab, which);
+    if (model == 2)
+        return exact ? ishikawa2d_fused_exact_variant(nlab, which)
+                     : ishikawa2d_fused_fast_variant(nlab, which);
+    return nullptr;
 }
 
 // ---------------------------------------------------------------- labels

@@ -1,0 +1,50 @@
+// Compiled instances of the one-pass multi-label 2D kernels (stencil2d_labels.cuh)
+// for the Ishikawa model, 2 to 9 labels: the label update in the flow
+// warps, by one label warp, by two; fast projection, built with FMA contraction and flush to zero (held
+// to the parity tolerance, not bit-exactness).
+#include "variants.cuh"
+
+namespace asets {
+
+static const StencilVariant kSync[] = {
+    make_variant_labels<2, 2, false, 0>(),
+    make_variant_labels<2, 3, false, 0>(),
+    make_variant_labels<2, 4, false, 0>(),
+    make_variant_labels<2, 5, false, 0>(),
+    make_variant_labels<2, 6, false, 0>(),
+    make_variant_labels<2, 7, false, 0>(),
+    make_variant_labels<2, 8, false, 0>(),
+    make_variant_labels<2, 9, false, 0>(),
+};
+static const StencilVariant kOne[] = {
+    make_variant_labels<2, 2, false, 1>(),
+    make_variant_labels<2, 3, false, 1>(),
+    make_variant_labels<2, 4, false, 1>(),
+    make_variant_labels<2, 5, false, 1>(),
+    make_variant_labels<2, 6, false, 1>(),
+    make_variant_labels<2, 7, false, 1>(),
+    make_variant_labels<2, 8, false, 1>(),
+    make_variant_labels<2, 9, false, 1>(),
+};
+static const StencilVariant kTwo[] = {
+    make_variant_labels<2, 2, false, 2>(),
+    make_variant_labels<2, 3, false, 2>(),
+    make_variant_labels<2, 4, false, 2>(),
+    make_variant_labels<2, 5, false, 2>(),
+    make_variant_labels<2, 6, false, 2>(),
+    make_variant_labels<2, 7, false, 2>(),
+    make_variant_labels<2, 8, false, 2>(),
+    make_variant_labels<2, 9, false, 2>(),
+};
+
+// the instance for nlab labels (which: 0 in-step update, 1 one label warp,
+// 2 two), or null
+const StencilVariant *ishikawa2d_fused_fast_variant(int nlab, int which)
+{
+    const int i = nlab - 2;
+    if (i < 0 || i >= (int)(sizeof(kOne) / sizeof(kOne[0])) || which < 0 || which > 2)
+        return nullptr;
+    return which == 0 ? &kSync[i] : which == 1 ? &kOne[i] : &kTwo[i];
+}
+
+}  // namespace asets

@@ -46,6 +46,7 @@ enum Slot : int {
 enum Epilogue : int {
     EPI_BINARY = 0,  // binary model: ps/pt/u update + erriter
     EPI_DIV = 1,     // multi-label models: write the new flow and its divergence
+    EPI_FUSED = 2,   // multi-label 2D, one pass: flows of all labels and the label update
 };
 
 
@@ -59,9 +60,11 @@ enum TileSlot : int { TS_S1 = 0, TS_S2 = 1, TS_CS = 2, TS_CT = 3, NUM_TILE_SLOTS
 // alignment, which the CUtensorMap members give the struct).
 struct ProblemDesc {
     CUtensorMap halo[2][NUM_SLOTS];        // [source parity][slot]
-    CUtensorMap tile[2][NUM_TILE_SLOTS];   // binary only
+    CUtensorMap tile[2][NUM_TILE_SLOTS];   // binary; EPI_FUSED: [.][TS_CT] = Ct, all labels,
+                                           // halo rows (the same map for both parities)
     float *dst_b[2][3];                    // [source parity][SL_BC, SL_BR, SL_BS]
-    float *dst_s[2][3];                    // binary: ps, pt, u; EPI_DIV: [.][0] = divergence
+    float *dst_s[2][3];                    // binary: ps, pt, u; EPI_DIV: [.][0] = divergence;
+                                           // EPI_FUSED: Potts ps, pt, u; Ishikawa pt, -, u
     IterControl *ctl;
     double *item_partials;                 // binary: one erriter partial per item
     float *cvg;
@@ -77,6 +80,7 @@ struct ProblemDesc {
     int lab_mul[NUM_SLOTS];
     int lab_add[NUM_SLOTS];
     float cc, inv_cc, steps;
+    float inv_cc_l;                        // EPI_FUSED Potts: 1/(cc*L), cc*L rounded to float
 };
 
 // A launch over one or more problems of the same kind (dimension, model).

@@ -374,18 +374,57 @@ static long long round_pitch(int nr)
     return ((long long)nr + 3) / 4 * 4;
 }
 
-static const StencilVariant *pick_variant(const asets_solver *s, int exact, int tile_config)
+// Whether the solver can run the one-pass multi-label 2D kernel: it needs
+// the second parity of pt/u/ps, allocated for the label counts it covers.
+static bool has_fused(const asets_solver *s)
 {
+    return s->dim == 2 && s->model != ASETS_BINARY && s->pt[1] != s->pt[0];
+}
+
+// The kernel variants open to a solve, in tile_config order (entry k-1 for
+// tile_config k): the one-pass multi-label 2D kernel first where it applies
+// (not in a batch, whose group shares one variant across label counts), then
+// the kind's table.
+static std::vector<const StencilVariant *> solver_candidates(const asets_solver *s, int exact,
+                                                             bool single)
+{
+    std::vector<const StencilVariant *> c;
+    if (single && has_fused(s))
+        for (int w = 0; const StencilVariant *f = fused2d_variant((int)s->model, s->nlab, exact, w); ++w)
+            c.push_back(f);
     int n = 0;
     const StencilVariant *tab = stencil_variants(s->dim, s->model == ASETS_BINARY ? EPI_BINARY : EPI_DIV,
                                                  exact, &n);
-    std::vector<const StencilVariant *> match;
     for (int i = 0; i < n; ++i)
-        match.push_back(&tab[i]);
+        c.push_back(&tab[i]);
+    return c;
+}
+
+static const StencilVariant *pick_variant(const asets_solver *s, int exact, int tile_config,
+                                          bool single)
+{
+    std::vector<const StencilVariant *> match = solver_candidates(s, exact, single);
     if (match.empty())
         return nullptr;
     if (tile_config > 0 && tile_config <= (int)match.size())
         return match[tile_config - 1];
+    // the one-pass multi-label kernels lead the list (in-step update, one
+    // label warp, two); by default they run where they measured faster than
+    // the two-pass form on a GB300: two million pixels and more (two label
+    // warps for up to three flow labels, one above), and half a million with
+    // six flow labels or more (in-step update)
+    int n_fused = 0;
+    while (n_fused < (int)match.size() && match[n_fused]->epi == EPI_FUSED)
+        ++n_fused;
+    if (n_fused == 3) {
+        const long long px = (long long)s->nr * s->ns;
+        const int fl = s->flow_labels;
+        if (px >= 2000000)
+            return match[fl <= 3 ? 2 : 1];
+        if (px >= 500000 && fl >= 6)
+            return match[0];
+    }
+    match.erase(match.begin(), match.begin() + n_fused);
     if (s->dim == 2 && s->nr <= 112) {
         // short columns: the narrow 2D variant wastes fewer rows
         for (auto *v : match)
@@ -395,8 +434,10 @@ static const StencilVariant *pick_variant(const asets_solver *s, int exact, int 
     return match[0];
 }
 
-// The solver's buffers as the iteration kernel sees them (both parities).
-static StencilProblem stencil_problem_of(const asets_solver *s)
+// The solver's buffers as the iteration kernel sees them (both parities);
+// `fused`: for the one-pass multi-label kernel, whose pt/u/ps ping-pong like
+// the flows.
+static StencilProblem stencil_problem_of(const asets_solver *s, bool fused)
 {
     const bool binary = (s->model == ASETS_BINARY);
     StencilProblem p;
@@ -418,6 +459,15 @@ static StencilProblem stencil_problem_of(const asets_solver *s)
             p.dst_s[par][0] = s->ps[par ^ 1];
             p.dst_s[par][1] = s->pt[par ^ 1];
             p.dst_s[par][2] = s->u[par ^ 1];
+        } else if (fused) {
+            const int q = par ^ 1;
+            const bool potts = (s->model == ASETS_POTTS);
+            p.src[par][0] = potts ? s->ps[par] : s->pt[par];
+            p.src[par][1] = s->pt[par];
+            p.src[par][2] = s->u[par];
+            p.dst_s[par][0] = potts ? s->ps[q] : s->pt[q];
+            p.dst_s[par][1] = potts ? s->pt[q] : nullptr;
+            p.dst_s[par][2] = s->u[q];
         } else if (s->model == ASETS_POTTS) {
             p.src[par][0] = s->ps[0];
             p.src[par][1] = s->pt[0];
@@ -451,18 +501,19 @@ static StencilProblem stencil_problem_of(const asets_solver *s)
     p.alpha_labels = s->alpha_labels;
     p.cs = s->cs;
     p.ct = s->ct;
+    p.ct_labels = s->ct_labels;
     return p;
 }
 
 // Build the kernel arguments (TMA maps for both parities, destinations).
-static asets_status setup_kernel(asets_solver *s, int exact, int tile_config)
+static asets_status setup_kernel(asets_solver *s, int exact, int tile_config, bool single)
 {
-    const StencilVariant *v = pick_variant(s, exact, tile_config);
+    const StencilVariant *v = pick_variant(s, exact, tile_config, single);
     if (!v)
         return fail(ASETS_ERR_UNSUPPORTED, "no kernel variant for this configuration");
     if (s->variant == v)
         return ASETS_OK;
-    const StencilProblem p = stencil_problem_of(s);
+    const StencilProblem p = stencil_problem_of(s, v->epi == EPI_FUSED);
     ProblemDesc &A = s->desc;
     int r = build_problem_desc(s->ctx->encode, *v, p, &A);
     if (r)
@@ -610,9 +661,17 @@ extern "C" ASETS_API asets_status asets_solver_create(asets_context *ctx, asets_
         ALLOC(s->pt[0], n * s->pt_labels);
         ALLOC(s->u[0], n * s->u_labels);
         ALLOC(s->dv, n * s->flow_labels);
-        s->ps[1] = s->ps[0];
-        s->pt[1] = s->pt[0];
-        s->u[1] = s->u[0];
+        if (dim == 2 && fused2d_variant((int)model, nLab, 0)) {
+            // the one-pass kernel writes the new state to a second parity
+            if (model == ASETS_POTTS)
+                ALLOC(s->ps[1], n);
+            ALLOC(s->pt[1], n * s->pt_labels);
+            ALLOC(s->u[1], n * s->u_labels);
+        } else {
+            s->ps[1] = s->ps[0];
+            s->pt[1] = s->pt[0];
+            s->u[1] = s->u[0];
+        }
     }
     {
         void *p = nullptr;
@@ -880,7 +939,7 @@ static LabelArgs label_args(asets_solver *s)
 // Reset the solver's iteration state for a run of maxIt iterations and queue
 // its initial state (zero flows; u/ps/pt from init or the warm start).
 static asets_status prepare_run(asets_solver *s, int flags, int tile_config, int maxIt,
-                                float errBound, float cc, float steps)
+                                float errBound, float cc, float steps, bool single = true)
 {
     cudaStream_t st = s->ctx->stream;
     if (maxIt >= 1 && !s->alpha_ok && !(flags & ASETS_FLAG_NO_ALPHA_CHECK))
@@ -888,7 +947,7 @@ static asets_status prepare_run(asets_solver *s, int flags, int tile_config, int
                                                ? "alpha(x,l) must be positive. Exiting..."
                                                : "alpha(x) must be positive. Exiting...");
     const int exact = (flags & ASETS_FLAG_EXACT) ? 1 : 0;
-    asets_status ss = setup_kernel(s, exact, tile_config);
+    asets_status ss = setup_kernel(s, exact, tile_config, single);
     if (ss != ASETS_OK)
         return ss;
     if (maxIt + 1 > s->cvg_cap) {
@@ -904,6 +963,8 @@ static asets_status prepare_run(asets_solver *s, int flags, int tile_config, int
     A.cvg = s->cvg;
     A.cc = cc;
     A.inv_cc = 1.0f / cc;  // `1/cc` of the reference, a float division
+    // `1/(cc*nLab)` of updatePSU: cc*nLab rounded to float, then divided
+    A.inv_cc_l = 1.0f / (cc * (float)s->nlab);
     A.steps = steps;
     CU_TRY(cudaMemcpyAsync(s->d_desc, &A, sizeof A, cudaMemcpyHostToDevice, st));
     CU_TRY(cudaMemsetAsync(s->d_queue, 0, 4 * sizeof(unsigned int), st));
@@ -950,7 +1011,7 @@ static asets_status prepare_run(asets_solver *s, int flags, int tile_config, int
 static cudaError_t launch_iteration(asets_solver *s)
 {
     cudaError_t e = launch_stencil(s);
-    if (e != cudaSuccess || s->model == ASETS_BINARY)
+    if (e != cudaSuccess || s->model == ASETS_BINARY || s->variant->epi == EPI_FUSED)
         return e;
     LabelArgs la = label_args(s);
     const int grid = label_kernel_grid(s->cells, s->ctx->num_sms);
@@ -1032,7 +1093,9 @@ static asets_status finish_run(asets_solver *s, const IterControl &out, int *itN
     const int parity = (s->variant && s->variant->temporal == 2)
                            ? (((out.last_iter >> 1) & 1) ^ 1)
                            : ((out.last_iter + 1) & 1);
-    s->final_parity = (s->model == ASETS_BINARY) ? parity : 0;
+    // the two-pass multi-label form keeps pt/u/ps in place (parity 0)
+    const bool pingpong = (s->model == ASETS_BINARY) || (s->variant && s->variant->epi == EPI_FUSED);
+    s->final_parity = pingpong ? parity : 0;
     s->flow_parity = parity;
     if (itNum)
         *itNum = (maxIt == 0) ? 0 : out.it_num;
@@ -1062,7 +1125,7 @@ static asets_status replay_first_of_pass(asets_solver *s, const IterControl &out
             v = &tab[i];
     if (!v)
         return fail(ASETS_ERR_UNSUPPORTED, "no one-iteration kernel variant to re-run with");
-    const StencilProblem sp = stencil_problem_of(s);
+    const StencilProblem sp = stencil_problem_of(s, false);
     ProblemDesc D;
     int r = build_problem_desc(s->ctx->encode, *v, sp, &D);
     if (r)
@@ -1156,14 +1219,13 @@ static asets_status solver_autotune(asets_solver *s, int flags, float cc, float 
             }
     }
     cudaStream_t st = s->ctx->stream;
-    int n = 0;
-    const StencilVariant *tab =
-        stencil_variants(s->dim, s->model == ASETS_BINARY ? EPI_BINARY : EPI_DIV, exact, &n);
+    const std::vector<const StencilVariant *> cands = solver_candidates(s, exact, true);
+    const int n = (int)cands.size();
     int best = 1;
     float best_ms = 1e30f;
     for (int cand = 1; cand <= n; ++cand) {
         // one chunk of launches: kGraphIters x (iterations per launch) iterations
-        const int per_launch = tab[cand - 1].temporal;
+        const int per_launch = cands[cand - 1]->temporal;
         asets_status ss = prepare_run(s, flags, cand, kGraphIters * per_launch, 0.0f, cc, steps);
         if (ss != ASETS_OK)
             return ss;
@@ -1246,7 +1308,8 @@ extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_
     float ms = 0.f;
     CU_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
     s->last_ms = ms;
-    s->last_launches = chunks * kGraphIters * (s->model == ASETS_BINARY ? 1 : 2) + replays;
+    const bool one_kernel = (s->model == ASETS_BINARY) || s->variant->epi == EPI_FUSED;
+    s->last_launches = chunks * kGraphIters * (one_kernel ? 1 : 2) + replays;
     s->last_iters = (maxIt == 0) ? 0 : out.last_iter + 1;
     return finish_run(s, out, itNum);
 }
@@ -1772,7 +1835,8 @@ static asets_status batch_prepare(asets_batch *b, int flags, const int tile_conf
         if (!s->inputs_set)
             return fail(ASETS_ERR_INVALID_ARG, "batch member %zu has no inputs", i);
         const int gi = batch_group(s);
-        asets_status st = prepare_run(s, flags, tile_config[gi], maxIt, errBound, cc, steps);
+        asets_status st =
+            prepare_run(s, flags, tile_config[gi], maxIt, errBound, cc, steps, false);
         if (st != ASETS_OK)
             return st;
         b->groups[gi].idx.push_back((int)i);

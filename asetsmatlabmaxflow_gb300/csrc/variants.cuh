@@ -4,6 +4,7 @@
 #include "internal.h"
 #include "stencil2_kernel.cuh"
 #include "stencil2d_t2.cuh"
+#include "stencil2d_labels.cuh"
 
 namespace asets {
 
@@ -50,6 +51,43 @@ StencilVariant make_variant_t2()
     v.tile_box_rows = G::TB;
     v.temporal = 2;
     v.fn = reinterpret_cast<const void *>(&stencil2d_t2_kernel<NW, NSTAGE, EXACT, MINB, UNROLL>);
+    return v;
+}
+
+// The one-pass multi-label 2D kernels (stencil2d_labels.cuh) for MODEL
+// (1 Potts, 2 Ishikawa) with L labels: one warp per flow label, and LW label
+// warps (1 or 2; 0: the label update in the flow warps), about 768 threads
+// per SM.
+template <int MODEL, int L, bool EXACT, int LW, int NSTAGE = 4>
+StencilVariant make_variant_labels()
+{
+    using G = Lab2Geom<MODEL, L>;
+    constexpr int NW = G::FL + LW;
+    constexpr int MINB = (24 / NW < 1) ? 1 : (24 / NW > 16 ? 16 : 24 / NW);
+    StencilVariant v;
+    v.dim = 2;
+    v.epi = EPI_FUSED;
+    v.exact = EXACT ? 1 : 0;
+    v.tr = G::TR;
+    v.tc = 1;
+    v.nt = 32 * NW;
+    v.nstage = NSTAGE;
+    if constexpr (LW == 0) {
+        v.smem_bytes = Lab2SyncGeom<MODEL, L>::template smem_bytes<NSTAGE>();
+        v.fn = reinterpret_cast<const void *>(
+            &stencil2d_labels_sync_kernel<MODEL, L, NSTAGE, EXACT, MINB>);
+    } else {
+        v.smem_bytes = Lab2WarpsGeom<MODEL, L, LW>::template smem_bytes<NSTAGE>();
+        v.fn = reinterpret_cast<const void *>(
+            &stencil2d_labels_kernel<MODEL, L, LW, NSTAGE, EXACT, MINB>);
+    }
+    v.box_rows = G::LR;
+    v.box_cols = 1;
+    v.box_cols_bc = 1;
+    v.tile_box_rows = G::TR;
+    v.temporal = 1;
+    v.label_boxes = LB_ALL;
+    v.ct_box_rows = G::LR;
     return v;
 }
 
