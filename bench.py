@@ -73,10 +73,11 @@ def parse():
     ap.add_argument("--shape", default="256,256,256", help="volume for --profile-iters")
     ap.add_argument("--tile-config", type=int, default=0, help="kernel variant for --profile-iters")
     ap.add_argument("--profile-model", default="binary",
-                    choices=["binary", "potts", "potts192", "ishikawa1024", "hmf", "dag", "costs",
-                             "matlab3d", "starshape"],
+                    choices=["binary", "potts", "potts192", "ishikawa1024", "potts2048", "hmf",
+                             "dag", "costs", "matlab3d", "starshape"],
                     help="model for --profile-iters (potts: the warm-start workload, seed 1000000; "
                          "potts192: Potts 3D 192^3 L=4; ishikawa1024: Ishikawa 2D 1024^2 L=8; "
+                         "potts2048: Potts 2D 2048^2 L=4 (the Ishikawa field's Ct, alpha 0.2); "
                          "hmf / dag: the 1024^2 six-node tree / graph of the `next` entries; "
                          "costs: N pairs of L1-cost and contrast-alpha calls on 256^3; "
                          "matlab3d: Matlab-semantics binary 3D 256^3; starshape: 512^2 L=4)")
@@ -171,11 +172,15 @@ def profile_run(args):
         torch.cuda.synchronize()
         print(json.dumps({"profile_run": "costs 256^3", "calls": args.profile_iters}))
         return
-    if args.profile_model in ("potts192", "ishikawa1024"):
+    if args.profile_model in ("potts192", "ishikawa1024", "potts2048"):
         # the multi-region configurations: cc 0.3, steps 0.11 (3D) / 0.16 (2D)
         if args.profile_model == "potts192":
             ct, a = synth.potts3d(seed=0)
             model, dims, L, steps = "potts", ct.shape[:3], ct.shape[3], 0.11
+        elif args.profile_model == "potts2048":
+            ct, _ = synth.ishikawa2d(seed=0, shape=(2048, 2048), L=4)
+            a = np.full(ct.shape, 0.2, np.float32, order="F")
+            model, dims, L, steps = "potts", ct.shape[:2], ct.shape[2], 0.16
         else:
             ct, a = synth.ishikawa2d(seed=0)
             model, dims, L, steps = "ishikawa", ct.shape[:2], ct.shape[2], 0.16
