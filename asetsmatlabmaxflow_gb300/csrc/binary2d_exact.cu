@@ -13,6 +13,9 @@ static const StencilVariant kVariants[] = {
     make_variant<2, 2, 4, EPI_BINARY, true>(),
     // two iterations per pass, 224-row tiles
     make_variant_t2<4, 5, true, 3, 4>(),
+    // square tiles for small images: 32 x 32 (256 threads), 16 x 16 (128)
+    make_variant_tile<32, 32, 256, true>(),
+    make_variant_tile<16, 16, 128, true, 4>(),
 };
 
 const StencilVariant *binary2d_exact_variants(int *count)

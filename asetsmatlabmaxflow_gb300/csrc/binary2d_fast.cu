@@ -17,6 +17,9 @@ static const StencilVariant kVariants[] = {
     make_variant<2, 8, 4, EPI_BINARY, false, 4, 4>(),       // 224-row tiles
     make_variant<2, 2, 4, EPI_BINARY, false>(),             // 56-row tiles (short columns)
     make_variant<2, 4, 4, EPI_BINARY, false, 4, 4, 2>(),
+    // square tiles for small images: 32 x 32 (256 threads), 16 x 16 (128)
+    make_variant_tile<32, 32, 256, false>(),
+    make_variant_tile<16, 16, 128, false, 4>(),
 };
 
 const StencilVariant *binary2d_fast_variants(int *count)

@@ -30,6 +30,7 @@ struct StencilVariant {
     const void *fn;
     int label_boxes = LB_ONE;
     int ct_box_rows = 0;     // rows of the Ct box of the one-pass multi-label kernel (0: none)
+    int s_tile = 0;          // stream columns of a square-tile kernel's tile (0: a sweep)
 };
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,

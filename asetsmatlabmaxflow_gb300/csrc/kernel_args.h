@@ -65,6 +65,7 @@ struct ProblemDesc {
     float *dst_b[2][3];                    // [source parity][SL_BC, SL_BR, SL_BS]
     float *dst_s[2][3];                    // binary: ps, pt, u; EPI_DIV: [.][0] = divergence;
                                            // EPI_FUSED: Potts ps, pt, u; Ishikawa pt, -, u
+    const float *alpha, *cs, *ct;          // inputs, for kernels that read them without TMA
     IterControl *ctl;
     double *item_partials;                 // binary: one erriter partial per item
     float *cvg;

@@ -1709,7 +1709,8 @@ static std::vector<int> choose_batch_chunks(const std::vector<asets_solver *> &l
         for (size_t j = 0; j < live.size(); ++j) {
             const asets_solver *s = live[j];
             const int max_k = std::max(1, s->ns / 8);
-            const int k = std::min(max_k, std::max(1, (s->ns + len / 2) / len));
+            const int k = v.s_tile > 0 ? (s->ns + v.s_tile - 1) / v.s_tile  // square tiles
+                                       : std::min(max_k, std::max(1, (s->ns + len / 2) / len));
             cur[j] = k;
             const long long it = problem_items(item_geometry(s), v, k);
             items += it;

@@ -67,6 +67,9 @@ int build_problem_desc(EncodeTiledFn fn, const StencilVariant &v, const StencilP
         A->lab_mul[s] = p.lab_mul[s];
         A->lab_add[s] = p.lab_add[s];
     }
+    A->alpha = p.alpha;
+    A->cs = p.cs;
+    A->ct = p.ct;
     A->pitch = p.pitch;
     // the largest destination: the flows, or the new pt of a one-pass
     // multi-label kernel (Ishikawa: one label more than the flows)
@@ -102,6 +105,8 @@ int choose_zchunks(const StencilProblem &p, const StencilVariant &v, long long s
 {
     const long long tiles = (long long)((p.nr + v.tr - 1) / v.tr) *
                             ((v.dim == 3) ? (p.nc + v.tc - 1) / v.tc : 1) * item_labels(p, v);
+    if (v.s_tile > 0)
+        return (p.ns + v.s_tile - 1) / v.s_tile;  // square tiles: one item per tile
     if (slots < 1 || tiles < 1)
         return 1;
     // Items (tile, chunk) run in waves of `slots` blocks; each chunk pays a

@@ -5,6 +5,7 @@
 #include "stencil2_kernel.cuh"
 #include "stencil2d_t2.cuh"
 #include "stencil2d_labels.cuh"
+#include "stencil2d_tile.cuh"
 
 namespace asets {
 
@@ -51,6 +52,30 @@ StencilVariant make_variant_t2()
     v.tile_box_rows = G::TB;
     v.temporal = 2;
     v.fn = reinterpret_cast<const void *>(&stencil2d_t2_kernel<NW, NSTAGE, EXACT, MINB, UNROLL>);
+    return v;
+}
+
+// The binary 2D square-tile kernel (stencil2d_tile.cuh): R x S tiles, NT threads.
+template <int R, int S, int NT, bool EXACT, int MINB = 2>
+StencilVariant make_variant_tile()
+{
+    using G = Tile2Geom<R, S>;
+    StencilVariant v;
+    v.dim = 2;
+    v.epi = EPI_BINARY;
+    v.exact = EXACT ? 1 : 0;
+    v.tr = R;
+    v.tc = 1;
+    v.nt = NT;
+    v.nstage = 0;
+    v.smem_bytes = G::smem_bytes();
+    v.box_rows = R + 8;       // unused maps, encoded like the sweep's
+    v.box_cols = 1;
+    v.box_cols_bc = 1;
+    v.tile_box_rows = R;
+    v.temporal = 1;
+    v.fn = reinterpret_cast<const void *>(&stencil2d_tile_kernel<R, S, NT, EXACT, MINB>);
+    v.s_tile = S;
     return v;
 }
 
