@@ -16,6 +16,9 @@ static const StencilVariant kVariants[] = {
     // square tiles for small images: 32 x 32 (256 threads), 16 x 16 (128)
     make_variant_tile<32, 32, 256, true>(),
     make_variant_tile<16, 16, 128, true, 4>(),
+    // the same, every iteration in one cooperative launch (single solves)
+    make_variant_tile<32, 32, 256, true, 2, true>(),
+    make_variant_tile<16, 16, 128, true, 4, true>(),
 };
 
 const StencilVariant *binary2d_exact_variants(int *count)

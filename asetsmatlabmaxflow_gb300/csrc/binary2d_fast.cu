@@ -20,6 +20,9 @@ static const StencilVariant kVariants[] = {
     // square tiles for small images: 32 x 32 (256 threads), 16 x 16 (128)
     make_variant_tile<32, 32, 256, false>(),
     make_variant_tile<16, 16, 128, false, 4>(),
+    // the same, every iteration in one cooperative launch (single solves)
+    make_variant_tile<32, 32, 256, false, 2, true>(),
+    make_variant_tile<16, 16, 128, false, 4, true>(),
 };
 
 const StencilVariant *binary2d_fast_variants(int *count)

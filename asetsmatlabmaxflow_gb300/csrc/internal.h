@@ -31,6 +31,7 @@ struct StencilVariant {
     int label_boxes = LB_ONE;
     int ct_box_rows = 0;     // rows of the Ct box of the one-pass multi-label kernel (0: none)
     int s_tile = 0;          // stream columns of a square-tile kernel's tile (0: a sweep)
+    int persistent = 0;      // 1: every iteration in one cooperative launch, one block per tile
 };
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,

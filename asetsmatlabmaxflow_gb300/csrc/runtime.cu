@@ -395,9 +395,30 @@ static std::vector<const StencilVariant *> solver_candidates(const asets_solver 
     int n = 0;
     const StencilVariant *tab = stencil_variants(s->dim, s->model == ASETS_BINARY ? EPI_BINARY : EPI_DIV,
                                                  exact, &n);
+    // a batch launch serves many problems: no whole-solve cooperative kernels
     for (int i = 0; i < n; ++i)
-        c.push_back(&tab[i]);
+        if (single || !tab[i].persistent)
+            c.push_back(&tab[i]);
     return c;
+}
+
+// Whether a whole-solve cooperative variant can hold every tile of the
+// solver's problem resident at once (one block per tile).
+static bool persistent_fits(const asets_solver *s, const StencilVariant *v)
+{
+    const long long tiles = (long long)((s->nr + v->tr - 1) / v->tr) * ((s->ns + v->s_tile - 1) / v->s_tile);
+    if (cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, v->smem_bytes) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, v->nt, v->smem_bytes) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return tiles <= (long long)per_sm * s->ctx->num_sms;
 }
 
 static const StencilVariant *pick_variant(const asets_solver *s, int exact, int tile_config,
@@ -425,6 +446,24 @@ static const StencilVariant *pick_variant(const asets_solver *s, int exact, int 
             return match[0];
     }
     match.erase(match.begin(), match.begin() + n_fused);
+    // small binary 2D images: the whole solve in one cooperative launch when
+    // every tile can be resident (16 x 16 tiles up to 2^17 pixels, else
+    // 32 x 32), measured faster than the sweeps there
+    if (single && s->dim == 2 && s->model == ASETS_BINARY) {
+        const long long px = (long long)s->nr * s->ns;
+        for (int want : {16, 32}) {
+            if (want == 16 && px > (1LL << 17))
+                continue;
+            for (auto *v : match)
+                if (v->persistent && v->s_tile == want && persistent_fits(s, v))
+                    return v;
+        }
+    }
+    for (size_t i = 0; i < match.size();)
+        if (match[i]->persistent || match[i]->s_tile > 0)
+            match.erase(match.begin() + i);  // square tiles: by tile_config or the autotuner
+        else
+            ++i;
     if (s->dim == 2 && s->nr <= 112) {
         // short columns: the narrow 2D variant wastes fewer rows
         for (auto *v : match)
@@ -513,6 +552,8 @@ static asets_status setup_kernel(asets_solver *s, int exact, int tile_config, bo
         return fail(ASETS_ERR_UNSUPPORTED, "no kernel variant for this configuration");
     if (s->variant == v)
         return ASETS_OK;
+    if (v->persistent && !persistent_fits(s, v))
+        return fail(ASETS_ERR_UNSUPPORTED, "too many tiles for one cooperative launch");
     const StencilProblem p = stencil_problem_of(s, v->epi == EPI_FUSED);
     ProblemDesc &A = s->desc;
     int r = build_problem_desc(s->ctx->encode, *v, p, &A);
@@ -559,6 +600,8 @@ static asets_status setup_kernel(asets_solver *s, int exact, int tile_config, bo
     s->bargs.total_items = items;
     s->bargs.queue = s->d_queue;
     s->bargs.done_count = s->d_queue + 2;
+    if (v->persistent)
+        s->grid = items;  // one block per tile, all resident
     // erriter partials of the label kernels (labelled models)
     const int need = std::max(s->ctx->num_sms * 8, 1024);
     if (need > s->partials_cap) {
@@ -1023,6 +1066,17 @@ static cudaError_t launch_iteration(asets_solver *s)
 // graph and replayed; the kernels skip work once their problem is done.
 static constexpr int kGraphIters = 16;
 
+// The whole solve as one cooperative launch (square-tile kernels): every
+// block resident, a grid barrier between iterations (the kernel stops at
+// errBound or maxIt by itself).
+static cudaError_t launch_persistent(asets_solver *s)
+{
+    const StencilVariant *v = s->variant;
+    void *params[] = {&s->bargs};
+    return cudaLaunchCooperativeKernel(v->fn, dim3(s->grid), dim3(v->nt), params, v->smem_bytes,
+                                       s->ctx->stream);
+}
+
 
 template <class LaunchOne>
 static asets_status capture_chunk(ChunkGraph &g, cudaStream_t st, LaunchOne launch_one)
@@ -1226,15 +1280,24 @@ static asets_status solver_autotune(asets_solver *s, int flags, float cc, float 
     for (int cand = 1; cand <= n; ++cand) {
         // one chunk of launches: kGraphIters x (iterations per launch) iterations
         const int per_launch = cands[cand - 1]->temporal;
+        if (cands[cand - 1]->persistent && !persistent_fits(s, cands[cand - 1]))
+            continue;
         asets_status ss = prepare_run(s, flags, cand, kGraphIters * per_launch, 0.0f, cc, steps);
         if (ss != ASETS_OK)
             return ss;
-        ss = capture_chunk(s->graph, st, [&] { return launch_iteration(s); });
-        if (ss != ASETS_OK)
-            return ss;
-        CU_TRY(cudaEventRecord(s->ev0, st));
-        CU_TRY(cudaGraphLaunch(s->graph.exec, st));
-        CU_TRY(cudaEventRecord(s->ev1, st));
+        if (s->variant->persistent) {
+            // kGraphIters iterations in one cooperative launch
+            CU_TRY(cudaEventRecord(s->ev0, st));
+            CU_TRY(launch_persistent(s));
+            CU_TRY(cudaEventRecord(s->ev1, st));
+        } else {
+            ss = capture_chunk(s->graph, st, [&] { return launch_iteration(s); });
+            if (ss != ASETS_OK)
+                return ss;
+            CU_TRY(cudaEventRecord(s->ev0, st));
+            CU_TRY(cudaGraphLaunch(s->graph.exec, st));
+            CU_TRY(cudaEventRecord(s->ev1, st));
+        }
         CU_TRY(cudaEventSynchronize(s->ev1));
         float ms = 0.f;
         CU_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
@@ -1249,6 +1312,27 @@ static asets_status solver_autotune(asets_solver *s, int flags, float cc, float 
     g_solver_tune.emplace_back(key, best);
     *tile_config = best;
     return ASETS_OK;
+}
+
+// Run a prepared solve whose variant is a whole-solve cooperative kernel.
+static asets_status persistent_run(asets_solver *s, int maxIt, int *itNum)
+{
+    cudaStream_t st = s->ctx->stream;
+    CU_TRY(cudaEventRecord(s->ev0, st));
+    if (maxIt > 0) {
+        NvtxRange r("asets cooperative solve");
+        CU_TRY(launch_persistent(s));
+    }
+    CU_TRY(cudaEventRecord(s->ev1, st));
+    IterControl out;
+    CU_TRY(cudaMemcpyAsync(&out, s->ctl, sizeof out, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    CU_TRY(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    s->last_ms = ms;
+    s->last_launches = maxIt > 0 ? 1 : 0;
+    s->last_iters = (maxIt == 0) ? 0 : out.last_iter + 1;
+    return finish_run(s, out, itNum);
 }
 
 extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_options *opt,
@@ -1275,6 +1359,8 @@ extern "C" ASETS_API asets_status asets_solver_run(asets_solver *s, const asets_
     asets_status ss = prepare_run(s, flags, tile_config, maxIt, errBound, cc, steps);
     if (ss != ASETS_OK)
         return ss;
+    if (s->variant->persistent)
+        return persistent_run(s, maxIt, itNum);
     // the labelled models pass cc by value to the label kernel: recapture
     // when it changes
     if (!s->graph.exec || s->graph.key_fn != s->variant->fn ||
@@ -2015,6 +2101,8 @@ static asets_status batch_autotune(asets_batch *b, int flags, float cc, float st
         int best = 1;
         float best_ms = 1e30f;
         for (int cand = 1; cand <= n; ++cand) {
+            if (tab[cand - 1].persistent)
+                continue;  // single solves only
             int tc[4] = {tile_config[0], tile_config[1], tile_config[2], tile_config[3]};
             tc[gi] = cand;
             // 2 x kGraphIters iterations of every member: two chunks of one

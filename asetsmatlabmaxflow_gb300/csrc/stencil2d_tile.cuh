@@ -11,11 +11,13 @@
 // new flows b'' and, on the tile, the divergence and the ps/pt/u update with
 // erriter -- the same float expressions, in the same order and with the
 // same border masks, as the sweep kernel (EXACT results are bit-identical).
-// Old state is read with plain coalesced loads (a small problem sits in L2),
-// all of a thread's loads in flight at once; out-of-volume cells read as 0,
-// the zero-flux border.  Items are the tiles,
-// handed out by the same queue, closed by the same per-item erriter partials
-// and ticket.
+// Old state is read with coalesced loads through L2 (a small problem sits in
+// L2), all of a thread's loads in flight at once; out-of-volume cells read
+// as 0, the zero-flux border.  Two kernels: one launch per iteration, items
+// handed out by the same queue and closed by the same per-item erriter
+// partials and ticket as the sweeps; or every iteration in one cooperative
+// launch with a grid barrier between iterations, which removes the launch
+// and hand-off latency that dominates an iteration of a small image.
 #pragma once
 
 #include "stencil2_kernel.cuh"
@@ -31,58 +33,31 @@ struct Tile2Geom {
     static constexpr int smem_bytes() { return NARR * F * 4 + 16; }
 };
 
-template <int R, int S, int NT, bool EXACT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) stencil2d_tile_kernel(const __grid_constant__ BatchArgs B)
+// One ALM iteration of tile li of problem P from parity par, in the frame
+// `fsm` (Tile2Geom::NARR arrays): loads, the phases, the stores of the new
+// flows and state.  Returns the thread's share of erriter.  State is read
+// through L2 (ld.global.cg): the persistent kernel reads what other blocks
+// wrote during the same launch.
+template <int R, int S, int NT, bool EXACT>
+__device__ __forceinline__ float tile2_iteration(const ProblemDesc &P, int par, int li, float *fsm)
 {
     using G = Tile2Geom<R, S>;
-    constexpr int FR = G::FR, FC = G::FC, F = G::F;
-
-    extern __shared__ __align__(16) float fsm[];
-    __shared__ double s_red[NT / 32];
-    __shared__ int s_is_last;
-    __shared__ int s_item;
-    __shared__ int s_iter;
-
-    // frame arrays [column][row]: old flows (overwritten by b''), old state,
-    // alpha, gk, b', g2
+    constexpr int FR = G::FR, F = G::F;
     float *BR = fsm, *BS = fsm + F, *PS = fsm + 2 * F, *PT = fsm + 3 * F, *U = fsm + 4 * F;
     float *AL = fsm + 5 * F, *GK = fsm + 6 * F, *BR1 = fsm + 7 * F, *BS1 = fsm + 8 * F;
     float *G2 = fsm + 9 * F;
     const int tid = threadIdx.x;
-
-    while (true) {
-        if (tid == 0) {
-            const int itm = (int)atomicAdd(&B.queue[0], 1u);
-            int iter = -1;
-            if (itm < B.total_items) {
-                const IterControl *c = B.probs[B.item_problem[itm]].ctl;
-                iter = *(const volatile int *)&c->done ? -1 : *(const volatile int *)&c->iter;
-            }
-            s_item = itm;
-            s_iter = iter;
-        }
-        __syncthreads();
-        const int item = s_item;
-        const int it = s_iter;
-        __syncthreads();  // s_item/s_iter are rewritten by the next fetch
-        if (item >= B.total_items)
-            break;
-        if (it < 0)
-            continue;  // the problem has converged
-        const ProblemDesc &P = B.probs[B.item_problem[item]];
-        const int par = it & 1;
-        const int nr = P.nr, ns = P.ns;
-        const float cc = P.cc, inv_cc = P.inv_cc, steps = P.steps;
-        const int li = item - P.item_begin;
-        const int r0 = (li % P.tiles_r) * R;
-        const int s0 = (li / P.tiles_r) * S;
-        const unsigned int pitch = (unsigned int)P.plane_stride;  // one row of Matlab x
-        // old state: the other parity's destinations
-        const float *__restrict__ src_br = P.dst_b[par ^ 1][SL_BR];
-        const float *__restrict__ src_bs = P.dst_b[par ^ 1][SL_BS];
-        const float *__restrict__ src_ps = P.dst_s[par ^ 1][0];
-        const float *__restrict__ src_pt = P.dst_s[par ^ 1][1];
-        const float *__restrict__ src_u = P.dst_s[par ^ 1][2];
+    const int nr = P.nr, ns = P.ns;
+    const float cc = P.cc, inv_cc = P.inv_cc, steps = P.steps;
+    const int r0 = (li % P.tiles_r) * R;
+    const int s0 = (li / P.tiles_r) * S;
+    const unsigned int pitch = (unsigned int)P.plane_stride;  // one row of Matlab x
+    // old state: the other parity's destinations
+    const float *src_br = P.dst_b[par ^ 1][SL_BR];
+    const float *src_bs = P.dst_b[par ^ 1][SL_BS];
+    const float *src_ps = P.dst_s[par ^ 1][0];
+    const float *src_pt = P.dst_s[par ^ 1][1];
+    const float *src_u = P.dst_s[par ^ 1][2];
         float erru = 0.0f;
 
         // Frame cell (c, q) <-> pixel (r0-2+q, s0-2+c).  Every load of the
@@ -98,12 +73,12 @@ __global__ void __launch_bounds__(NT, MINB) stencil2d_tile_kernel(const __grid_c
             const int r = r0 - 2 + q, s = s0 - 2 + c;
             const bool in = (i < F && r >= 0 && r < nr && s >= 0 && s < ns);
             const unsigned int g = (unsigned int)s * pitch + (unsigned int)r;
-            v[0][k] = in ? src_br[g] : 0.f;
-            v[1][k] = in ? src_bs[g] : 0.f;
-            v[2][k] = in ? src_ps[g] : 0.f;
-            v[3][k] = in ? src_pt[g] : 0.f;
-            v[4][k] = in ? src_u[g] : 0.f;
-            v[5][k] = in ? P.alpha[g] : 0.f;
+            v[0][k] = in ? __ldcg(src_br + g) : 0.f;
+            v[1][k] = in ? __ldcg(src_bs + g) : 0.f;
+            v[2][k] = in ? __ldcg(src_ps + g) : 0.f;
+            v[3][k] = in ? __ldcg(src_pt + g) : 0.f;
+            v[4][k] = in ? __ldcg(src_u + g) : 0.f;
+            v[5][k] = in ? __ldcg(P.alpha + g) : 0.f;
         }
 #pragma unroll
         for (int k = 0; k < PIX; ++k) {
@@ -111,8 +86,8 @@ __global__ void __launch_bounds__(NT, MINB) stencil2d_tile_kernel(const __grid_c
             const int r = r0 + i % R, s = s0 + i / R;
             const bool in = (i < R * S && r < nr && s < ns);
             const unsigned int g = (unsigned int)s * pitch + (unsigned int)r;
-            cs_v[k] = in ? P.cs[g] : 0.f;
-            ct_v[k] = in ? P.ct[g] : 0.f;
+            cs_v[k] = in ? __ldcg(P.cs + g) : 0.f;
+            ct_v[k] = in ? __ldcg(P.ct + g) : 0.f;
         }
 #pragma unroll
         for (int k = 0; k < PER; ++k) {
@@ -224,7 +199,42 @@ __global__ void __launch_bounds__(NT, MINB) stencil2d_tile_kernel(const __grid_c
             d_pt[g] = pt_n;
             d_u[g] = u - e;
         }
-        __syncthreads();  // the frame is reused by the next item
+    __syncthreads();  // the frame is reused by the next item or iteration
+    return erru;
+}
+
+template <int R, int S, int NT, bool EXACT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) stencil2d_tile_kernel(const __grid_constant__ BatchArgs B)
+{
+    extern __shared__ __align__(16) float fsm[];
+    __shared__ double s_red[NT / 32];
+    __shared__ int s_is_last;
+    __shared__ int s_item;
+    __shared__ int s_iter;
+    const int tid = threadIdx.x;
+
+    while (true) {
+        if (tid == 0) {
+            const int itm = (int)atomicAdd(&B.queue[0], 1u);
+            int iter = -1;
+            if (itm < B.total_items) {
+                const IterControl *c = B.probs[B.item_problem[itm]].ctl;
+                iter = *(const volatile int *)&c->done ? -1 : *(const volatile int *)&c->iter;
+            }
+            s_item = itm;
+            s_iter = iter;
+        }
+        __syncthreads();
+        const int item = s_item;
+        const int it = s_iter;
+        __syncthreads();  // s_item/s_iter are rewritten by the next fetch
+        if (item >= B.total_items)
+            break;
+        if (it < 0)
+            continue;  // the problem has converged
+        const ProblemDesc &P = B.probs[B.item_problem[item]];
+        const int li = item - P.item_begin;
+        const float erru = tile2_iteration<R, S, NT, EXACT>(P, it & 1, li, fsm);
         finish_item<NT>(erru, P, li, it, B.done_count, s_red, &s_is_last);
     }
 
@@ -236,6 +246,94 @@ __global__ void __launch_bounds__(NT, MINB) stencil2d_tile_kernel(const __grid_c
             B.queue[1] = 0;
             __threadfence();
         }
+    }
+}
+
+// Every iteration of one problem in one cooperative launch: block b keeps
+// tile b for the whole solve; after each iteration the blocks meet at a grid
+// barrier (an arrival counter in B.queue[0], zeroed before the launch; each
+// wait bounded by time, a timeout sets DEV_ERR_TIMEOUT and ends the solve),
+// then every block sums the tiles' erriter partials in the order finish_item
+// uses, so all take the same stopping decision; block 0 records cvg, itNum
+// and the control block as finish_item does.  The launch and per-iteration
+// hand-off of the one-launch-per-iteration form (queue, ticket, kernel
+// boundary) is replaced by one barrier.  Partials alternate between two
+// halves of item_partials by iteration parity.
+template <int R, int S, int NT, bool EXACT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    stencil2d_tile_persistent_kernel(const __grid_constant__ BatchArgs B)
+{
+    extern __shared__ __align__(16) float fsm[];
+    __shared__ double s_red[NT / 32];
+    __shared__ int s_stop;
+    const int tid = threadIdx.x;
+    const ProblemDesc &P = B.probs[0];
+    IterControl *ctl = P.ctl;
+    const int nb = (int)gridDim.x;   // one block per tile
+    const int li = (int)blockIdx.x;
+    if (*(volatile int *)&ctl->done)
+        return;
+    int it = *(volatile int *)&ctl->iter;
+    const int max_it = ctl->max_it;
+    const int break_lt = ctl->break_lt;
+    const float err_bound = ctl->err_bound, denom = ctl->denom;
+    unsigned int *arrivals = &B.queue[0];
+    for (unsigned int gen = 1;; ++gen) {
+        const float erru = tile2_iteration<R, S, NT, EXACT>(P, it & 1, li, fsm);
+        const double part = block_sum_double<NT>(erru, s_red);
+        if (tid == 0) {
+            P.item_partials[(it & 1) * nb + li] = part;
+            __threadfence();
+            atomicAdd(arrivals, 1u);
+            // grid barrier: every block's state and partial of iteration it
+            const unsigned int target = gen * (unsigned int)nb;
+            int stop = 0;
+            if (*(volatile unsigned int *)arrivals < target) {
+                const unsigned long long t0 = global_timer_ns();
+                while (*(volatile unsigned int *)arrivals < target) {
+                    if (global_timer_ns() - t0 > kWaitBudgetNs) {
+                        atomicOr(&ctl->error, DEV_ERR_TIMEOUT);
+                        stop = 2;
+                        break;
+                    }
+                }
+            }
+            __threadfence();
+            s_stop = stop;
+        }
+        __syncthreads();
+        if (s_stop == 2)
+            break;  // a block did not arrive
+        if (tid < 32) {
+            double acc = 0.0;
+            for (int b = tid; b < nb; b += 32)
+                acc += __ldcg(P.item_partials + (it & 1) * nb + b);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+                acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (tid == 0) {
+                // cvg[i] = total_err / (float)N, total_err a float
+                // (maxflow/asetsBinaryMF2D_mex.c, runMaxFlow)
+                const float c = __fdiv_rn((float)acc, denom);
+                const bool conv = break_lt ? (c < err_bound) : (c <= err_bound);
+                const int done = (conv || it + 1 >= max_it) ? 1 : 0;
+                if (li == 0) {
+                    P.cvg[it] = c;
+                    ctl->last_iter = it;
+                    ctl->iter = it + 1;
+                    if (done) {
+                        ctl->it_num = conv ? it : max_it;
+                        ctl->done = 1;
+                    }
+                    __threadfence();
+                }
+                s_stop = done;
+            }
+        }
+        __syncthreads();
+        if (s_stop)
+            break;
+        ++it;
     }
 }
 

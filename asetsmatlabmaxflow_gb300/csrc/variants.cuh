@@ -55,8 +55,10 @@ StencilVariant make_variant_t2()
     return v;
 }
 
-// The binary 2D square-tile kernel (stencil2d_tile.cuh): R x S tiles, NT threads.
-template <int R, int S, int NT, bool EXACT, int MINB = 2>
+// The binary 2D square-tile kernels (stencil2d_tile.cuh): R x S tiles, NT
+// threads; one launch per iteration, or (PERSISTENT) every iteration in one
+// cooperative launch.
+template <int R, int S, int NT, bool EXACT, int MINB = 2, bool PERSISTENT = false>
 StencilVariant make_variant_tile()
 {
     using G = Tile2Geom<R, S>;
@@ -74,8 +76,12 @@ StencilVariant make_variant_tile()
     v.box_cols_bc = 1;
     v.tile_box_rows = R;
     v.temporal = 1;
-    v.fn = reinterpret_cast<const void *>(&stencil2d_tile_kernel<R, S, NT, EXACT, MINB>);
+    if constexpr (PERSISTENT)
+        v.fn = reinterpret_cast<const void *>(&stencil2d_tile_persistent_kernel<R, S, NT, EXACT, MINB>);
+    else
+        v.fn = reinterpret_cast<const void *>(&stencil2d_tile_kernel<R, S, NT, EXACT, MINB>);
     v.s_tile = S;
+    v.persistent = PERSISTENT ? 1 : 0;
     return v;
 }
 

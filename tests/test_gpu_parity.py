@@ -253,12 +253,13 @@ def test_odd_shapes_binary3d_against_oracle(dims):
     s.close()
 
 
-@pytest.mark.parametrize("tile_config", [1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("tile_config", [1, 2, 3, 4, 5, 6, 7, 8, 9])
 def test_every_binary2d_fast_variant_meets_parity_bar(tile_config):
     """Each compiled variant of the fast binary 2D kernel (two iterations per
     pass with 224-row tiles; one per pass with 224- and 56-row tiles and two
     rows per thread with 240-row tiles and four or six stages; 32 x 32 and
-    16 x 16 square tiles), selected explicitly, against the oracle, on a
+    16 x 16 square tiles, per iteration and whole-solve), selected
+    explicitly, against the oracle, on a
     column length that is not a multiple of any tile and is odd."""
     from asetsmatlabmaxflow_gb300 import native as N
 

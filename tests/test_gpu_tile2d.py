@@ -1,11 +1,14 @@
-"""GPU parity of the binary 2D square-tile kernel (stencil2d_tile.cuh): one
-whole iteration of a 32 x 32 or 16 x 16 tile per block, for small images.
+"""GPU parity of the binary 2D square-tile kernels (stencil2d_tile.cuh): one
+whole iteration of a 32 x 32 or 16 x 16 tile per block, for small images,
+one launch per iteration or every iteration in one cooperative launch.
 
-It is selected with tile_config 6, 7 (fast) and 5, 6 (EXACT), after the
-sweep variants.  EXACT results must be bit-identical to the oracle and to
-the sweep kernel (u, ps, pt and the spatial flows), the fast build meets
-the parity bar, stopping runs stop where the oracle stops, and a batch of
-small images runs it."""
+They are selected with tile_config 6-9 (fast) and 5-8 (EXACT), after the
+sweep variants: 32 x 32, 16 x 16, then the same as whole-solve launches.
+EXACT results must be bit-identical to the oracle and to the sweep kernel
+(u, ps, pt and the spatial flows), the fast build meets the parity bar,
+stopping runs stop where the oracle stops, a batch of small images runs
+the per-iteration form, and a problem with more tiles than can be resident
+is refused by the whole-solve form."""
 import numpy as np
 import pytest
 
@@ -14,8 +17,8 @@ from tests.gpu_helpers import assert_parity_bar, bits, require_gpu
 
 pytestmark = pytest.mark.gpu
 
-TILE_FAST = (6, 7)
-TILE_EXACT = (5, 6)
+TILE_FAST = (6, 7, 8, 9)
+TILE_EXACT = (5, 6, 7, 8)
 SWEEP = 1
 
 
@@ -82,7 +85,8 @@ def test_fast_tile_meets_parity_bar(dims, tc):
 
 
 @pytest.mark.parametrize("exact", [True, False])
-def test_tile_stops_where_the_oracle_stops(exact):
+@pytest.mark.parametrize("k", [0, 1, 2, 3])
+def test_tile_stops_where_the_oracle_stops(exact, k):
     dims = (256, 256)
     inp = _inputs(dims, 23)
     free = O.solve("binary", dims, inp["Ct"], inp["alpha"], cs=inp["Cs"], max_it=400,
@@ -96,7 +100,7 @@ def test_tile_stops_where_the_oracle_stops(exact):
     assert 120 <= ref["it"] < 400
     if np.any(np.abs(free["cvg"][:ref["it"] + 1] / eb - 1.0) < 1e-3):
         pytest.skip("an erriter lies within rounding of errBound")
-    t = _solve(dims, inp, 400, eb, exact, TILE_EXACT[0] if exact else TILE_FAST[0])
+    t = _solve(dims, inp, 400, eb, exact, TILE_EXACT[k] if exact else TILE_FAST[k])
     assert t["it"] == ref["it"]
     if exact:
         np.testing.assert_array_equal(bits(t["u"]), bits(ref["u"]))
@@ -126,3 +130,62 @@ def test_batch_of_small_images_with_square_tiles():
     b.close()
     for s in solvers:
         s.close()
+
+
+@pytest.mark.parametrize("tc", TILE_EXACT[2:])
+def test_whole_solve_launch_edges(tc):
+    """maxIt 0 and 1, a warm start continued from a saved state (the second
+    run equals an uninterrupted one), all in one cooperative launch each."""
+    from asetsmatlabmaxflow_gb300 import native as N
+
+    dims = (97, 83)
+    inp = _inputs(dims, 40)
+    ref = O.solve("binary", dims, inp["Ct"], inp["alpha"], cs=inp["Cs"], max_it=20,
+                  err_bound=0.0, cc=0.3, steps=0.16)
+    s = N.Solver(N.Context.default(), "binary", dims)
+    s.set_inputs(inp["Ct"], inp["alpha"], inp["Cs"])
+    assert s.run(0, 0.0, 0.3, 0.16, exact=True, tile_config=tc) == 0
+    assert s.last_run_stats()[1] == 0
+    assert s.run(1, 0.0, 0.3, 0.16, exact=True, tile_config=tc) == 1
+    assert s.last_run_stats()[1] == 1
+    s.run(12, 0.0, 0.3, 0.16, exact=True, tile_config=tc)
+    u = s.get_u()
+    ps, pt = s.get_flows()
+    bx, by, _ = s.get_spatial_flows()
+    s.set_initial(u0=u, ps0=ps, pt0=pt)
+    s.set_initial_flows(bx=bx, by=by)
+    assert s.run(8, 0.0, 0.3, 0.16, exact=True, tile_config=tc) == 8
+    np.testing.assert_array_equal(bits(s.get_u()), bits(ref["u"]))
+    s.close()
+
+
+def test_whole_solve_launch_refuses_too_many_tiles():
+    """4096^2 in 16 x 16 tiles is 65,536 blocks: more than can be resident,
+    so the cooperative form reports UNSUPPORTED instead of launching."""
+    from asetsmatlabmaxflow_gb300 import native as N
+
+    dims = (4096, 4096)
+    g = np.random.default_rng(41)
+    cs, ct = (np.asfortranarray(g.random(dims, dtype=np.float32)) for _ in range(2))
+    s = N.Solver(N.Context.default(), "binary", dims)
+    s.set_inputs(ct, np.full(dims, 0.5, np.float32, order="F"), cs)
+    with pytest.raises(N.AsetsError, match="too many tiles"):
+        s.run(4, 0.0, 0.3, 0.16, tile_config=TILE_FAST[3])
+    assert s.run(4, 0.0, 0.3, 0.16) == 4  # the default still solves it
+    s.close()
+
+
+@pytest.mark.parametrize("dims,launches", [((256, 256), 1), ((301, 170), 1), ((512, 512), 1),
+                                           ((1024, 1024), 16)])
+def test_default_whole_solve_on_small_images(dims, launches):
+    """Without a tile_config a binary 2D image whose tiles can all be
+    resident runs as one cooperative launch; a larger one keeps the sweep
+    (16 iterations per CUDA-graph chunk, two per launch)."""
+    from asetsmatlabmaxflow_gb300 import native as N
+
+    inp = _inputs(dims, 42)
+    s = N.Solver(N.Context.default(), "binary", dims)
+    s.set_inputs(inp["Ct"], inp["alpha"], inp["Cs"])
+    assert s.run(20, 0.0, 0.3, 0.16) == 20
+    assert s.last_run_stats()[1] == launches
+    s.close()
