@@ -421,6 +421,9 @@ static bool persistent_fits(const asets_solver *s, const StencilVariant *v)
     return tiles <= (long long)per_sm * s->ctx->num_sms;
 }
 
+// Largest multi-label 2D image (pixels) the whole-solve tile kernel takes by default.
+static constexpr long long kTileLabelsMaxPx = 1LL << 17;
+
 static const StencilVariant *pick_variant(const asets_solver *s, int exact, int tile_config,
                                           bool single)
 {
@@ -429,17 +432,22 @@ static const StencilVariant *pick_variant(const asets_solver *s, int exact, int 
         return nullptr;
     if (tile_config > 0 && tile_config <= (int)match.size())
         return match[tile_config - 1];
-    // the one-pass multi-label kernels lead the list (in-step update, one
-    // label warp, two); by default they run where they measured faster than
-    // the two-pass form on a GB300: two million pixels and more (two label
-    // warps for up to three flow labels, one above), and half a million with
-    // six flow labels or more (in-step update)
+    // the one-pass multi-label kernels lead the list: three sweeps (in-step
+    // update, one label warp, two), then 16 x 16 tiles (one launch per
+    // iteration, the whole solve in one).  By default they run where they
+    // measured faster than the two-pass form on a GB300: the whole-solve
+    // tiles on small images whose tiles all fit at once, up to five flow
+    // labels (the tile runs its labels one after another); the sweeps on two
+    // million pixels and more (two label warps for up to three flow labels,
+    // one above), and half a million with six flow labels or more (in-step)
     int n_fused = 0;
     while (n_fused < (int)match.size() && match[n_fused]->epi == EPI_FUSED)
         ++n_fused;
-    if (n_fused == 3) {
+    if (n_fused == 5) {
         const long long px = (long long)s->nr * s->ns;
         const int fl = s->flow_labels;
+        if (px <= kTileLabelsMaxPx && fl <= 5 && persistent_fits(s, match[4]))
+            return match[4];
         if (px >= 2000000)
             return match[fl <= 3 ? 2 : 1];
         if (px >= 500000 && fl >= 6)

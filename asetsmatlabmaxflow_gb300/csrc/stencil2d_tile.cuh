@@ -250,24 +250,21 @@ __global__ void __launch_bounds__(NT, MINB) stencil2d_tile_kernel(const __grid_c
 }
 
 // Every iteration of one problem in one cooperative launch: block b keeps
-// tile b for the whole solve; after each iteration the blocks meet at a grid
-// barrier (an arrival counter in B.queue[0], zeroed before the launch; each
-// wait bounded by time, a timeout sets DEV_ERR_TIMEOUT and ends the solve),
-// then every block sums the tiles' erriter partials in the order finish_item
-// uses, so all take the same stopping decision; block 0 records cvg, itNum
-// and the control block as finish_item does.  The launch and per-iteration
-// hand-off of the one-launch-per-iteration form (queue, ticket, kernel
-// boundary) is replaced by one barrier.  Partials alternate between two
-// halves of item_partials by iteration parity.
-template <int R, int S, int NT, bool EXACT, int MINB>
-__global__ void __launch_bounds__(NT, MINB)
-    stencil2d_tile_persistent_kernel(const __grid_constant__ BatchArgs B)
+// tile b for the whole solve; after each iteration (`iteration(it)` returns
+// the thread's erriter share) the blocks meet at a grid barrier (an arrival
+// counter, zeroed before the launch; each wait bounded by time, a timeout
+// sets DEV_ERR_TIMEOUT and ends the solve), then every block sums the
+// tiles' erriter partials in the order finish_item uses, so all take the
+// same stopping decision; block 0 records cvg, itNum and the control block
+// as finish_item does.  The launch and per-iteration hand-off of the
+// one-launch-per-iteration form (queue, ticket, kernel boundary) is replaced
+// by one barrier.  Partials alternate between two halves of item_partials by
+// iteration parity.
+template <int NT, class Iteration>
+__device__ __forceinline__ void tile_solve_loop(const ProblemDesc &P, unsigned int *arrivals,
+                                                double *s_red, int *s_stop, Iteration iteration)
 {
-    extern __shared__ __align__(16) float fsm[];
-    __shared__ double s_red[NT / 32];
-    __shared__ int s_stop;
     const int tid = threadIdx.x;
-    const ProblemDesc &P = B.probs[0];
     IterControl *ctl = P.ctl;
     const int nb = (int)gridDim.x;   // one block per tile
     const int li = (int)blockIdx.x;
@@ -277,9 +274,8 @@ __global__ void __launch_bounds__(NT, MINB)
     const int max_it = ctl->max_it;
     const int break_lt = ctl->break_lt;
     const float err_bound = ctl->err_bound, denom = ctl->denom;
-    unsigned int *arrivals = &B.queue[0];
     for (unsigned int gen = 1;; ++gen) {
-        const float erru = tile2_iteration<R, S, NT, EXACT>(P, it & 1, li, fsm);
+        const float erru = iteration(it);
         const double part = block_sum_double<NT>(erru, s_red);
         if (tid == 0) {
             P.item_partials[(it & 1) * nb + li] = part;
@@ -299,10 +295,10 @@ __global__ void __launch_bounds__(NT, MINB)
                 }
             }
             __threadfence();
-            s_stop = stop;
+            *s_stop = stop;
         }
         __syncthreads();
-        if (s_stop == 2)
+        if (*s_stop == 2)
             break;  // a block did not arrive
         if (tid < 32) {
             double acc = 0.0;
@@ -312,8 +308,7 @@ __global__ void __launch_bounds__(NT, MINB)
             for (int o = 16; o > 0; o >>= 1)
                 acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (tid == 0) {
-                // cvg[i] = total_err / (float)N, total_err a float
-                // (maxflow/asetsBinaryMF2D_mex.c, runMaxFlow)
+                // cvg[i] = total_err / (float)N, total_err a float (runMaxFlow)
                 const float c = __fdiv_rn((float)acc, denom);
                 const bool conv = break_lt ? (c < err_bound) : (c <= err_bound);
                 const int done = (conv || it + 1 >= max_it) ? 1 : 0;
@@ -327,14 +322,27 @@ __global__ void __launch_bounds__(NT, MINB)
                     }
                     __threadfence();
                 }
-                s_stop = done;
+                *s_stop = done;
             }
         }
         __syncthreads();
-        if (s_stop)
+        if (*s_stop)
             break;
         ++it;
     }
+}
+
+template <int R, int S, int NT, bool EXACT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
+    stencil2d_tile_persistent_kernel(const __grid_constant__ BatchArgs B)
+{
+    extern __shared__ __align__(16) float fsm[];
+    __shared__ double s_red[NT / 32];
+    __shared__ int s_stop;
+    const ProblemDesc &P = B.probs[0];
+    tile_solve_loop<NT>(P, B.queue, s_red, &s_stop, [&](int it) {
+        return tile2_iteration<R, S, NT, EXACT>(P, it & 1, (int)blockIdx.x, fsm);
+    });
 }
 
 }  // namespace asets

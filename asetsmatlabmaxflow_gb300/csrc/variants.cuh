@@ -6,6 +6,7 @@
 #include "stencil2d_t2.cuh"
 #include "stencil2d_labels.cuh"
 #include "stencil2d_tile.cuh"
+#include "stencil2d_tile_labels.cuh"
 
 namespace asets {
 
@@ -81,6 +82,38 @@ StencilVariant make_variant_tile()
     else
         v.fn = reinterpret_cast<const void *>(&stencil2d_tile_kernel<R, S, NT, EXACT, MINB>);
     v.s_tile = S;
+    v.persistent = PERSISTENT ? 1 : 0;
+    return v;
+}
+
+// The multi-label 2D 16 x 16 tile kernels (stencil2d_tile_labels.cuh) for
+// MODEL (1 Potts, 2 Ishikawa), any label count up to 8 flow labels; one
+// launch per iteration, or (PERSISTENT) the whole solve in one cooperative
+// launch.  pt/u/ps ping-pong as in the one-pass sweep kernels.
+template <int MODEL, bool EXACT, bool PERSISTENT>
+StencilVariant make_variant_tile_labels()
+{
+    using G = LTileGeom<MODEL>;
+    constexpr int NT = 128;
+    StencilVariant v;
+    v.dim = 2;
+    v.epi = EPI_FUSED;
+    v.exact = EXACT ? 1 : 0;
+    v.tr = G::R;
+    v.tc = 1;
+    v.nt = NT;
+    v.nstage = 0;
+    v.smem_bytes = G::smem_bytes();
+    v.box_rows = G::R + 8;    // unused maps, encoded like the sweep's
+    v.box_cols = 1;
+    v.box_cols_bc = 1;
+    v.tile_box_rows = G::R;
+    v.temporal = 1;
+    if constexpr (PERSISTENT)
+        v.fn = reinterpret_cast<const void *>(&stencil2d_tile_labels_persistent_kernel<MODEL, NT, EXACT>);
+    else
+        v.fn = reinterpret_cast<const void *>(&stencil2d_tile_labels_kernel<MODEL, NT, EXACT>);
+    v.s_tile = G::S;
     v.persistent = PERSISTENT ? 1 : 0;
     return v;
 }

@@ -27,9 +27,9 @@ def _rand(model, dims, L, seed):
 CASES = [
     ("binary", (33, 41, 29), 1, 5, 4), ("binary", (5, 7, 3), 1, 5, 4), ("binary", (1, 9, 8), 1, 5, 4),
     ("binary", (121, 13, 6), 1, 5, 4), ("binary", (301, 170), 1, 9, 8), ("binary", (1, 9), 1, 9, 8),
-    ("binary", (450, 5), 1, 9, 8), ("potts", (48, 40, 20), 4, 6, 6), ("potts", (130, 97), 5, 7, 7),
-    ("potts", (7, 33), 2, 7, 7), ("ishikawa", (40, 33, 17), 4, 6, 6),
-    ("ishikawa", (160, 120), 8, 7, 7), ("ishikawa", (61, 9), 3, 7, 7),
+    ("binary", (450, 5), 1, 9, 8), ("potts", (48, 40, 20), 4, 6, 6), ("potts", (130, 97), 5, 9, 9),
+    ("potts", (7, 33), 2, 9, 9), ("ishikawa", (40, 33, 17), 4, 6, 6),
+    ("ishikawa", (160, 120), 8, 9, 9), ("ishikawa", (61, 9), 3, 9, 9),
 ]
 # (model, shape, labels, fast variants, EXACT variants): the variant counts of
 # the tables in csrc/{binary,flow}{2d,3d}_{fast,exact}.cu, plus the one-pass

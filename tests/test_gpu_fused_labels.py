@@ -15,9 +15,10 @@ from tests.gpu_helpers import assert_parity_bar, bits, require_gpu
 pytestmark = pytest.mark.gpu
 
 # tile_config of the one-pass forms: the label update in the flow warps,
-# one label warp, two label warps; then the two-pass form
-FUSED_FORMS = (1, 2, 3)
-FUSED, TWO_PASS = 1, 4
+# one label warp, two label warps, 16 x 16 tiles per iteration and for the
+# whole solve; then the two-pass form
+FUSED_FORMS = (1, 2, 3, 4, 5)
+FUSED, TWO_PASS = 1, 6
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -115,20 +116,23 @@ def test_fused_stops_where_the_oracle_stops(model, L, exact, tc):
     assert_parity_bar(model, dims, L, f["u"], ref["u"], f["cvg"], ref["cvg"], it=n)
 
 
-@pytest.mark.parametrize("model,dims,L,fused", [
-    ("potts", (2048, 1024), 4, True), ("ishikawa", (1024, 1024), 8, True),
-    ("ishikawa", (1024, 1024), 3, False), ("potts", (512, 512), 8, False)])
-def test_default_form_by_size(model, dims, L, fused):
-    """Without a tile_config the one-pass kernel runs on two million pixels
-    and more, and on half a million with six flow labels or more: one launch
-    per iteration instead of two."""
+@pytest.mark.parametrize("model,dims,L,launches", [
+    ("potts", (2048, 1024), 4, 16), ("ishikawa", (1024, 1024), 8, 16),
+    ("ishikawa", (1024, 1024), 3, 32), ("potts", (512, 512), 8, 32),
+    ("potts", (256, 256), 4, 1), ("ishikawa", (200, 150), 6, 1), ("potts", (256, 256), 8, 32)])
+def test_default_form_by_size(model, dims, L, launches):
+    """Without a tile_config the one-pass sweep kernel runs on two million
+    pixels and more, and on half a million with six flow labels or more (one
+    launch per iteration, one chunk of 16); small images with up to five
+    flow labels run the whole solve in one cooperative launch; the rest the
+    two-pass form (two launches per iteration)."""
     from asetsmatlabmaxflow_gb300 import native as N
 
     ct, alpha = _inputs(model, dims, L, 16)
     s = N.Solver(N.Context.default(), model, dims, L)
     s.set_inputs(ct, alpha)
     assert s.run(4, 0.0, 0.3, 0.16) == 4
-    assert s.last_run_stats()[1] == (16 if fused else 32)  # one chunk of 16 iterations
+    assert s.last_run_stats()[1] == launches
     s.close()
 
 
