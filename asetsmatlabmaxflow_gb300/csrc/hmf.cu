@@ -10,7 +10,8 @@
 //      of every non-root node (the first line of UpdateSpatialFlows) -- all
 //      per-pixel, so one pass;
 //   K2 gradient step of the spatial flows, K3 flow magnitude and projection
-//   factor, K4 flow rescale, K5 divergence (the rest of UpdateSpatialFlows).
+//   factor, K4 flow rescale, K5 divergence (the rest of UpdateSpatialFlows);
+//   in 2D without direction fields one tiled kernel runs K2-K5.
 // Costs (CalculateCostsFullFlow) are summed on the device in double.
 //
 // The DAG solver (maxflow/asetsDAGMF2D.m / 3D, nodes may have several
@@ -647,6 +648,136 @@ __global__ void k_dag_point(const HArgs<T> A)
     }
 }
 
+// The four spatial passes (k2 .. k5) fused for 2D solves without direction
+// fields: one block per (node, R x S tile of cells) computes, in shared
+// memory over the tile and a two-cell halo, the gradient step of the faces
+// (k2), the projection factor (k3), the rescale (k4) and the divergence
+// (k5), with each pass's expression and validity tests, and stores the
+// tile's faces, divergence and factor (g) as the passes leave them.  The
+// halo's faces are recomputed by the neighbouring tiles' blocks; one read
+// and one write of each array instead of four passes over them.
+template <class T, int R, int S>
+struct SpatialTile {
+    static constexpr int FR = R + 4;   // frame cells y0-2 .. y0+R+1
+    static constexpr int FC = S + 4;   // frame cells x0-2 .. x0+S+1
+    static constexpr int F = FR * FC;
+    static constexpr int smem_bytes() { return 5 * F * (int)sizeof(T); }
+};
+
+template <class T, int R, int S>
+__global__ void __launch_bounds__(kThreads) k_spatial_tile2d(const HArgs<T> A, int tiles_y)
+{
+    using Q = SpatialTile<T, R, S>;
+    constexpr int FR = Q::FR, F = Q::F;
+    extern __shared__ __align__(16) unsigned char hsm[];
+    T *G = reinterpret_cast<T *>(hsm);   // g, at cells
+    T *P1 = G + F;                        // face (y, y+1) at cell y
+    T *P2 = P1 + F;                       // face (x, x+1) at cell x
+    T *FS = P2 + F;                       // projection factor
+    T *AL = FS + F;
+    const int i = 1 + (int)blockIdx.y;    // non-root node
+    const int y0 = ((int)blockIdx.x % tiles_y) * R, x0 = ((int)blockIdx.x / tiles_y) * S;
+    const int d1 = A.d1, d2 = A.d2;
+    const NodeDev<T> nd = A.nodes[i];
+    const T *g = A.g + (long long)i * A.n;
+    T *p1 = A.p1 + (long long)i * A.f1;
+    T *p2 = A.p2 + (long long)i * A.f2;
+    const int tid = threadIdx.x;
+    for (int k = tid; k < F; k += kThreads) {
+        const int c = k / FR, q = k - c * FR;
+        const int y = y0 - 2 + q, x = x0 - 2 + c;
+        const bool in = (y >= 0 && y < d1 && x >= 0 && x < d2);
+        const unsigned int cell = (unsigned int)x * (unsigned int)d1 + (unsigned int)y;
+        G[k] = in ? g[cell] : (T)0;
+        P1[k] = (in && y + 1 < d1) ? p1[(unsigned int)x * (unsigned int)(d1 - 1) + (unsigned int)y] : (T)0;
+        P2[k] = (in && x + 1 < d2) ? p2[cell] : (T)0;
+        AL[k] = in ? (nd.alpha ? nd.alpha[cell] : nd.alpha_s) : (T)0;
+    }
+    __syncthreads();
+    // k2: 2D p + (g(k+1) - g(k)) (asetsHMF2D.m), else (p + g(k+1)) - g(k)
+    auto step = [&](T pv, T gn, T gc) { return A.paren ? add(pv, sub(gn, gc)) : sub(add(pv, gn), gc); };
+    for (int k = tid; k < (R + 3) * (S + 2); k += kThreads) {   // p1: y0-2 .. y0+R, x0-1 .. x0+S
+        const int c = 1 + k / (R + 3), q = k % (R + 3);
+        const int f = c * FR + q;
+        const int y = y0 - 2 + q, x = x0 - 2 + c;
+        if (y >= 0 && y + 1 < d1 && x >= 0 && x < d2)
+            P1[f] = step(P1[f], G[f + 1], G[f]);
+    }
+    for (int k = tid; k < (R + 2) * (S + 3); k += kThreads) {   // p2: y0-1 .. y0+R, x0-2 .. x0+S
+        const int c = k / (R + 2), q = 1 + k % (R + 2);
+        const int f = c * FR + q;
+        const int y = y0 - 2 + q, x = x0 - 2 + c;
+        if (x >= 0 && x + 1 < d2 && y >= 0 && y < d1)
+            P2[f] = step(P2[f], G[f + FR], G[f]);
+    }
+    __syncthreads();
+    // k3: the cell's faces' squares in the .m files' order, the factor
+    for (int k = tid; k < (R + 2) * (S + 2); k += kThreads) {   // y0-1 .. y0+R, x0-1 .. x0+S
+        const int c = 1 + k / (R + 2), q = 1 + k % (R + 2);
+        const int f = c * FR + q;
+        const int y = y0 - 2 + q, x = x0 - 2 + c;
+        if (y < 0 || y >= d1 || x < 0 || x >= d2)
+            continue;
+        T sq = (T)0;
+        if (y + 1 < d1)
+            sq = add(sq, mul(P1[f], P1[f]));
+        if (y >= 1)
+            sq = add(sq, mul(P1[f - 1], P1[f - 1]));
+        if (x + 1 < d2)
+            sq = add(sq, mul(P2[f], P2[f]));
+        if (x >= 1)
+            sq = add(sq, mul(P2[f - FR], P2[f - FR]));
+        const T mag = sqr(sq);
+        const T al = AL[f];
+        FS[f] = (mag <= al) ? (T)1 : dvd(al, mag);
+    }
+    __syncthreads();
+    // k4: p = 0.5 p (f(k+1) + f(k)); the tile's own faces are stored
+    for (int k = tid; k < (R + 1) * S; k += kThreads) {         // p1: y0-1 .. y0+R-1, tile columns
+        const int c = 2 + k / (R + 1), q = 1 + k % (R + 1);
+        const int f = c * FR + q;
+        const int y = y0 - 2 + q, x = x0 - 2 + c;
+        if (y < 0 || y + 1 >= d1 || x >= d2)
+            continue;
+        const T r = mul(mul((T)0.5, P1[f]), add(FS[f + 1], FS[f]));
+        P1[f] = r;
+        if (q >= 2)
+            p1[(unsigned int)x * (unsigned int)(d1 - 1) + (unsigned int)y] = r;
+    }
+    for (int k = tid; k < R * (S + 1); k += kThreads) {         // p2: tile rows, x0-1 .. x0+S-1
+        const int c = 1 + k / R, q = 2 + k % R;
+        const int f = c * FR + q;
+        const int y = y0 - 2 + q, x = x0 - 2 + c;
+        if (x < 0 || x + 1 >= d2 || y >= d1)
+            continue;
+        const T r = mul(mul((T)0.5, P2[f]), add(FS[f + FR], FS[f]));
+        P2[f] = r;
+        if (c >= 2)
+            p2[(unsigned int)x * (unsigned int)d1 + (unsigned int)y] = r;
+    }
+    __syncthreads();
+    // k5: the tile's divergence; g keeps the factor, as k3 leaves it
+    T *divp = A.div + (long long)i * A.n;
+    T *gw = A.g + (long long)i * A.n;
+    for (int k = tid; k < R * S; k += kThreads) {
+        const int c = 2 + k / R, q = 2 + k % R;
+        const int f = c * FR + q;
+        const int y = y0 - 2 + q, x = x0 - 2 + c;
+        if (y >= d1 || x >= d2)
+            continue;
+        T d = (y + 1 < d1) ? P1[f] : (T)0;
+        if (y >= 1)
+            d = sub(d, P1[f - 1]);
+        if (x + 1 < d2)
+            d = add(d, P2[f]);
+        if (x >= 1)
+            d = sub(d, P2[f - FR]);
+        const unsigned int cell = (unsigned int)x * (unsigned int)d1 + (unsigned int)y;
+        divp[cell] = d;
+        gw[cell] = FS[f];
+    }
+}
+
 int h_grid(long long n, int sms)
 {
     long long b = (n + kThreads - 1) / kThreads;
@@ -659,6 +790,16 @@ int h_grid(long long n, int sms)
 template <class T>
 void spatial_passes(const HArgs<T> &A, int gn, cudaStream_t st, bool dirs)
 {
+    if (A.dim == 2 && !dirs && A.m > 1) {
+        // 32 x 32 tiles in float, 16 x 32 in double: the frame stays within
+        // the default 48 KB of dynamic shared memory
+        constexpr int R = sizeof(T) == 8 ? 16 : 32, S = 32;
+        using Q = SpatialTile<T, R, S>;
+        static_assert(Q::smem_bytes() <= 48 * 1024, "frame above the default shared memory");
+        const int ty = (A.d1 + R - 1) / R, tx = (A.d2 + S - 1) / S;
+        k_spatial_tile2d<T, R, S><<<dim3(ty * tx, A.m - 1), kThreads, Q::smem_bytes(), st>>>(A, ty);
+        return;
+    }
     k2_gradient<T><<<gn, kThreads, 0, st>>>(A);
     if (dirs) {
         k_exempt_a<T><<<gn, kThreads, 0, st>>>(A);
