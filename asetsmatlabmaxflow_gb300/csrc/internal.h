@@ -32,6 +32,9 @@ struct StencilVariant {
     int ct_box_rows = 0;     // rows of the Ct box of the one-pass multi-label kernel (0: none)
     int s_tile = 0;          // stream columns of a square-tile kernel's tile (0: a sweep)
     int persistent = 0;      // 1: every iteration in one cooperative launch, one block per tile
+    // dynamic shared memory of a launch: smem_bytes + smem_per_fl x flow
+    // labels + smem_per_l x labels (label counts known only at run time)
+    int smem_per_fl = 0, smem_per_l = 0;
 };
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,

@@ -402,19 +402,32 @@ static std::vector<const StencilVariant *> solver_candidates(const asets_solver 
     return c;
 }
 
+// Dynamic shared memory of a launch of variant v for the solver's label counts.
+static int launch_smem(const asets_solver *s, const StencilVariant *v)
+{
+    return v->smem_bytes + v->smem_per_fl * s->flow_labels + v->smem_per_l * s->nlab;
+}
+
+// The function attribute covers every label count (8 flow labels, 9
+// labels), so that solvers of different label counts can share a variant.
+static int attr_smem(const StencilVariant *v)
+{
+    return v->smem_bytes + v->smem_per_fl * 8 + v->smem_per_l * 9;
+}
+
 // Whether a whole-solve cooperative variant can hold every tile of the
 // solver's problem resident at once (one block per tile).
 static bool persistent_fits(const asets_solver *s, const StencilVariant *v)
 {
     const long long tiles = (long long)((s->nr + v->tr - 1) / v->tr) * ((s->ns + v->s_tile - 1) / v->s_tile);
-    if (cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, v->smem_bytes) !=
+    const int smem = launch_smem(s, v);
+    if (cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, attr_smem(v)) !=
         cudaSuccess) {
         cudaGetLastError();
         return false;
     }
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, v->nt, v->smem_bytes) !=
-        cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, v->nt, smem) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
@@ -436,8 +449,7 @@ static const StencilVariant *pick_variant(const asets_solver *s, int exact, int 
     // update, one label warp, two), then 16 x 16 tiles (one launch per
     // iteration, the whole solve in one).  By default they run where they
     // measured faster than the two-pass form on a GB300: the whole-solve
-    // tiles on small images whose tiles all fit at once, up to five flow
-    // labels (the tile runs its labels one after another); the sweeps on two
+    // tiles on small images whose tiles all fit at once; the sweeps on two
     // million pixels and more (two label warps for up to three flow labels,
     // one above), and half a million with six flow labels or more (in-step)
     int n_fused = 0;
@@ -446,7 +458,7 @@ static const StencilVariant *pick_variant(const asets_solver *s, int exact, int 
     if (n_fused == 5) {
         const long long px = (long long)s->nr * s->ns;
         const int fl = s->flow_labels;
-        if (px <= kTileLabelsMaxPx && fl <= 5 && persistent_fits(s, match[4]))
+        if (px <= kTileLabelsMaxPx && persistent_fits(s, match[4]))
             return match[4];
         if (px >= 2000000)
             return match[fl <= 3 ? 2 : 1];
@@ -568,10 +580,10 @@ static asets_status setup_kernel(asets_solver *s, int exact, int tile_config, bo
     if (r)
         return fail(ASETS_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", r);
 
-    CU_TRY(cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                v->smem_bytes));
+    const int smem = launch_smem(s, v);
+    CU_TRY(cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, attr_smem(v)));
     int per_sm = 0;
-    CU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, v->nt, v->smem_bytes));
+    CU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, v->nt, smem));
     if (per_sm < 1)
         return fail(ASETS_ERR_UNSUPPORTED, "stencil kernel does not fit on an SM");
     const long long slots = (long long)s->ctx->num_sms * per_sm;
@@ -957,7 +969,7 @@ static cudaError_t launch_stencil(asets_solver *s)
 {
     const StencilVariant *v = s->variant;
     void *params[] = {&s->bargs};
-    return cudaLaunchKernel(v->fn, dim3(s->grid), dim3(v->nt), params, v->smem_bytes,
+    return cudaLaunchKernel(v->fn, dim3(s->grid), dim3(v->nt), params, launch_smem(s, v),
                             s->ctx->stream);
 }
 
@@ -1081,7 +1093,7 @@ static cudaError_t launch_persistent(asets_solver *s)
 {
     const StencilVariant *v = s->variant;
     void *params[] = {&s->bargs};
-    return cudaLaunchCooperativeKernel(v->fn, dim3(s->grid), dim3(v->nt), params, v->smem_bytes,
+    return cudaLaunchCooperativeKernel(v->fn, dim3(s->grid), dim3(v->nt), params, launch_smem(s, v),
                                        s->ctx->stream);
 }
 

@@ -6,12 +6,15 @@
 // at once (16-byte cp.async copies through L2, zero-filled outside the
 // image: the zero-flux border), then per flow label runs the phases of the
 // binary tile kernel -- gk, b', g2, b'' (stored), the divergence on the tile
-// -- and finally the per-pixel label update over all labels: Potts pt_k,
+// -- in groups of 128 threads, one label per group at a time, each group
+// ordered by its own named barrier -- and finally the per-pixel label update
+// over all labels: Potts pt_k,
 // the source flow ps (terms summed in label order) and the multipliers
 // (maxflow/asetsPotts2D_mex.c:365-434); Ishikawa the ordered sink-flow chain
 // and the multipliers (maxflow/asetsIshikawa2D_mex.c:392-482).  The label
-// count is a run-time value (ProblemDesc::nlab_items flow labels), the
-// shared frame sized for the largest.  Every value is the two-pass form's
+// count is a run-time value (ProblemDesc::nlab_items flow labels); the
+// shared memory of a launch is sized for its label count
+// (LTileGeom::smem_bytes).  Every value is the two-pass form's
 // float expression in the same order: EXACT results are bit-identical.
 // Like the binary tile kernel it runs one launch per iteration or the whole
 // solve in one cooperative launch (one block per tile, grid barrier between
@@ -30,16 +33,36 @@ struct LTileGeom {
     static constexpr int RO = 2;              // frame row of pixel row r0-2
     static constexpr int FC = S + 5;          // frame columns s0-2 .. s0+S+2
     static constexpr int F = FR * FC;         // floats per frame (a multiple of 4)
+    static constexpr int GROUPS = 4;          // label groups of 128 threads (group_sync)
+    static constexpr int NT = 128 * GROUPS;
     static constexpr int FLMAX = 8;           // flow labels
     static constexpr int LMAX = (MODEL == 1) ? 8 : 9;
     // frames: BR, BS, U, AL per flow label, PT per label, PS (Potts), then
-    // GK, BR1, BS1, G2; then DV per flow label and CT per label on the tile
-    static constexpr int frames(int fl, int l) { return 4 * fl + l + (MODEL == 1 ? 1 : 0) + 4; }
-    static constexpr int smem_bytes()
+    // GK, BR1, BS1, G2 per group; then DV per flow label and CT per label on
+    // the tile
+    static constexpr int frames(int fl, int l) { return 4 * fl + l + (MODEL == 1 ? 1 : 0) + 4 * GROUPS; }
+    // shared memory of a launch for fl flow labels and l labels: a base and
+    // a share per flow label and per label (the runtime sizes launches so)
+    static constexpr int smem_base() { return ((MODEL == 1 ? 1 : 0) + 4 * GROUPS) * F * 4 + 16; }
+    static constexpr int smem_per_fl() { return (4 * F + R * S) * 4; }
+    static constexpr int smem_per_l() { return (F + R * S) * 4; }
+    static constexpr int smem_bytes(int fl, int l)
     {
-        return (frames(FLMAX, LMAX) * F + (FLMAX + LMAX) * R * S) * 4 + 16;
+        return smem_base() + fl * smem_per_fl() + l * smem_per_l();
     }
 };
+
+// barrier of one 128-thread label group (ids 1..4; 0 is __syncthreads).
+// Immediate ids: a register id would reserve all sixteen barriers.
+__device__ __forceinline__ void group_sync(int g)
+{
+    switch (g) {
+    case 0: asm volatile("bar.sync 1, 128;" ::: "memory"); break;
+    case 1: asm volatile("bar.sync 2, 128;" ::: "memory"); break;
+    case 2: asm volatile("bar.sync 3, 128;" ::: "memory"); break;
+    default: asm volatile("bar.sync 4, 128;" ::: "memory"); break;
+    }
+}
 
 // 16-byte asynchronous copy global -> shared through L2; `bytes` < 16
 // zero-fills the rest (0: the whole chunk)
@@ -71,8 +94,8 @@ __device__ __forceinline__ float ltile_iteration(const ProblemDesc &P, int par, 
     float *BRf = sm, *BSf = BRf + FL * F, *Uf = BSf + FL * F, *ALf = Uf + FL * F;
     float *PTf = ALf + FL * F;
     float *PSf = PTf + L * F;                                   // Potts only
-    float *GK = PSf + (MODEL == 1 ? F : 0), *BR1 = GK + F, *BS1 = BR1 + F, *G2 = BS1 + F;
-    float *DV = G2 + F, *CT = DV + FL * R * S;
+    float *Wk = PSf + (MODEL == 1 ? F : 0);                     // per group: GK, BR1, BS1, G2
+    float *DV = Wk + 4 * G::GROUPS * F, *CT = DV + FL * R * S;
     // old state (the other parity), and the new
     const float *src_br = P.dst_b[par ^ 1][SL_BR], *src_bs = P.dst_b[par ^ 1][SL_BS];
     const float *src_u = P.dst_s[par ^ 1][2];
@@ -122,13 +145,18 @@ __device__ __forceinline__ float ltile_iteration(const ProblemDesc &P, int par, 
         __syncthreads();
     }
 
-    // ---- per flow label: gk, b', g2, b'' (stored), the divergence on the tile
-    for (int k = 0; k < FL; ++k) {
+    // ---- per flow label: gk, b', g2, b'' (stored), the divergence on the
+    // tile; group gi takes labels gi, gi + GROUPS, ... with its own work
+    // frames and barrier
+    static_assert(NT == G::NT, "four label groups of 128 threads");
+    const int gi = tid >> 7, gt = tid & 127;
+    float *GK = Wk + gi * 4 * F, *BR1 = GK + F, *BS1 = BR1 + F, *G2 = BS1 + F;
+    for (int k = gi; k < FL; k += G::GROUPS) {
         float *BR = BRf + k * F, *BS = BSf + k * F;
         const float *U = Uf + k * F, *AL = ALf + k * F;
         const float *S0 = (MODEL == 1) ? PSf : PTf + k * F;         // ps, or pt_k
         const float *S1 = (MODEL == 1) ? PTf + k * F : PTf + (k + 1) * F;  // pt_k, or pt_{k+1}
-        for (int i = tid; i < (R + 4) * (S + 4); i += NT) {
+        for (int i = gt; i < (R + 4) * (S + 4); i += 128) {
             const int c = i / (R + 4), q = i - c * (R + 4);
             const int f = c * FR + RO + q;
             float d = BR[f + 1] - BR[f];
@@ -136,8 +164,8 @@ __device__ __forceinline__ float ltile_iteration(const ProblemDesc &P, int par, 
             d = d - BS[f];
             GK[f] = d - ((S0[f] - S1[f]) + div_cc<EXACT>(U[f], cc, inv_cc));
         }
-        __syncthreads();
-        for (int i = tid; i < (R + 3) * (S + 2); i += NT) {
+        group_sync(gi);
+        for (int i = gt; i < (R + 3) * (S + 2); i += 128) {
             const int c = 1 + i / (R + 3), q = 1 + i % (R + 3);
             const int f = c * FR + RO + q;
             const int r = r0 - 2 + q, s = s0 - 2 + c;
@@ -145,7 +173,7 @@ __device__ __forceinline__ float ltile_iteration(const ProblemDesc &P, int par, 
             BR1[f] = keep_if<EXACT>(steps * (GK[f] - GK[f - 1]) + BR[f], fr_ok && s_in,
                                     fr_ok ? 1.f : 0.f);
         }
-        for (int i = tid; i < (R + 2) * (S + 3); i += NT) {
+        for (int i = gt; i < (R + 2) * (S + 3); i += 128) {
             const int c = 1 + i / (R + 2), q = 1 + i % (R + 2);
             const int f = c * FR + RO + q;
             const int r = r0 - 2 + q, s = s0 - 2 + c;
@@ -153,15 +181,15 @@ __device__ __forceinline__ float ltile_iteration(const ProblemDesc &P, int par, 
             BS1[f] = keep_if<EXACT>(steps * (GK[f] - GK[f - FR]) + BS[f], inplane && sb_in,
                                     sb_in ? 1.f : 0.f);
         }
-        __syncthreads();
-        for (int i = tid; i < (R + 2) * (S + 2); i += NT) {
+        group_sync(gi);
+        for (int i = gt; i < (R + 2) * (S + 2); i += 128) {
             const int c = 1 + i / (R + 2), q = 1 + i % (R + 2);
             const int f = c * FR + RO + q;
             G2[f] = Proj<EXACT>::gk(BS1[f + FR], BS1[f], BR1[f + 1], BR1[f], AL[f]);
         }
-        __syncthreads();
+        group_sync(gi);
         const unsigned int lo = (unsigned int)k * lst;
-        for (int i = tid; i < (R + 1) * S; i += NT) {
+        for (int i = gt; i < (R + 1) * S; i += 128) {
             const int c = 2 + i / (R + 1), q = 2 + i % (R + 1);
             const int f = c * FR + RO + q;
             const int r = r0 - 2 + q, s = s0 - 2 + c;
@@ -172,7 +200,7 @@ __device__ __forceinline__ float ltile_iteration(const ProblemDesc &P, int par, 
             if (q < R + 2 && r < nr && s < ns)
                 d_br[lo + (unsigned int)s * pitch + (unsigned int)r] = v;
         }
-        for (int i = tid; i < R * (S + 1); i += NT) {
+        for (int i = gt; i < R * (S + 1); i += 128) {
             const int c = 2 + i / R, q = 2 + i % R;
             const int f = c * FR + RO + q;
             const int r = r0 - 2 + q, s = s0 - 2 + c;
@@ -183,8 +211,8 @@ __device__ __forceinline__ float ltile_iteration(const ProblemDesc &P, int par, 
             if (c < S + 2 && r < nr && s < ns)
                 d_bs[lo + (unsigned int)s * pitch + (unsigned int)r] = v;
         }
-        __syncthreads();
-        for (int i = tid; i < R * S; i += NT) {
+        group_sync(gi);
+        for (int i = gt; i < R * S; i += 128) {
             const int c = 2 + i / R, q = 2 + i % R;
             const int f = c * FR + RO + q;
             float dv = BR[f + 1] - BR[f];
@@ -192,10 +220,9 @@ __device__ __forceinline__ float ltile_iteration(const ProblemDesc &P, int par, 
             dv = dv - BS[f];
             DV[k * R * S + i] = dv;
         }
-        // the next label's phases write only GK, BR1, BS1, G2 and its own
-        // frames; this label's divergence reads its BR, BS
+        group_sync(gi);  // the group's work frames are reused by its next label
     }
-    __syncthreads();
+    __syncthreads();  // every label's divergence
 
     // ---- the label update of the tile's pixels
     float erru = 0.0f;
@@ -268,7 +295,7 @@ __device__ __forceinline__ float ltile_iteration(const ProblemDesc &P, int par, 
 }
 
 template <int MODEL, int NT, bool EXACT>
-__global__ void __launch_bounds__(NT) stencil2d_tile_labels_kernel(const __grid_constant__ BatchArgs B)
+__global__ void __launch_bounds__(NT, 2) stencil2d_tile_labels_kernel(const __grid_constant__ BatchArgs B)
 {
     extern __shared__ __align__(16) float fsm[];
     __shared__ double s_red[NT / 32];
@@ -313,7 +340,7 @@ __global__ void __launch_bounds__(NT) stencil2d_tile_labels_kernel(const __grid_
 
 // The whole solve in one cooperative launch, as stencil2d_tile_persistent_kernel.
 template <int MODEL, int NT, bool EXACT>
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, 2)
     stencil2d_tile_labels_persistent_kernel(const __grid_constant__ BatchArgs B)
 {
     extern __shared__ __align__(16) float fsm[];

@@ -87,14 +87,15 @@ StencilVariant make_variant_tile()
 }
 
 // The multi-label 2D 16 x 16 tile kernels (stencil2d_tile_labels.cuh) for
-// MODEL (1 Potts, 2 Ishikawa), any label count up to 8 flow labels; one
-// launch per iteration, or (PERSISTENT) the whole solve in one cooperative
-// launch.  pt/u/ps ping-pong as in the one-pass sweep kernels.
+// MODEL (1 Potts, 2 Ishikawa), any label count up to 8 flow labels, four
+// label groups of 128 threads; one launch per iteration, or (PERSISTENT) the
+// whole solve in one cooperative launch.  pt/u/ps ping-pong as in the
+// one-pass sweep kernels; shared memory sized per launch by label count.
 template <int MODEL, bool EXACT, bool PERSISTENT>
 StencilVariant make_variant_tile_labels()
 {
     using G = LTileGeom<MODEL>;
-    constexpr int NT = 128;
+    constexpr int NT = G::NT;
     StencilVariant v;
     v.dim = 2;
     v.epi = EPI_FUSED;
@@ -103,7 +104,9 @@ StencilVariant make_variant_tile_labels()
     v.tc = 1;
     v.nt = NT;
     v.nstage = 0;
-    v.smem_bytes = G::smem_bytes();
+    v.smem_bytes = G::smem_base();
+    v.smem_per_fl = G::smem_per_fl();
+    v.smem_per_l = G::smem_per_l();
     v.box_rows = G::R + 8;    // unused maps, encoded like the sweep's
     v.box_cols = 1;
     v.box_cols_bc = 1;
