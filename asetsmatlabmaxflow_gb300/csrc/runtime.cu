@@ -415,27 +415,42 @@ static int attr_smem(const StencilVariant *v)
     return v->smem_bytes + v->smem_per_fl * 8 + v->smem_per_l * 9;
 }
 
-// Whether a whole-solve cooperative variant can hold every tile of the
-// solver's problem resident at once (one block per tile).
-static bool persistent_fits(const asets_solver *s, const StencilVariant *v)
+// Blocks of a whole-solve cooperative launch of variant v that can be
+// resident at once (0: it does not fit on an SM).
+static long long persistent_slots(const asets_solver *s, const StencilVariant *v)
 {
-    const long long tiles = (long long)((s->nr + v->tr - 1) / v->tr) * ((s->ns + v->s_tile - 1) / v->s_tile);
     const int smem = launch_smem(s, v);
     if (cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, attr_smem(v)) !=
         cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return 0;
     }
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v->fn, v->nt, smem) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return 0;
     }
-    return tiles <= (long long)per_sm * s->ctx->num_sms;
+    return (long long)per_sm * s->ctx->num_sms;
+}
+
+// Tiles of the solver's problem per resident block in a whole-solve launch
+// of v (0: not launchable).
+static double persistent_load(const asets_solver *s, const StencilVariant *v)
+{
+    const long long slots = persistent_slots(s, v);
+    if (slots < 1)
+        return 0.0;
+    const long long tiles = (long long)((s->nr + v->tr - 1) / v->tr) * ((s->ns + v->s_tile - 1) / v->s_tile);
+    return (double)tiles / (double)slots;
 }
 
 // Largest multi-label 2D image (pixels) the whole-solve tile kernel takes by default.
 static constexpr long long kTileLabelsMaxPx = 1LL << 17;
+// Most 32 x 32 tiles per resident block the binary whole-solve kernel takes
+// by default: fast, every tile resident at once (beyond that the
+// two-iteration sweep wins); EXACT, up to eight (about 1600^2 pixels: the
+// EXACT sweep runs one iteration per pass)
+static constexpr double kTileBinaryMaxLoad = 1.0, kTileBinaryMaxLoadExact = 8.0;
 
 static const StencilVariant *pick_variant(const asets_solver *s, int exact, int tile_config,
                                           bool single)
@@ -458,7 +473,8 @@ static const StencilVariant *pick_variant(const asets_solver *s, int exact, int 
     if (n_fused == 5) {
         const long long px = (long long)s->nr * s->ns;
         const int fl = s->flow_labels;
-        if (px <= kTileLabelsMaxPx && persistent_fits(s, match[4]))
+        const double load = persistent_load(s, match[4]);
+        if (px <= kTileLabelsMaxPx && load > 0.0 && load <= 1.0)
             return match[4];
         if (px >= 2000000)
             return match[fl <= 3 ? 2 : 1];
@@ -468,15 +484,21 @@ static const StencilVariant *pick_variant(const asets_solver *s, int exact, int 
     match.erase(match.begin(), match.begin() + n_fused);
     // small binary 2D images: the whole solve in one cooperative launch when
     // every tile can be resident (16 x 16 tiles up to 2^17 pixels, else
-    // 32 x 32), measured faster than the sweeps there
+    // 32 x 32; EXACT also with up to eight 32 x 32 tiles per block),
+    // measured faster than the sweeps there
     if (single && s->dim == 2 && s->model == ASETS_BINARY) {
         const long long px = (long long)s->nr * s->ns;
         for (int want : {16, 32}) {
             if (want == 16 && px > (1LL << 17))
                 continue;
             for (auto *v : match)
-                if (v->persistent && v->s_tile == want && persistent_fits(s, v))
-                    return v;
+                if (v->persistent && v->s_tile == want) {
+                    const double load = persistent_load(s, v);
+                    const double most = want == 16 ? 1.0
+                                                   : (exact ? kTileBinaryMaxLoadExact : kTileBinaryMaxLoad);
+                    if (load > 0.0 && load <= most)
+                        return v;
+                }
         }
     }
     for (size_t i = 0; i < match.size();)
@@ -572,8 +594,8 @@ static asets_status setup_kernel(asets_solver *s, int exact, int tile_config, bo
         return fail(ASETS_ERR_UNSUPPORTED, "no kernel variant for this configuration");
     if (s->variant == v)
         return ASETS_OK;
-    if (v->persistent && !persistent_fits(s, v))
-        return fail(ASETS_ERR_UNSUPPORTED, "too many tiles for one cooperative launch");
+    if (v->persistent && persistent_slots(s, v) < 1)
+        return fail(ASETS_ERR_UNSUPPORTED, "whole-solve kernel does not fit on an SM");
     const StencilProblem p = stencil_problem_of(s, v->epi == EPI_FUSED);
     ProblemDesc &A = s->desc;
     int r = build_problem_desc(s->ctx->encode, *v, p, &A);
@@ -621,7 +643,7 @@ static asets_status setup_kernel(asets_solver *s, int exact, int tile_config, bo
     s->bargs.queue = s->d_queue;
     s->bargs.done_count = s->d_queue + 2;
     if (v->persistent)
-        s->grid = items;  // one block per tile, all resident
+        s->grid = (int)std::min<long long>(items, slots);  // all resident, one or more tiles each
     // erriter partials of the label kernels (labelled models)
     const int need = std::max(s->ctx->num_sms * 8, 1024);
     if (need > s->partials_cap) {
@@ -1300,7 +1322,7 @@ static asets_status solver_autotune(asets_solver *s, int flags, float cc, float 
     for (int cand = 1; cand <= n; ++cand) {
         // one chunk of launches: kGraphIters x (iterations per launch) iterations
         const int per_launch = cands[cand - 1]->temporal;
-        if (cands[cand - 1]->persistent && !persistent_fits(s, cands[cand - 1]))
+        if (cands[cand - 1]->persistent && persistent_slots(s, cands[cand - 1]) < 1)
             continue;
         asets_status ss = prepare_run(s, flags, cand, kGraphIters * per_launch, 0.0f, cc, steps);
         if (ss != ASETS_OK)

@@ -16,8 +16,9 @@
 // as 0, the zero-flux border.  Two kernels: one launch per iteration, items
 // handed out by the same queue and closed by the same per-item erriter
 // partials and ticket as the sweeps; or every iteration in one cooperative
-// launch with a grid barrier between iterations, which removes the launch
-// and hand-off latency that dominates an iteration of a small image.
+// launch with a grid barrier between iterations (every block resident, each
+// taking one or more tiles), which removes the launch and hand-off latency
+// that dominates an iteration of a small image.
 #pragma once
 
 #include "stencil2_kernel.cuh"
@@ -249,14 +250,14 @@ __global__ void __launch_bounds__(NT, MINB) stencil2d_tile_kernel(const __grid_c
     }
 }
 
-// Every iteration of one problem in one cooperative launch: block b keeps
-// tile b for the whole solve; after each iteration (`iteration(it)` returns
-// the thread's erriter share) the blocks meet at a grid barrier (an arrival
+// Every iteration of one problem in one cooperative launch: block b takes
+// tiles b, b + grid, ... of every iteration (`iteration(it, tile)` returns
+// the thread's erriter share); after each iteration the blocks meet at a grid barrier (an arrival
 // counter, zeroed before the launch; each wait bounded by time, a timeout
 // sets DEV_ERR_TIMEOUT and ends the solve), then every block sums the
-// tiles' erriter partials in the order finish_item uses, so all take the
-// same stopping decision; block 0 records cvg, itNum and the control block
-// as finish_item does.  The launch and per-iteration hand-off of the
+// blocks' erriter partials in the order finish_item uses for items, so all
+// take the same stopping decision; block 0 records cvg, itNum and the
+// control block as finish_item does.  The launch and per-iteration hand-off of the
 // one-launch-per-iteration form (queue, ticket, kernel boundary) is replaced
 // by one barrier.  Partials alternate between two halves of item_partials by
 // iteration parity.
@@ -266,7 +267,7 @@ __device__ __forceinline__ void tile_solve_loop(const ProblemDesc &P, unsigned i
 {
     const int tid = threadIdx.x;
     IterControl *ctl = P.ctl;
-    const int nb = (int)gridDim.x;   // one block per tile
+    const int nb = (int)gridDim.x;   // at most one block per tile
     const int li = (int)blockIdx.x;
     if (*(volatile int *)&ctl->done)
         return;
@@ -275,7 +276,9 @@ __device__ __forceinline__ void tile_solve_loop(const ProblemDesc &P, unsigned i
     const int break_lt = ctl->break_lt;
     const float err_bound = ctl->err_bound, denom = ctl->denom;
     for (unsigned int gen = 1;; ++gen) {
-        const float erru = iteration(it);
+        float erru = 0.0f;
+        for (int tile = li; tile < P.n_items; tile += nb)
+            erru += iteration(it, tile);
         const double part = block_sum_double<NT>(erru, s_red);
         if (tid == 0) {
             P.item_partials[(it & 1) * nb + li] = part;
@@ -340,8 +343,8 @@ __global__ void __launch_bounds__(NT, MINB)
     __shared__ double s_red[NT / 32];
     __shared__ int s_stop;
     const ProblemDesc &P = B.probs[0];
-    tile_solve_loop<NT>(P, B.queue, s_red, &s_stop, [&](int it) {
-        return tile2_iteration<R, S, NT, EXACT>(P, it & 1, (int)blockIdx.x, fsm);
+    tile_solve_loop<NT>(P, B.queue, s_red, &s_stop, [&](int it, int tile) {
+        return tile2_iteration<R, S, NT, EXACT>(P, it & 1, tile, fsm);
     });
 }
 

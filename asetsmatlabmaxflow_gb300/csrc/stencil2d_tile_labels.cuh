@@ -17,8 +17,9 @@
 // (LTileGeom::smem_bytes).  Every value is the two-pass form's
 // float expression in the same order: EXACT results are bit-identical.
 // Like the binary tile kernel it runs one launch per iteration or the whole
-// solve in one cooperative launch (one block per tile, grid barrier between
-// iterations); new pt, u and ps go to the other parity.
+// solve in one cooperative launch (every block resident, one or more tiles
+// each, a grid barrier between iterations); new pt, u and ps go to the
+// other parity.
 #pragma once
 
 #include "stencil2d_tile.cuh"
@@ -347,8 +348,8 @@ __global__ void __launch_bounds__(NT, 2)
     __shared__ double s_red[NT / 32];
     __shared__ int s_stop;
     const ProblemDesc &P = B.probs[0];
-    tile_solve_loop<NT>(P, B.queue, s_red, &s_stop, [&](int it) {
-        return ltile_iteration<MODEL, NT, EXACT>(P, it & 1, (int)blockIdx.x, fsm);
+    tile_solve_loop<NT>(P, B.queue, s_red, &s_stop, [&](int it, int tile) {
+        return ltile_iteration<MODEL, NT, EXACT>(P, it & 1, tile, fsm);
     });
 }
 

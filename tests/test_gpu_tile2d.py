@@ -7,8 +7,8 @@ sweep variants: 32 x 32, 16 x 16, then the same as whole-solve launches.
 EXACT results must be bit-identical to the oracle and to the sweep kernel
 (u, ps, pt and the spatial flows), the fast build meets the parity bar,
 stopping runs stop where the oracle stops, a batch of small images runs
-the per-iteration form, and a problem with more tiles than can be resident
-is refused by the whole-solve form."""
+the per-iteration form, and the whole-solve form takes several tiles per
+block when they cannot all be resident."""
 import numpy as np
 import pytest
 
@@ -159,33 +159,34 @@ def test_whole_solve_launch_edges(tc):
     s.close()
 
 
-def test_whole_solve_launch_refuses_too_many_tiles():
-    """4096^2 in 16 x 16 tiles is 65,536 blocks: more than can be resident,
-    so the cooperative form reports UNSUPPORTED instead of launching."""
-    from asetsmatlabmaxflow_gb300 import native as N
+@pytest.mark.parametrize("tc", TILE_EXACT[2:])
+def test_whole_solve_launch_with_more_tiles_than_blocks(tc):
+    """1024 x 1000 in 16 x 16 or 32 x 32 tiles is more tiles than can be
+    resident at once: each block takes several per iteration, with the same
+    EXACT result as the sweep, in one launch."""
+    dims = (1024, 1000)
+    inp = _inputs(dims, 43)
+    t = _solve(dims, inp, 11, 0.0, True, tc)
+    w = _solve(dims, inp, 11, 0.0, True, SWEEP)
+    assert t["it"] == w["it"] == 11
+    for k in ("u", "ps", "pt", "bx", "by"):
+        np.testing.assert_array_equal(bits(t[k]), bits(w[k]), err_msg=k)
+    np.testing.assert_allclose(t["cvg"], w["cvg"], rtol=2e-5, atol=1e-12)
 
-    dims = (4096, 4096)
-    g = np.random.default_rng(41)
-    cs, ct = (np.asfortranarray(g.random(dims, dtype=np.float32)) for _ in range(2))
-    s = N.Solver(N.Context.default(), "binary", dims)
-    s.set_inputs(ct, np.full(dims, 0.5, np.float32, order="F"), cs)
-    with pytest.raises(N.AsetsError, match="too many tiles"):
-        s.run(4, 0.0, 0.3, 0.16, tile_config=TILE_FAST[3])
-    assert s.run(4, 0.0, 0.3, 0.16) == 4  # the default still solves it
-    s.close()
 
-
-@pytest.mark.parametrize("dims,launches", [((256, 256), 1), ((301, 170), 1), ((512, 512), 1),
-                                           ((1024, 1024), 16)])
-def test_default_whole_solve_on_small_images(dims, launches):
+@pytest.mark.parametrize("dims,exact,launches", [
+    ((256, 256), False, 1), ((301, 170), False, 1), ((512, 512), False, 1), ((1024, 1024), False, 16),
+    ((1024, 1024), True, 1), ((2048, 2048), True, 32)])
+def test_default_whole_solve_on_small_images(dims, exact, launches):
     """Without a tile_config a binary 2D image whose tiles can all be
-    resident runs as one cooperative launch; a larger one keeps the sweep
-    (16 iterations per CUDA-graph chunk, two per launch)."""
+    resident runs as one cooperative launch (EXACT: up to eight tiles per
+    block); a larger one keeps the sweep (16 iterations per CUDA-graph
+    chunk: fast two per launch, EXACT one)."""
     from asetsmatlabmaxflow_gb300 import native as N
 
     inp = _inputs(dims, 42)
     s = N.Solver(N.Context.default(), "binary", dims)
     s.set_inputs(inp["Ct"], inp["alpha"], inp["Cs"])
-    assert s.run(20, 0.0, 0.3, 0.16) == 20
+    assert s.run(20, 0.0, 0.3, 0.16, exact=exact) == 20
     assert s.last_run_stats()[1] == launches
     s.close()
