@@ -464,7 +464,8 @@ static const StencilVariant *pick_variant(const asets_solver *s, int exact, int 
     // update, one label warp, two), then 16 x 16 tiles (one launch per
     // iteration, the whole solve in one).  By default they run where they
     // measured faster than the two-pass form on a GB300: the whole-solve
-    // tiles on small images whose tiles all fit at once; the sweeps on two
+    // tiles on images of up to 2^17 pixels (two tiles per block at most);
+    // the sweeps on two
     // million pixels and more (two label warps for up to three flow labels,
     // one above), and half a million with six flow labels or more (in-step)
     int n_fused = 0;
@@ -474,7 +475,7 @@ static const StencilVariant *pick_variant(const asets_solver *s, int exact, int 
         const long long px = (long long)s->nr * s->ns;
         const int fl = s->flow_labels;
         const double load = persistent_load(s, match[4]);
-        if (px <= kTileLabelsMaxPx && load > 0.0 && load <= 1.0)
+        if (px <= kTileLabelsMaxPx && load > 0.0 && load <= 2.0)
             return match[4];
         if (px >= 2000000)
             return match[fl <= 3 ? 2 : 1];

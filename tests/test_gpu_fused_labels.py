@@ -120,14 +120,14 @@ def test_fused_stops_where_the_oracle_stops(model, L, exact, tc):
     ("potts", (2048, 1024), 4, 16), ("ishikawa", (1024, 1024), 8, 16),
     ("ishikawa", (1024, 1024), 3, 32), ("potts", (512, 512), 8, 32),
     ("potts", (256, 256), 4, 1), ("ishikawa", (200, 150), 6, 1), ("ishikawa", (128, 128), 8, 1),
-    ("potts", (256, 256), 8, 32)])
+    ("potts", (256, 256), 8, 1), ("potts", (512, 512), 4, 32)])
 def test_default_form_by_size(model, dims, L, launches):
     """Without a tile_config the one-pass sweep kernel runs on two million
     pixels and more, and on half a million with six flow labels or more (one
-    launch per iteration, one chunk of 16); small images whose tiles all fit
-    at once run the whole solve in one cooperative launch (Potts 256^2 with
-    eight labels does not fit); the rest the two-pass form (two launches
-    per iteration)."""
+    launch per iteration, one chunk of 16); images of up to 2^17 pixels run
+    the whole solve in one cooperative launch (Potts 256^2 with eight labels
+    two tiles per block); the rest the two-pass form (two launches per
+    iteration)."""
     from asetsmatlabmaxflow_gb300 import native as N
 
     ct, alpha = _inputs(model, dims, L, 16)
