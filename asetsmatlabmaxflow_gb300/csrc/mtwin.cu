@@ -18,6 +18,9 @@
 //   3 face flows *= 0.5 (gk + gk of the cell below)
 //   4 per cell: divp of every label, then the model's sink/source flows and
 //     multipliers, and erriter; the last block records erriter and the break.
+// In double precision, where the FP64 pipe bounds the passes, u/cc (the
+// same quotient in passes 0 and 4 of an iteration, twice in 4 for Ishikawa)
+// is divided once, where u is written, and kept beside u.
 #include <chrono>
 #include <cstring>
 #include <string>
@@ -46,7 +49,7 @@ struct MTArgs {
     long long n, f1, f2, f3;  // cells and faces per flow label
     T cc, steps, half, one_over_cc, one_over_ccl, beta;
     const T *cs, *ct, *alpha;
-    T *u, *pt, *ps, *divp, *gk, *p1, *p2, *p3;
+    T *u, *ucc, *pt, *ps, *divp, *gk, *p1, *p2, *p3;
     double *partials;
     T *erriter;
     MTCtl *ctl;
@@ -67,6 +70,23 @@ template <> __device__ __forceinline__ double sub(double a, double b) { return _
 template <> __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
 template <> __device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
 template <> __device__ __forceinline__ double sqr(double a) { return __dsqrt_rn(a); }
+
+// u/cc of element o: kept beside u in double precision, divided here in single
+template <class T>
+__device__ __forceinline__ T u_cc(const MTArgs<T> &A, long long o)
+{
+    if constexpr (sizeof(T) == 8)
+        return A.ucc[o];
+    else
+        return dvd(A.u[o], A.cc);
+}
+template <class T>
+__device__ __forceinline__ void set_u(const MTArgs<T> &A, long long o, T v)
+{
+    A.u[o] = v;
+    if constexpr (sizeof(T) == 8)
+        A.ucc[o] = dvd(v, A.cc);
+}
 
 // Matlab's min(a, b) for ordered values; a NaN a is kept (as the restatement)
 template <class T>
@@ -142,7 +162,7 @@ __device__ __forceinline__ T ud(const MTArgs<T> &A, int k, long long g)
         a = A.pt[o];
         b = A.pt[o + A.n];
     }
-    return sub(A.divp[o], add(sub(a, b), dvd(A.u[o], A.cc)));
+    return sub(A.divp[o], add(sub(a, b), u_cc(A, o)));
 }
 
 // ud of every flow label and cell, into the gk buffer (free until mt_gk):
@@ -208,8 +228,8 @@ __global__ void mt_gk(const MTArgs<T> A)
         }
         const T g = sqr(mul(s, A.half));
         const T al = A.alpha[t];
-        const T r = (g <= al) ? (T)1 : dvd(g, al);
-        A.gk[t] = dvd((T)1, r);
+        // 1/max(1, g/al); 1/1 is exactly 1, so no division below alpha
+        A.gk[t] = (g <= al) ? (T)1 : dvd((T)1, dvd(g, al));
     }
 }
 
@@ -264,20 +284,20 @@ __global__ void mt_cell(const MTArgs<T> A)
         for (int k = 0; k < A.nflow; ++k)
             A.divp[(long long)k * n + g] = divergence<T, D>(A, k, c);
         if (M == MT_BINARY) {
-            const T dv = A.divp[g], u = A.u[g], uc = dvd(u, A.cc);
+            const T dv = A.divp[g], u = A.u[g], uc = u_cc(A, g);
             const T ps = mn(add(sub(add(dv, A.pt[g]), uc), A.one_over_cc), A.cs[g]);
             const T pt = mn(add(add(-dv, ps), uc), A.ct[g]);
             const T e = mul(A.cc, sub(add(dv, pt), ps));
             A.ps[g] = ps;
             A.pt[g] = pt;
-            A.u[g] = sub(u, e);
+            set_u(A, g, sub(u, e));
             err += fabs((double)e);
         } else if (M == MT_POTTS) {
             const T ps = A.ps[g];
             T pd = (T)0;
             for (int k = 0; k < A.nlab; ++k) {
                 const long long o = (long long)k * n + g;
-                const T dv = A.divp[o], uc = dvd(A.u[o], A.cc);
+                const T dv = A.divp[o], uc = u_cc(A, o);
                 const T pt = mn(add(add(-dv, ps), uc), A.ct[o]);
                 A.pt[o] = pt;
                 pd = add(pd, sub(add(dv, pt), uc));
@@ -287,7 +307,7 @@ __global__ void mt_cell(const MTArgs<T> A)
             for (int k = 0; k < A.nlab; ++k) {
                 const long long o = (long long)k * n + g;
                 const T e = mul(A.cc, sub(add(A.divp[o], A.pt[o]), psn));
-                A.u[o] = sub(A.u[o], e);
+                set_u(A, o, sub(A.u[o], e));
                 err += fabs((double)e);
             }
         } else {
@@ -296,12 +316,12 @@ __global__ void mt_cell(const MTArgs<T> A)
                 const long long o = (long long)k * n + g;
                 T v;
                 if (k == 0) {
-                    v = add(sub(add(A.divp[g], A.pt[g + n]), dvd(A.u[g], A.cc)), A.one_over_cc);
+                    v = add(sub(add(A.divp[g], A.pt[g + n]), u_cc(A, g)), A.one_over_cc);
                 } else {
                     const long long ob = o - n;  // label k-1: its pt is the new one
-                    v = add(add(-A.divp[ob], A.pt[ob]), dvd(A.u[ob], A.cc));
+                    v = add(add(-A.divp[ob], A.pt[ob]), u_cc(A, ob));
                     if (k < L - 1) {
-                        v = sub(add(add(v, A.divp[o]), A.pt[o + n]), dvd(A.u[o], A.cc));
+                        v = sub(add(add(v, A.divp[o]), A.pt[o + n]), u_cc(A, o));
                         v = dvd(v, (T)2);
                     }
                 }
@@ -310,7 +330,7 @@ __global__ void mt_cell(const MTArgs<T> A)
             for (int k = 0; k < L - 1; ++k) {
                 const long long o = (long long)k * n + g;
                 const T e = mul(A.cc, sub(add(A.divp[o], A.pt[o + n]), A.pt[o]));
-                A.u[o] = sub(A.u[o], e);
+                set_u(A, o, sub(A.u[o], e));
                 err += fabs((double)e);
             }
         }
@@ -358,7 +378,7 @@ __global__ void mt_init(const MTArgs<T> A)
         const long long g = t, n = A.n;
         if (M == MT_BINARY) {
             const T cs = A.cs[g], ct = A.ct[g];
-            A.u[g] = (sub(cs, ct) >= (T)0) ? (T)1 : (T)0;
+            set_u(A, g, (sub(cs, ct) >= (T)0) ? (T)1 : (T)0);
             const T ps = mn(cs, ct);
             A.ps[g] = ps;
             A.pt[g] = ps;
@@ -379,10 +399,10 @@ __global__ void mt_init(const MTArgs<T> A)
         if (M == MT_POTTS) {
             A.ps[g] = m;
             for (int k = 0; k < A.nlab; ++k)
-                A.u[(long long)k * n + g] = (I == k) ? (T)1 : (T)0;
+                set_u(A, (long long)k * n + g, (I == k) ? (T)1 : (T)0);
         } else {
             for (int k = 0; k < A.nlab - 1; ++k)  // u(:,:,k) = init > k, 1-based
-                A.u[(long long)k * n + g] = (I > k) ? (T)1 : (T)0;
+                set_u(A, (long long)k * n + g, (I > k) ? (T)1 : (T)0);
         }
     }
 }
@@ -435,7 +455,7 @@ asets_status mt_run(asets_context *ctx, int rows, int cols, int slices, int nlab
     asets_status status = ASETS_OK;
     const int grid = mt_grid(n * A.nflow, sms), gcell = mt_grid(n, sms);
     bool ok = get(&ct, n * nct) && get(&al, n * A.nflow) && get(&A.u, n * nu) &&
-              get(&A.pt, n * npt) && get(&A.ps, n) && get(&A.divp, n * A.nflow) &&
+              (sizeof(T) != 8 || get(&A.ucc, n * nu)) && get(&A.pt, n * npt) && get(&A.ps, n) && get(&A.divp, n * A.nflow) &&
               get(&A.gk, n * A.nflow) && get(&A.p1, A.f1 * A.nflow) && get(&A.p2, A.f2 * A.nflow) &&
               get(&A.p3, A.f3 * A.nflow) && get(&A.erriter, iterNum) &&
               (M != MT_BINARY || get(&cs, n));

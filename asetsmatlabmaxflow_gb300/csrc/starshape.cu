@@ -10,7 +10,11 @@
 // and gdv = div(v ve) enters the flow balance (:67-97, :141-170).
 //
 // One iteration = six passes over all labels (each recomputes the neighbour
-// values it needs from the state, so every face is written by one thread):
+// values it needs from the state, so every face is written by one thread;
+// u/cc, the same quotient in passes A, D and E of an iteration, is divided
+// once, where u is written, and kept beside u; the ud of pass A is formed
+// per cell at the end of F and the ud of pass E at the end of D, and the
+// gradients read them):
 //   A  gradient step of pp1/pp2 from ud = divp + gdv - (ps - pt + u/cc)
 //   B  projection factor gk = 1/max(1, |p|/alpha) per cell
 //   C  pp1/pp2 *= mean of gk across the face
@@ -44,7 +48,7 @@ struct SSArgs {
     long long N;  // rows * cols
     double cc, steps, stepv, inv_ccl;
     const double *ct, *alpha, *ve1, *ve2, *div_ve;
-    double *u, *pt, *ps, *divp, *pp1, *pp2, *gk, *v, *gdv;
+    double *u, *ucc, *ud, *pt, *ps, *divp, *pp1, *pp2, *gk, *v, *gdv;
     double *partials, *erriter;
     SSCtl *ctl;
 };
@@ -75,22 +79,32 @@ __device__ __forceinline__ double minimum(double a, double b)
 }
 
 // ud of pass A: (divp + gdv) - ((ps - pt) + u/cc)
-__device__ __forceinline__ double ud_a(const SSArgs &A, int k, int y, int x)
+__device__ __forceinline__ double ud_a(double divp, double gdv, double ps, double pt, double ucc)
 {
-    const long long c = cell(A, k, y, x);
-    const long long g = (long long)x * A.rows + y;
-    return __dsub_rn(__dadd_rn(A.divp[c], A.gdv[c]),
-                     __dadd_rn(__dsub_rn(A.ps[g], A.pt[c]), __ddiv_rn(A.u[c], A.cc)));
+    return __dsub_rn(__dadd_rn(divp, gdv), __dadd_rn(__dsub_rn(ps, pt), ucc));
 }
 
 // ud of pass E: ((gdv + divp) + pt) - (ps + u/cc)
-__device__ __forceinline__ double ud_e(const SSArgs &A, int k, int y, int x)
+__device__ __forceinline__ double ud_e(double gdv, double divp, double pt, double ps, double ucc)
 {
-    const long long c = cell(A, k, y, x);
-    const long long g = (long long)x * A.rows + y;
-    return __dsub_rn(__dadd_rn(__dadd_rn(A.gdv[c], A.divp[c]), A.pt[c]),
-                     __dadd_rn(A.ps[g], __ddiv_rn(A.u[c], A.cc)));
+    return __dsub_rn(__dadd_rn(__dadd_rn(gdv, divp), pt), __dadd_rn(ps, ucc));
 }
+
+// (label, row, column) of element t of a label-major loop, in 32-bit
+// arithmetic (every index is below 2^31: entry check)
+struct LabelCell {
+    int k, y, x;
+    long long g;
+    __device__ LabelCell(const SSArgs &A, long long t)
+    {
+        const unsigned int tt = (unsigned int)t, n = (unsigned int)A.N, r = (unsigned int)A.rows;
+        const unsigned int kk = tt / n, gg = tt - kk * n, xx = gg / r;
+        k = (int)kk;
+        g = gg;
+        x = (int)xx;
+        y = (int)(gg - xx * r);
+    }
+};
 
 #define SS_LOOP(total)                                                                 \
     for (long long t = blockIdx.x * (long long)kThreads + threadIdx.x; t < (total);    \
@@ -102,17 +116,16 @@ __global__ void pass_a(const SSArgs A)
         return;
     SS_LOOP(A.N * A.nlab)
     {
-        const int k = (int)(t / A.N);
-        const long long g = t - (long long)k * A.N;
-        const int x = (int)(g / A.rows), y = (int)(g - (long long)x * A.rows);
-        const double ud = ud_a(A, k, y, x);
+        const LabelCell lc(A, t);
+        const int k = lc.k, x = lc.x, y = lc.y;
+        const double ud = A.ud[t];
         if (x >= 1) {
             const long long f = f1(A, k, y, x);
-            A.pp1[f] = __dadd_rn(__dmul_rn(A.steps, __dsub_rn(ud, ud_a(A, k, y, x - 1))), A.pp1[f]);
+            A.pp1[f] = __dadd_rn(__dmul_rn(A.steps, __dsub_rn(ud, A.ud[t - A.rows])), A.pp1[f]);
         }
         if (y >= 1) {
             const long long f = f2(A, k, y, x);
-            A.pp2[f] = __dadd_rn(__dmul_rn(A.steps, __dsub_rn(ud, ud_a(A, k, y - 1, x))), A.pp2[f]);
+            A.pp2[f] = __dadd_rn(__dmul_rn(A.steps, __dsub_rn(ud, A.ud[t - 1])), A.pp2[f]);
         }
     }
 }
@@ -123,9 +136,8 @@ __global__ void pass_b(const SSArgs A)
         return;
     SS_LOOP(A.N * A.nlab)
     {
-        const int k = (int)(t / A.N);
-        const long long g = t - (long long)k * A.N;
-        const int x = (int)(g / A.rows), y = (int)(g - (long long)x * A.rows);
+        const LabelCell lc(A, t);
+        const int k = lc.k, x = lc.x, y = lc.y;
         const double a = A.pp1[f1(A, k, y, x)], b = A.pp1[f1(A, k, y, x + 1)];
         const double c = A.pp2[f2(A, k, y, x)], d = A.pp2[f2(A, k, y + 1, x)];
         double s = __dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b));
@@ -133,8 +145,8 @@ __global__ void pass_b(const SSArgs A)
         s = __dadd_rn(s, __dmul_rn(d, d));
         const double n = __dsqrt_rn(__dmul_rn(s, 0.5));
         const double al = A.alpha[t];
-        const double q = (n <= al) ? 1.0 : __ddiv_rn(n, al);
-        A.gk[t] = __ddiv_rn(1.0, q);
+        // 1/max(1, n/al); 1/1 is exactly 1, so no division below alpha
+        A.gk[t] = (n <= al) ? 1.0 : __ddiv_rn(1.0, __ddiv_rn(n, al));
     }
 }
 
@@ -144,9 +156,8 @@ __global__ void pass_c(const SSArgs A)
         return;
     SS_LOOP(A.N * A.nlab)
     {
-        const int k = (int)(t / A.N);
-        const long long g = t - (long long)k * A.N;
-        const int x = (int)(g / A.rows), y = (int)(g - (long long)x * A.rows);
+        const LabelCell lc(A, t);
+        const int k = lc.k, x = lc.x, y = lc.y;
         const double gc = A.gk[t];
         if (x >= 1) {
             const long long f = f1(A, k, y, x);
@@ -165,7 +176,8 @@ __global__ void pass_d(const SSArgs A)
         return;
     SS_LOOP(A.N)
     {
-        const int x = (int)(t / A.rows), y = (int)(t - (long long)x * A.rows);
+        const unsigned int tt = (unsigned int)t, r = (unsigned int)A.rows;
+        const int x = (int)(tt / r), y = (int)(tt - (unsigned int)x * r);
         const double ps = A.ps[t];
         double pd = 0.0;
         for (int k = 0; k < A.nlab; ++k) {
@@ -175,13 +187,19 @@ __global__ void pass_d(const SSArgs A)
             dv = __dsub_rn(dv, A.pp2[f2(A, k, y, x)]);
             A.divp[c] = dv;
             const double s = __dadd_rn(dv, A.gdv[c]);
-            const double uc = __ddiv_rn(A.u[c], A.cc);
+            const double uc = A.ucc[c];
             const double ud = __dadd_rn(__dadd_rn(-s, ps), uc);
             const double pt = minimum(ud, A.ct[c]);
             A.pt[c] = pt;
             pd = __dadd_rn(pd, __dsub_rn(__dadd_rn(s, pt), uc));
         }
-        A.ps[t] = __dadd_rn(__ddiv_rn(pd, (double)A.nlab), A.inv_ccl);
+        const double psn = __dadd_rn(__ddiv_rn(pd, (double)A.nlab), A.inv_ccl);
+        A.ps[t] = psn;
+        // the ud of pass E, from this pass's divp, pt and ps
+        for (int k = 0; k < A.nlab; ++k) {
+            const long long c = cell(A, k, y, x);
+            A.ud[c] = ud_e(A.gdv[c], A.divp[c], A.pt[c], psn, A.ucc[c]);
+        }
     }
 }
 
@@ -191,15 +209,14 @@ __global__ void pass_e(const SSArgs A)
         return;
     SS_LOOP(A.N * A.nlab)
     {
-        const int k = (int)(t / A.N);
-        const long long g = t - (long long)k * A.N;
-        const int x = (int)(g / A.rows), y = (int)(g - (long long)x * A.rows);
-        const double ud = ud_e(A, k, y, x);
+        const LabelCell lc(A, t);
+        const int k = lc.k, x = lc.x, y = lc.y;
+        const double ud = A.ud[t];
         // vx on the four faces of the cell (border faces stay 0)
-        const double vl = x >= 1 ? __dsub_rn(ud, ud_e(A, k, y, x - 1)) : 0.0;
-        const double vr = x + 1 < A.cols ? __dsub_rn(ud_e(A, k, y, x + 1), ud) : 0.0;
-        const double vu = y >= 1 ? __dsub_rn(ud, ud_e(A, k, y - 1, x)) : 0.0;
-        const double vd = y + 1 < A.rows ? __dsub_rn(ud_e(A, k, y + 1, x), ud) : 0.0;
+        const double vl = x >= 1 ? __dsub_rn(ud, A.ud[t - A.rows]) : 0.0;
+        const double vr = x + 1 < A.cols ? __dsub_rn(A.ud[t + A.rows], ud) : 0.0;
+        const double vu = y >= 1 ? __dsub_rn(ud, A.ud[t - 1]) : 0.0;
+        const double vd = y + 1 < A.rows ? __dsub_rn(A.ud[t + 1], ud) : 0.0;
         double s = __dadd_rn(__dmul_rn(vl, A.ve1[f1(A, k, y, x)]), __dmul_rn(vr, A.ve1[f1(A, k, y, x + 1)]));
         s = __dadd_rn(s, __dmul_rn(vu, A.ve2[f2(A, k, y, x)]));
         s = __dadd_rn(s, __dmul_rn(vd, A.ve2[f2(A, k, y + 1, x)]));
@@ -219,9 +236,8 @@ __global__ void pass_f(const SSArgs A)
     double err = 0.0;
     SS_LOOP(A.N * A.nlab)
     {
-        const int k = (int)(t / A.N);
-        const long long g = t - (long long)k * A.N;
-        const int x = (int)(g / A.rows), y = (int)(g - (long long)x * A.rows);
+        const LabelCell lc(A, t);
+        const int k = lc.k, x = lc.x, y = lc.y;
         const double vc = A.v[t];
         const double vl = x >= 1 ? __dsub_rn(vc, A.v[t - A.rows]) : 0.0;
         const double vr = x + 1 < A.cols ? __dsub_rn(A.v[t + A.rows], vc) : 0.0;
@@ -233,8 +249,13 @@ __global__ void pass_f(const SSArgs A)
         const double gdv = __dadd_rn(__dmul_rn(s, 0.5), __dmul_rn(vc, A.div_ve[t]));
         A.gdv[t] = gdv;
         const double e = __dmul_rn(A.cc, __dsub_rn(__dadd_rn(__dadd_rn(A.divp[t], gdv), A.pt[t]),
-                                                  A.ps[g]));
-        A.u[t] = __dsub_rn(A.u[t], e);
+                                                  A.ps[lc.g]));
+        const double un = __dsub_rn(A.u[t], e);
+        const double ucc = __ddiv_rn(un, A.cc);
+        A.u[t] = un;
+        A.ucc[t] = ucc;
+        // the ud of the next iteration's pass A
+        A.ud[t] = ud_a(A.divp[t], gdv, A.ps[lc.g], A.pt[t], ucc);
         err += fabs(e);
     }
     // erriter: block partials, the last block sums them in a fixed order
@@ -286,9 +307,8 @@ __global__ void direction_kernel(const SSArgs A, const int *seeds, double *ve1, 
 {
     SS_LOOP(A.N * A.nlab)
     {
-        const int k = (int)(t / A.N);
-        const long long g = t - (long long)k * A.N;
-        const int x = (int)(g / A.rows), y = (int)(g - (long long)x * A.rows);
+        const LabelCell lc(A, t);
+        const int k = lc.k, x = lc.x, y = lc.y;
         const int x0 = seeds[2 * k] - 1, y0 = seeds[2 * k + 1] - 1;
         const float d = seed_dist(y, x, y0, x0);
         // faces at the cell's lower index: interior ones only
@@ -299,6 +319,7 @@ __global__ void direction_kernel(const SSArgs A, const int *seeds, double *ve1, 
         const double e1r = x + 1 < A.cols ? (double)__fsub_rn(seed_dist(y, x + 1, y0, x0), d) : 0.0;
         const double e2d = y + 1 < A.rows ? (double)__fsub_rn(seed_dist(y + 1, x, y0, x0), d) : 0.0;
         div_ve[t] = __dsub_rn(__dadd_rn(__dsub_rn(e1r, e1), e2d), e2);
+        A.ucc[t] = __ddiv_rn(A.u[t], A.cc);  // u/cc of the initial (zero) u
         if (x + 1 == A.cols)
             ve1[f1(A, k, y, x + 1)] = 0.0;
         if (y + 1 == A.rows)
@@ -314,6 +335,16 @@ __global__ void init_ps_kernel(const SSArgs A)
         for (int k = 1; k < A.nlab; ++k)
             m = fmin(m, A.ct[(long long)k * A.N + t]);
         A.ps[t] = m;
+    }
+}
+
+// ud of the first pass A, from the initial state (after init_ps_kernel)
+__global__ void init_ud_kernel(const SSArgs A)
+{
+    SS_LOOP(A.N * A.nlab)
+    {
+        const LabelCell lc(A, t);
+        A.ud[t] = ud_a(A.divp[t], A.gdv[t], A.ps[lc.g], A.pt[t], A.ucc[t]);
     }
 }
 
@@ -395,7 +426,7 @@ extern "C" ASETS_API asets_status asets_potts2d_starshape(
     int h_done[2] = {0, 0};
     int chunk = 0;
     if (!alloc(&ct, NL) || !alloc(&al, NL) || !alloc(&ve1, F1) || !alloc(&ve2, F2) ||
-        !alloc(&dve, NL) || !alloc(&A.u, NL) || !alloc(&A.pt, NL) || !alloc(&A.ps, N) ||
+        !alloc(&dve, NL) || !alloc(&A.u, NL) || !alloc(&A.ucc, NL) || !alloc(&A.ud, NL) || !alloc(&A.pt, NL) || !alloc(&A.ps, N) ||
         !alloc(&A.divp, NL) || !alloc(&A.pp1, F1) || !alloc(&A.pp2, F2) || !alloc(&A.gk, NL) ||
         !alloc(&A.v, NL) || !alloc(&A.gdv, NL) || !alloc(&A.partials, grid) ||
         !alloc(&A.erriter, iterNum)) {
@@ -433,6 +464,7 @@ extern "C" ASETS_API asets_status asets_potts2d_starshape(
         if (e == cudaSuccess) {
             direction_kernel<<<grid, kThreads, 0, st>>>(A, seeds, ve1, ve2, dve);
             init_ps_kernel<<<ss_grid(N, sms), kThreads, 0, st>>>(A);
+            init_ud_kernel<<<grid, kThreads, 0, st>>>(A);
             e = cudaGetLastError();
         }
         // iterations in chunks; every kernel exits at entry once converged

@@ -446,13 +446,16 @@ def configs_run(ctx, cpu: bool) -> list:
 
 def _per_iteration_s(solve, n: int) -> float:
     """Seconds per iteration of a synchronous host-array solve: the slope of
-    the wall time of n-, 2n- and 4n-iteration solves (best of two each;
-    copies and set-up do not depend on the iteration count)."""
+    the wall time of n-, 2n- and 4n-iteration solves (best of three each;
+    copies and set-up do not depend on the iteration count).  While the
+    iterations are not at least half of the n-iteration solve's time, or the
+    slope is not positive, n grows fourfold (at most three times), so that
+    host copy noise cannot swamp the iteration time."""
     import torch
 
     def wall(k):
         best = float("inf")
-        for _ in range(2):
+        for _ in range(3):
             torch.cuda.synchronize()
             t = time.perf_counter()
             solve(k)
@@ -461,10 +464,16 @@ def _per_iteration_s(solve, n: int) -> float:
         return best
 
     solve(2)  # warm-up
-    ks = np.array([n, 2 * n, 4 * n], float)
-    ts = np.array([wall(int(k)) for k in ks])
-    slope = float(np.polyfit(ks, ts, 1)[0])
-    return max(slope, 1e-9)
+    for _ in range(4):
+        ks = np.array([n, 2 * n, 4 * n], float)
+        ts = np.array([wall(int(k)) for k in ks])
+        slope = float(np.polyfit(ks, ts, 1)[0])
+        if slope > 0 and slope * n >= 0.5 * ts[0]:
+            break
+        n *= 4
+    if slope <= 0:
+        raise RuntimeError("per-iteration time not resolved above host noise")
+    return slope
 
 
 def _hmf_tree(make, shape, dt, seed):
