@@ -9,18 +9,21 @@
 // evaluation order (IEEE operations, no contraction), so u matches a numpy
 // restatement in the same precision bit for bit.
 //
-// Per iteration, five passes over every flow label (binary 1, Potts L,
-// Ishikawa L-1):
-//   0 ud = divp - ((A - B) + u/cc) per cell (into the gk buffer),
-//     (A, B) = (ps, pt) binary, (ps, pt_k) Potts, (pt_k, pt_k+1) Ishikawa
-//   1 gradient step of the face flows from ud of the cell and the one below
+// Per iteration, over every flow label (binary 1, Potts L, Ishikawa L-1):
+//   1 gradient step of the face flows from ud = divp - ((A - B) + u/cc) of
+//     the cell and the one below, (A, B) = (ps, pt) binary, (ps, pt_k)
+//     Potts, (pt_k, pt_k+1) Ishikawa
 //   2 projection factor gk = 1/max(1, |p|/alpha) per cell
 //   3 face flows *= 0.5 (gk + gk of the cell below)
 //   4 per cell: divp of every label, then the model's sink/source flows and
-//     multipliers, and erriter; the last block records erriter and the break.
-// In double precision, where the FP64 pipe bounds the passes, u/cc (the
-// same quotient in passes 0 and 4 of an iteration, twice in 4 for Ishikawa)
-// is divided once, where u is written, and kept beside u.
+//     multipliers, erriter and the next iteration's ud; the last block
+//     records erriter and the break.
+// Single precision runs 1+2 and 3+4 as two passes (each cell also forms
+// the faces above it, which their own cells store); double precision, where
+// the FP64 pipe bounds the passes and recomputed faces would cost more
+// than the passes, runs the four, and keeps u/cc (the same quotient in 1
+// and 4 of an iteration, twice in 4 for Ishikawa) beside u, divided once
+// where u is written.
 #include <chrono>
 #include <cstring>
 #include <string>
@@ -49,7 +52,7 @@ struct MTArgs {
     long long n, f1, f2, f3;  // cells and faces per flow label
     T cc, steps, half, one_over_cc, one_over_ccl, beta;
     const T *cs, *ct, *alpha;
-    T *u, *ucc, *pt, *ps, *divp, *gk, *p1, *p2, *p3;
+    T *u, *ucc, *ud, *pt, *ps, *divp, *gk, *p1, *p2, *p3, *q1, *q2, *q3;
     double *partials;
     T *erriter;
     MTCtl *ctl;
@@ -73,6 +76,14 @@ template <> __device__ __forceinline__ double sqr(double a) { return __dsqrt_rn(
 
 // u/cc of element o: kept beside u in double precision, divided here in single
 template <class T>
+__device__ __forceinline__ T u_cc(const MTArgs<T> &A, long long o, T u)
+{
+    if constexpr (sizeof(T) == 8)
+        return A.ucc[o];
+    else
+        return dvd(u, A.cc);
+}
+template <class T>
 __device__ __forceinline__ T u_cc(const MTArgs<T> &A, long long o)
 {
     if constexpr (sizeof(T) == 8)
@@ -80,12 +91,16 @@ __device__ __forceinline__ T u_cc(const MTArgs<T> &A, long long o)
     else
         return dvd(A.u[o], A.cc);
 }
+// stores u of element o (and, in double precision, u/cc beside it);
+// returns the new u/cc
 template <class T>
-__device__ __forceinline__ void set_u(const MTArgs<T> &A, long long o, T v)
+__device__ __forceinline__ T set_u(const MTArgs<T> &A, long long o, T v)
 {
     A.u[o] = v;
+    const T q = dvd(v, A.cc);
     if constexpr (sizeof(T) == 8)
-        A.ucc[o] = dvd(v, A.cc);
+        A.ucc[o] = q;
+    return q;
 }
 
 // Matlab's min(a, b) for ordered values; a NaN a is kept (as the restatement)
@@ -165,20 +180,44 @@ __device__ __forceinline__ T ud(const MTArgs<T> &A, int k, long long g)
     return sub(A.divp[o], add(sub(a, b), u_cc(A, o)));
 }
 
-// ud of every flow label and cell, into the gk buffer (free until mt_gk):
-// the face pass then reads it for the cell and its three lower neighbours
-// instead of forming it four times.
+// ud of every flow label and cell of the initial state; the cell pass forms
+// it for the next iteration
 template <class T, int M>
 __global__ void mt_ud(const MTArgs<T> A)
 {
-    if (finished(A))
-        return;
     MT_LOOP(A.n * A.nflow)
     {
         const int k = label_of(t, A.n);
-        A.gk[t] = ud<T, M>(A, k, t - (long long)k * A.n);
+        A.ud[t] = ud<T, M>(A, k, t - (long long)k * A.n);
     }
 }
+
+// gradient step of a face flow pp from the ud of the face's upper and lower
+// cells: binary pp + steps*(d); Potts/Ishikawa steps*(d) + pp
+template <class T, int M>
+__device__ __forceinline__ T face_step(const MTArgs<T> &A, T pp, T ud_up, T ud_lo)
+{
+    const T s = mul(A.steps, sub(ud_up, ud_lo));
+    return (M == MT_BINARY) ? add(pp, s) : add(s, pp);
+}
+
+// projection rescale of a face flow: 0.5 (gk of the upper cell + gk of the lower) p
+template <class T>
+__device__ __forceinline__ T face_rescale(const MTArgs<T> &A, T p, T g_up, T g_lo)
+{
+    return mul(mul(A.half, add(g_up, g_lo)), p);
+}
+
+// projection factor 1/max(1, |p|/alpha) from the sum of squares s of the
+// cell's faces; 1/1 is exactly 1, so no division below alpha
+template <class T>
+__device__ __forceinline__ T proj_factor(const MTArgs<T> &A, T s, T al)
+{
+    const T g = sqr(mul(s, A.half));
+    return (g <= al) ? (T)1 : dvd((T)1, dvd(g, al));
+}
+
+// ---- double precision: four passes, each face formed once --------------
 
 template <class T, int M, int D>
 __global__ void mt_step(const MTArgs<T> A)
@@ -189,19 +228,15 @@ __global__ void mt_step(const MTArgs<T> A)
     {
         const int k = label_of(t, A.n);
         const Cell<T> c(A, t - (long long)k * A.n);
-        const T u0 = A.gk[t];
-        // binary: pp + steps*(d); Potts/Ishikawa: steps*(d) + pp
-        auto upd = [&](T *f, T nb) {
-            const T s = mul(A.steps, sub(u0, nb));
-            *f = (M == MT_BINARY) ? add(*f, s) : add(s, *f);
-        };
+        const T u0 = A.ud[t];
+        auto upd = [&](T *f, T nb) { *f = face_step<T, M>(A, *f, u0, nb); };
         if (c.x >= 1)
-            upd(A.p1 + (long long)k * A.f1 + j1(A, c.y, c.x, c.z), A.gk[t - A.rows]);
+            upd(A.p1 + (long long)k * A.f1 + j1(A, c.y, c.x, c.z), A.ud[t - A.rows]);
         if (c.y >= 1)
-            upd(A.p2 + (long long)k * A.f2 + j2(A, c.y, c.x, c.z), A.gk[t - 1]);
+            upd(A.p2 + (long long)k * A.f2 + j2(A, c.y, c.x, c.z), A.ud[t - 1]);
         if (D == 3 && c.z >= 1)
             upd(A.p3 + (long long)k * A.f3 + j3(A, c.y, c.x, c.z),
-                A.gk[t - (long long)A.rows * A.cols]);
+                A.ud[t - (long long)A.rows * A.cols]);
     }
 }
 
@@ -216,7 +251,7 @@ __global__ void mt_gk(const MTArgs<T> A)
         const Cell<T> c(A, t - (long long)k * A.n);
         const T *f1 = A.p1 + (long long)k * A.f1, *f2 = A.p2 + (long long)k * A.f2;
         const T a = f1[j1(A, c.y, c.x, c.z)], b = f1[j1(A, c.y, c.x + 1, c.z)];
-        const T d = A.p2[(long long)k * A.f2 + j2(A, c.y, c.x, c.z)], e = f2[j2(A, c.y + 1, c.x, c.z)];
+        const T d = f2[j2(A, c.y, c.x, c.z)], e = f2[j2(A, c.y + 1, c.x, c.z)];
         T s = add(mul(a, a), mul(b, b));
         s = add(s, mul(d, d));
         s = add(s, mul(e, e));
@@ -226,10 +261,7 @@ __global__ void mt_gk(const MTArgs<T> A)
             s = add(s, mul(p, p));
             s = add(s, mul(q, q));
         }
-        const T g = sqr(mul(s, A.half));
-        const T al = A.alpha[t];
-        // 1/max(1, g/al); 1/1 is exactly 1, so no division below alpha
-        A.gk[t] = (g <= al) ? (T)1 : dvd((T)1, dvd(g, al));
+        A.gk[t] = proj_factor(A, s, A.alpha[t]);
     }
 }
 
@@ -243,7 +275,7 @@ __global__ void mt_rescale(const MTArgs<T> A)
         const int k = label_of(t, A.n);
         const Cell<T> c(A, t - (long long)k * A.n);
         const T g0 = A.gk[t];
-        auto sc = [&](T *f, T gnb) { *f = mul(mul(A.half, add(g0, gnb)), *f); };
+        auto sc = [&](T *f, T gnb) { *f = face_rescale(A, *f, g0, gnb); };
         if (c.x >= 1)
             sc(A.p1 + (long long)k * A.f1 + j1(A, c.y, c.x, c.z), A.gk[t - A.rows]);
         if (c.y >= 1)
@@ -268,7 +300,219 @@ __device__ __forceinline__ T divergence(const MTArgs<T> &A, int k, const Cell<T>
     return d;
 }
 
+// ---- single precision: two passes ---------------------------------------
+// The gradient step and the projection factor in one pass, the rescale and
+// the cell update in the other.  A cell steps (rescales) its lower faces and
+// stores them, and forms its upper faces, which the cells above store, from
+// the same operands for its magnitude (divergence).  The stepped flows go
+// to the second face buffer (q), the rescaled ones back to p, so that no
+// pass reads a face another thread of it writes.
+
+// A cell's value of a per-cell array with those of its lower and upper
+// neighbours along each axis, and the cell's lower and upper faces of the
+// three face arrays, all loaded before any is used (the passes are bound
+// by the latency of these loads).  A neighbour outside the volume reads
+// the cell itself; its value is not used.
+template <class T, int D>
+struct Around {
+    T v, xl, xu, yl, yu, zl, zu;  // per-cell values
+    T a, b, d, e, p, q;           // faces: x lower/upper, y lower/upper, z lower/upper
+    long long fa, fd, fp;         // the lower faces' indices
+    bool has_xl, has_xu, has_yl, has_yu, has_zl, has_zu;
+    __device__ __forceinline__ Around(const MTArgs<T> &A, const Cell<T> &c, const T *cell,
+                                      const T *f1, const T *f2, const T *f3)
+    {
+        const long long g = c.g, pl = (long long)A.rows * A.cols;
+        has_xl = c.x >= 1;
+        has_xu = c.x + 1 < A.cols;
+        has_yl = c.y >= 1;
+        has_yu = c.y + 1 < A.rows;
+        has_zl = D == 3 && c.z >= 1;
+        has_zu = D == 3 && c.z + 1 < A.slices;
+        fa = j1(A, c.y, c.x, c.z);
+        fd = j2(A, c.y, c.x, c.z);
+        fp = j3(A, c.y, c.x, c.z);
+        v = cell[g];
+        xl = cell[has_xl ? g - A.rows : g];
+        xu = cell[has_xu ? g + A.rows : g];
+        yl = cell[has_yl ? g - 1 : g];
+        yu = cell[has_yu ? g + 1 : g];
+        a = f1[fa];
+        b = f1[j1(A, c.y, c.x + 1, c.z)];
+        d = f2[fd];
+        e = f2[j2(A, c.y + 1, c.x, c.z)];
+        if (D == 3) {
+            zl = cell[has_zl ? g - pl : g];
+            zu = cell[has_zu ? g + pl : g];
+            p = f3[fp];
+            q = f3[j3(A, c.y, c.x, c.z + 1)];
+        }
+    }
+};
+
 template <class T, int M, int D>
+__global__ void mt_step_gk(const MTArgs<T> A)
+{
+    if (finished(A))
+        return;
+    MT_LOOP(A.n * A.nflow)
+    {
+        const int k = label_of(t, A.n);
+        const Cell<T> c(A, t - (long long)k * A.n);
+        const Around<T, D> s(A, c, A.ud + (long long)k * A.n, A.p1 + (long long)k * A.f1,
+                             A.p2 + (long long)k * A.f2, A.p3 + (long long)k * A.f3);
+        const T al = A.alpha[t];
+        T *d1 = A.q1 + (long long)k * A.f1, *d2 = A.q2 + (long long)k * A.f2;
+        T a = s.a, b = s.b, d = s.d, e = s.e;
+        if (s.has_xl) {
+            a = face_step<T, M>(A, a, s.v, s.xl);
+            d1[s.fa] = a;
+        }
+        if (s.has_xu)
+            b = face_step<T, M>(A, b, s.xu, s.v);
+        if (s.has_yl) {
+            d = face_step<T, M>(A, d, s.v, s.yl);
+            d2[s.fd] = d;
+        }
+        if (s.has_yu)
+            e = face_step<T, M>(A, e, s.yu, s.v);
+        T m = add(mul(a, a), mul(b, b));
+        m = add(m, mul(d, d));
+        m = add(m, mul(e, e));
+        if (D == 3) {
+            T p = s.p, q = s.q;
+            if (s.has_zl) {
+                p = face_step<T, M>(A, p, s.v, s.zl);
+                A.q3[(long long)k * A.f3 + s.fp] = p;
+            }
+            if (s.has_zu)
+                q = face_step<T, M>(A, q, s.zu, s.v);
+            m = add(m, mul(p, p));
+            m = add(m, mul(q, q));
+        }
+        A.gk[t] = proj_factor(A, m, al);
+    }
+}
+
+// divergence of flow label k at cell c from the stepped flows (q), with the
+// rescale of every face; the cell's lower faces are stored (into p)
+template <class T, int D>
+__device__ __forceinline__ T rescaled_divergence(const MTArgs<T> &A, int k, const Cell<T> &c)
+{
+    const Around<T, D> s(A, c, A.gk + (long long)k * A.n, A.q1 + (long long)k * A.f1,
+                         A.q2 + (long long)k * A.f2, A.q3 + (long long)k * A.f3);
+    T a = s.a, b = s.b, d = s.d, e = s.e;
+    if (s.has_xl) {
+        a = face_rescale(A, a, s.v, s.xl);
+        A.p1[(long long)k * A.f1 + s.fa] = a;
+    }
+    if (s.has_xu)
+        b = face_rescale(A, b, s.xu, s.v);
+    if (s.has_yl) {
+        d = face_rescale(A, d, s.v, s.yl);
+        A.p2[(long long)k * A.f2 + s.fd] = d;
+    }
+    if (s.has_yu)
+        e = face_rescale(A, e, s.yu, s.v);
+    T dv = sub(b, a);
+    dv = add(dv, e);
+    dv = sub(dv, d);
+    if (D == 3) {
+        T p = s.p, q = s.q;
+        if (s.has_zl) {
+            p = face_rescale(A, p, s.v, s.zl);
+            A.p3[(long long)k * A.f3 + s.fp] = p;
+        }
+        if (s.has_zu)
+            q = face_rescale(A, q, s.zu, s.v);
+        dv = add(dv, q);
+        dv = sub(dv, p);
+    }
+    return dv;
+}
+
+// ---- the cell update (both precisions) -----------------------------------
+
+// binary: ps, pt, u of cell g from its divp dv and old u, pt, Cs, Ct, then
+// the next iteration's ud; returns |erru|
+template <class T>
+__device__ __forceinline__ double binary_update(const MTArgs<T> &A, long long g, T dv, T u, T pt0,
+                                                T cs, T ct)
+{
+    const T uc = u_cc(A, g, u);
+    const T ps = mn(add(sub(add(dv, pt0), uc), A.one_over_cc), cs);
+    const T pt = mn(add(add(-dv, ps), uc), ct);
+    const T e = mul(A.cc, sub(add(dv, pt), ps));
+    A.ps[g] = ps;
+    A.pt[g] = pt;
+    const T q = set_u(A, g, sub(u, e));
+    A.ud[g] = sub(dv, add(sub(ps, pt), q));
+    return fabs((double)e);
+}
+
+// The model's sink/source flows and multipliers of cell g from divp of
+// every flow label, then the ud of the next iteration; returns the cell's
+// share of erriter.
+template <class T, int M>
+__device__ __forceinline__ double cell_update(const MTArgs<T> &A, long long g)
+{
+    const long long n = A.n;
+    double err = 0.0;
+    if (M == MT_BINARY) {
+        err += binary_update(A, g, A.divp[g], A.u[g], A.pt[g], A.cs[g], A.ct[g]);
+    } else if (M == MT_POTTS) {
+        const T ps = A.ps[g];
+        T pd = (T)0;
+        for (int k = 0; k < A.nlab; ++k) {
+            const long long o = (long long)k * n + g;
+            const T dv = A.divp[o], uc = u_cc(A, o);
+            const T pt = mn(add(add(-dv, ps), uc), A.ct[o]);
+            A.pt[o] = pt;
+            pd = add(pd, sub(add(dv, pt), uc));
+        }
+        const T psn = add(dvd(pd, (T)A.nlab), A.one_over_ccl);
+        A.ps[g] = psn;
+        for (int k = 0; k < A.nlab; ++k) {
+            const long long o = (long long)k * n + g;
+            const T dv = A.divp[o], pt = A.pt[o];
+            const T e = mul(A.cc, sub(add(dv, pt), psn));
+            const T q = set_u(A, o, sub(A.u[o], e));
+            A.ud[o] = sub(dv, add(sub(psn, pt), q));
+            err += fabs((double)e);
+        }
+    } else {
+        const int L = A.nlab;
+        for (int k = 0; k < L; ++k) {
+            const long long o = (long long)k * n + g;
+            T v;
+            if (k == 0) {
+                v = add(sub(add(A.divp[g], A.pt[g + n]), u_cc(A, g)), A.one_over_cc);
+            } else {
+                const long long ob = o - n;  // label k-1: its pt is the new one
+                v = add(add(-A.divp[ob], A.pt[ob]), u_cc(A, ob));
+                if (k < L - 1) {
+                    v = sub(add(add(v, A.divp[o]), A.pt[o + n]), u_cc(A, o));
+                    v = dvd(v, (T)2);
+                }
+            }
+            A.pt[o] = mn(v, A.ct[o]);
+        }
+        for (int k = 0; k < L - 1; ++k) {
+            const long long o = (long long)k * n + g;
+            const T dv = A.divp[o], pa = A.pt[o], pb = A.pt[o + n];
+            const T e = mul(A.cc, sub(add(dv, pb), pa));
+            const T q = set_u(A, o, sub(A.u[o], e));
+            A.ud[o] = sub(dv, add(sub(pa, pb), q));
+            err += fabs((double)e);
+        }
+    }
+    return err;
+}
+
+// Per cell: divp of every flow label (FUSED: with the rescale of the
+// stepped flows), the cell update; the last block records erriter and the
+// break.
+template <class T, int M, int D, bool FUSED>
 __global__ void mt_cell(const MTArgs<T> A)
 {
     __shared__ double s_red[kThreads / 32];
@@ -280,60 +524,18 @@ __global__ void mt_cell(const MTArgs<T> A)
     MT_LOOP(A.n)
     {
         const Cell<T> c(A, t);
-        const long long g = t, n = A.n;
-        for (int k = 0; k < A.nflow; ++k)
-            A.divp[(long long)k * n + g] = divergence<T, D>(A, k, c);
-        if (M == MT_BINARY) {
-            const T dv = A.divp[g], u = A.u[g], uc = u_cc(A, g);
-            const T ps = mn(add(sub(add(dv, A.pt[g]), uc), A.one_over_cc), A.cs[g]);
-            const T pt = mn(add(add(-dv, ps), uc), A.ct[g]);
-            const T e = mul(A.cc, sub(add(dv, pt), ps));
-            A.ps[g] = ps;
-            A.pt[g] = pt;
-            set_u(A, g, sub(u, e));
-            err += fabs((double)e);
-        } else if (M == MT_POTTS) {
-            const T ps = A.ps[g];
-            T pd = (T)0;
-            for (int k = 0; k < A.nlab; ++k) {
-                const long long o = (long long)k * n + g;
-                const T dv = A.divp[o], uc = u_cc(A, o);
-                const T pt = mn(add(add(-dv, ps), uc), A.ct[o]);
-                A.pt[o] = pt;
-                pd = add(pd, sub(add(dv, pt), uc));
-            }
-            const T psn = add(dvd(pd, (T)A.nlab), A.one_over_ccl);
-            A.ps[g] = psn;
-            for (int k = 0; k < A.nlab; ++k) {
-                const long long o = (long long)k * n + g;
-                const T e = mul(A.cc, sub(add(A.divp[o], A.pt[o]), psn));
-                set_u(A, o, sub(A.u[o], e));
-                err += fabs((double)e);
-            }
-        } else {
-            const int L = A.nlab;
-            for (int k = 0; k < L; ++k) {
-                const long long o = (long long)k * n + g;
-                T v;
-                if (k == 0) {
-                    v = add(sub(add(A.divp[g], A.pt[g + n]), u_cc(A, g)), A.one_over_cc);
-                } else {
-                    const long long ob = o - n;  // label k-1: its pt is the new one
-                    v = add(add(-A.divp[ob], A.pt[ob]), u_cc(A, ob));
-                    if (k < L - 1) {
-                        v = sub(add(add(v, A.divp[o]), A.pt[o + n]), u_cc(A, o));
-                        v = dvd(v, (T)2);
-                    }
-                }
-                A.pt[o] = mn(v, A.ct[o]);
-            }
-            for (int k = 0; k < L - 1; ++k) {
-                const long long o = (long long)k * n + g;
-                const T e = mul(A.cc, sub(add(A.divp[o], A.pt[o + n]), A.pt[o]));
-                set_u(A, o, sub(A.u[o], e));
-                err += fabs((double)e);
-            }
+        if (M == MT_BINARY && FUSED) {
+            // the cell's own operands are loaded with the divergence's; divp
+            // is used by this thread alone and not stored
+            const T u = A.u[t], pt = A.pt[t], cs = A.cs[t], ct = A.ct[t];
+            const T dv = rescaled_divergence<T, D>(A, 0, c);
+            err += binary_update(A, t, dv, u, pt, cs, ct);
+            continue;
         }
+        for (int k = 0; k < A.nflow; ++k)
+            A.divp[(long long)k * A.n + t] =
+                FUSED ? rescaled_divergence<T, D>(A, k, c) : divergence<T, D>(A, k, c);
+        err += cell_update<T, M>(A, t);
     }
     for (int o = 16; o > 0; o >>= 1)
         err += __shfl_xor_sync(0xffffffffu, err, o);
@@ -454,7 +656,11 @@ asets_status mt_run(asets_context *ctx, int rows, int cols, int slices, int nlab
     T *cs = nullptr, *ct = nullptr, *al = nullptr;
     asets_status status = ASETS_OK;
     const int grid = mt_grid(n * A.nflow, sms), gcell = mt_grid(n, sms);
+    constexpr bool kFused = sizeof(T) == 4;
     bool ok = get(&ct, n * nct) && get(&al, n * A.nflow) && get(&A.u, n * nu) &&
+              get(&A.ud, n * A.nflow) &&
+              (!kFused || (get(&A.q1, A.f1 * A.nflow) && get(&A.q2, A.f2 * A.nflow) &&
+                           get(&A.q3, A.f3 * A.nflow))) &&
               (sizeof(T) != 8 || get(&A.ucc, n * nu)) && get(&A.pt, n * npt) && get(&A.ps, n) && get(&A.divp, n * A.nflow) &&
               get(&A.gk, n * A.nflow) && get(&A.p1, A.f1 * A.nflow) && get(&A.p2, A.f2 * A.nflow) &&
               get(&A.p3, A.f3 * A.nflow) && get(&A.erriter, iterNum) &&
@@ -485,10 +691,13 @@ asets_status mt_run(asets_context *ctx, int rows, int cols, int slices, int nlab
             e = cudaMemcpyAsync(cs, Cs, sizeof(T) * n, cudaMemcpyHostToDevice, st);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(A.ctl, &c0, sizeof c0, cudaMemcpyHostToDevice, st);
-        T *zero[] = {A.divp, A.p1, A.p2, A.p3, A.erriter};
+        // the flows and the second face buffer start at zero; their border
+        // faces are never written and stay zero (the zero-flux border)
+        T *zero[] = {A.divp, A.p1, A.p2, A.p3, A.erriter, A.q1, A.q2, A.q3};
+        const long long fq = kFused ? A.nflow : 0;
         const long long zn[] = {n * A.nflow, A.f1 * A.nflow, A.f2 * A.nflow, A.f3 * A.nflow,
-                                (long long)iterNum};
-        for (int i = 0; i < 5 && e == cudaSuccess; ++i)
+                                (long long)iterNum, A.f1 * fq, A.f2 * fq, A.f3 * fq};
+        for (int i = 0; i < 8 && e == cudaSuccess; ++i)
             if (zn[i] > 0)
                 e = cudaMemsetAsync(zero[i], 0, sizeof(T) * zn[i], st);
         A.cs = cs;
@@ -496,17 +705,22 @@ asets_status mt_run(asets_context *ctx, int rows, int cols, int slices, int nlab
         A.alpha = al;
         if (e == cudaSuccess) {
             mt_init<T, M><<<gcell, kThreads, 0, st>>>(A);
+            mt_ud<T, M><<<grid, kThreads, 0, st>>>(A);
             e = cudaGetLastError();
         }
         constexpr int kChunk = 16;
         int h_done = 0;
         for (int done_it = 0; e == cudaSuccess && done_it < iterNum; done_it += kChunk) {
             for (int i = 0; i < kChunk && done_it + i < iterNum; ++i) {
-                mt_ud<T, M><<<grid, kThreads, 0, st>>>(A);
-                mt_step<T, M, D><<<grid, kThreads, 0, st>>>(A);
-                mt_gk<T, M, D><<<grid, kThreads, 0, st>>>(A);
-                mt_rescale<T, M, D><<<grid, kThreads, 0, st>>>(A);
-                mt_cell<T, M, D><<<gcell, kThreads, 0, st>>>(A);
+                if constexpr (kFused) {
+                    mt_step_gk<T, M, D><<<grid, kThreads, 0, st>>>(A);
+                    mt_cell<T, M, D, true><<<gcell, kThreads, 0, st>>>(A);
+                } else {
+                    mt_step<T, M, D><<<grid, kThreads, 0, st>>>(A);
+                    mt_gk<T, M, D><<<grid, kThreads, 0, st>>>(A);
+                    mt_rescale<T, M, D><<<grid, kThreads, 0, st>>>(A);
+                    mt_cell<T, M, D, false><<<gcell, kThreads, 0, st>>>(A);
+                }
             }
             e = cudaGetLastError();
             if (e == cudaSuccess)
