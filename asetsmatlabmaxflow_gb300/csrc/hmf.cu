@@ -68,6 +68,7 @@ struct HArgs {
     const int *order;   // DAG: the top-down node list
     T *pn;              // DAG: pushed-down flow of multi-parent nodes
     T *pt, *u, *div, *g, *p1, *p2, *p3;
+    int nedges;         // DAG: child edges (entries of children)
     T *e1, *e2, *e3;  // exempt flow per face (nodes with direction fields)
     double *cost;  // [m][2]: sum u*Ct (leaves), sum u*div (non-root)
 };
@@ -169,6 +170,84 @@ __global__ void k1_pointwise(const HArgs<T> A)
             const T ptp = A.pt[(long long)A.nodes[i].parent * A.n + c];
             const T dv = A.div[o], pt = A.pt[o];
             const T u = add(A.u[o], mul(A.cc, sub(sub(ptp, dv), pt)));
+            A.u[o] = u;
+            A.g[o] = mul(A.steps, sub(sub(add(dv, pt), ptp), dvd(u, A.cc)));
+        }
+    }
+}
+
+// k1_pointwise with the pixel's values of every node staged in shared
+// memory (one column per thread): the pixel's loads are issued together
+// and the children-first chain of sink flows runs on shared memory instead
+// of reading back through L2 what the thread has just stored.  A leaf's old
+// sink flow is never read (its parent reads it after the leaf's update), so
+// its slot holds Ct until then.  The node table is staged once per block.
+// Same operations in the same order as k1_pointwise.
+struct K1Stage {
+    // the node table: parent, first child and child count per node and the
+    // children list (4m ints), then the nodes' Ct pointers; then the three
+    // per-thread columns (sink flow, divergence, label) of every node
+    static constexpr int ptr_off(int m) { return 16 * m; }
+    static constexpr int table_bytes(int m) { return 16 * m + (8 * m + 15) / 16 * 16; }
+    static constexpr int bytes(int m, int elem) { return table_bytes(m) + 3 * m * kThreads * elem; }
+};
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) k1_staged(const HArgs<T> A)
+{
+    extern __shared__ __align__(16) unsigned char k1sm[];
+    const int m = A.m, tid = threadIdx.x;
+    int *npar = reinterpret_cast<int *>(k1sm);
+    int *nfirst = npar + m, *ncount = nfirst + m, *kids = ncount + m;
+    const T **cts = reinterpret_cast<const T **>(k1sm + K1Stage::ptr_off(m));
+    T *PT = reinterpret_cast<T *>(k1sm + K1Stage::table_bytes(m));
+    T *DV = PT + m * kThreads, *U = DV + m * kThreads;
+    for (int i = tid; i < m; i += kThreads) {
+        const NodeDev<T> &nd = A.nodes[i];
+        npar[i] = nd.parent;
+        nfirst[i] = nd.child_begin;
+        ncount[i] = nd.nchild;
+        cts[i] = nd.ct;
+    }
+    for (int j = tid; j < m - 1; j += kThreads)
+        kids[j] = A.children[j];
+    __syncthreads();
+    H_LOOP(A.n)
+    {
+        const long long c = t;
+        for (int i = 0; i < m; ++i) {
+            const long long o = (long long)i * A.n + c;
+            PT[i * kThreads + tid] = ncount[i] == 0 ? cts[i][c] : A.pt[o];
+            if (i > 0) {
+                DV[i * kThreads + tid] = A.div[o];
+                U[i * kThreads + tid] = A.u[o];
+            }
+        }
+        for (int i = m - 1; i >= 0; --i) {
+            const int par = npar[i];
+            T acc = par >= 0 ? add(sub(PT[par * kThreads + tid], DV[i * kThreads + tid]),
+                                   dvd(U[i * kThreads + tid], A.cc))
+                             : A.inv_cc;
+            const int nc = ncount[i];
+            if (nc == 0) {
+                const T ct = PT[i * kThreads + tid];
+                PT[i * kThreads + tid] = (ct <= acc || ct != ct) ? ct : acc;
+                continue;
+            }
+            for (int j = 0; j < nc; ++j) {
+                const int ch = kids[nfirst[i] + j];
+                acc = sub(add(add(acc, PT[ch * kThreads + tid]), DV[ch * kThreads + tid]),
+                          dvd(U[ch * kThreads + tid], A.cc));
+            }
+            PT[i * kThreads + tid] = dvd(acc, (T)(par >= 0 ? 1 + nc : nc));
+        }
+        A.pt[c] = PT[tid];
+        for (int i = 1; i < m; ++i) {
+            const long long o = (long long)i * A.n + c;
+            const T ptp = PT[npar[i] * kThreads + tid];
+            const T dv = DV[i * kThreads + tid], pt = PT[i * kThreads + tid];
+            const T u = add(U[i * kThreads + tid], mul(A.cc, sub(sub(ptp, dv), pt)));
+            A.pt[o] = pt;
             A.u[o] = u;
             A.g[o] = mul(A.steps, sub(sub(add(dv, pt), ptp), dvd(u, A.cc)));
         }
@@ -648,6 +727,128 @@ __global__ void k_dag_point(const HArgs<T> A)
     }
 }
 
+// k_dag_point with the pixel's values of every node staged in shared memory
+// (one column per thread; as k1_staged): sink flow (a leaf's slot holds Ct
+// until its update, its old sink flow is never read), divergence, label,
+// pushed-down flow and the gradient input, with the graph's tables staged
+// once per block.  Same operations in the same order as k_dag_point; pn, g
+// and u are stored for the nodes k_dag_point stores them for.
+struct DagStage {
+    // ints: parents, first parent, first child, child count, top-down order
+    // (5m) and the children list (E); then the weights: wdiv (m) and the
+    // child edges' (E); then the nodes' Ct pointers; then five columns
+    static constexpr int int_bytes(int m, int e) { return (4 * (5 * m + e) + 15) / 16 * 16; }
+    static constexpr int w_bytes(int m, int e, int elem) { return (elem * (m + e) + 15) / 16 * 16; }
+    static constexpr int table_bytes(int m, int e, int elem)
+    {
+        return int_bytes(m, e) + w_bytes(m, e, elem) + (8 * m + 15) / 16 * 16;
+    }
+    static constexpr int bytes(int m, int e, int elem)
+    {
+        return table_bytes(m, e, elem) + 5 * m * kThreads * elem;
+    }
+};
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) k_dag_point_staged(const HArgs<T> A)
+{
+    extern __shared__ __align__(16) unsigned char dsm[];
+    const int m = A.m, ne = A.nedges, tid = threadIdx.x;
+    int *npar = reinterpret_cast<int *>(dsm);
+    int *par = npar + m, *first = par + m, *cnt = first + m, *order = cnt + m, *kids = order + m;
+    T *wdiv = reinterpret_cast<T *>(dsm + DagStage::int_bytes(m, ne));
+    T *wch = wdiv + m;
+    const T **cts = reinterpret_cast<const T **>(dsm + DagStage::int_bytes(m, ne) +
+                                                 DagStage::w_bytes(m, ne, (int)sizeof(T)));
+    T *PT = reinterpret_cast<T *>(dsm + DagStage::table_bytes(m, ne, (int)sizeof(T)));
+    T *DV = PT + m * kThreads, *U = DV + m * kThreads, *PN = U + m * kThreads, *G = PN + m * kThreads;
+    for (int i = tid; i < m; i += kThreads) {
+        const NodeDev<T> &nd = A.nodes[i];
+        npar[i] = nd.nparent;
+        par[i] = nd.parent;
+        first[i] = nd.child_begin;
+        cnt[i] = nd.nchild;
+        order[i] = A.order[i];
+        wdiv[i] = nd.wdiv;
+        cts[i] = nd.ct;
+    }
+    for (int j = tid; j < ne; j += kThreads) {
+        kids[j] = A.children[j];
+        wch[j] = A.wchild[j];
+    }
+    __syncthreads();
+    auto col = [&](T *X, int i) -> T & { return X[i * kThreads + tid]; };
+    // flow into node i: its pushed-down flow, or its one parent's sink flow
+    auto in_of = [&](int i) -> T { return npar[i] > 1 ? col(PN, i) : col(PT, par[i]); };
+    H_LOOP(A.n)
+    {
+        const long long c = t;
+        for (int i = 0; i < m; ++i) {
+            const long long o = (long long)i * A.n + c;
+            col(PT, i) = cnt[i] == 0 ? cts[i][c] : A.pt[o];
+            col(DV, i) = A.div[o];
+            col(U, i) = A.u[o];
+            col(PN, i) = (T)0;
+        }
+        // PushDownFlows, top-down
+        for (int j = 0; j < m; ++j) {
+            const int i = order[j];
+            const T pt = col(PT, i);
+            for (int k = 0; k < cnt[i]; ++k) {
+                const int ch = kids[first[i] + k];
+                if (npar[ch] > 1)
+                    col(PN, ch) = add(col(PN, ch), mul(wch[first[i] + k], pt));
+            }
+            if (npar[i] > 0 && cnt[i] > 0)
+                col(G, i) = add(sub(in_of(i), col(DV, i)), dvd(col(U, i), A.cc));
+            else if (npar[i] == 0)
+                col(G, i) = A.inv_cc;
+        }
+        // PushCapacityUp, bottom-up
+        for (int j = m - 1; j >= 0; --j) {
+            const int i = order[j];
+            if (cnt[i] == 0) {
+                const T x = add(sub(in_of(i), col(DV, i)), dvd(col(U, i), A.cc));
+                const T ct = col(PT, i);
+                col(PT, i) = (ct <= x || ct != ct) ? ct : x;
+                continue;
+            }
+            const T pto = col(PT, i);
+            T g = col(G, i);
+            for (int k = 0; k < cnt[i]; ++k) {
+                const int ch = kids[first[i] + k];
+                const T uc = dvd(col(U, ch), A.cc);
+                if (npar[ch] > 1) {
+                    const T w = wch[first[i] + k];
+                    const T e = sub(sub(add(add(col(DV, ch), col(PT, ch)), mul(w, pto)), col(PN, ch)), uc);
+                    g = add(g, mul(w, e));
+                } else {
+                    g = sub(add(add(g, col(DV, ch)), col(PT, ch)), uc);
+                }
+            }
+            col(G, i) = g;
+            col(PT, i) = dvd(g, wdiv[i]);
+        }
+        // labels, top-down
+        for (int j = 0; j < m; ++j) {
+            const int i = order[j];
+            if (npar[i] == 0)
+                continue;
+            col(U, i) = add(col(U, i), mul(A.cc, sub(sub(in_of(i), col(DV, i)), col(PT, i))));
+        }
+        for (int i = 0; i < m; ++i) {
+            const long long o = (long long)i * A.n + c;
+            A.pt[o] = col(PT, i);
+            if (npar[i] > 0)
+                A.u[o] = col(U, i);
+            if (npar[i] > 1)
+                A.pn[o] = col(PN, i);
+            if (cnt[i] > 0)
+                A.g[o] = col(G, i);
+        }
+    }
+}
+
 // The four spatial passes (k2 .. k5) fused for 2D solves without direction
 // fields: one block per (node, R x S tile of cells) computes, in shared
 // memory over the tile and a two-cell halo, the gradient step of the faces
@@ -976,11 +1177,16 @@ asets_status run_hmf(asets_context *ctx, int algo, int dim, int d1, int d2, int 
         set_last_error("asets_hmf_full_flow: out of device memory");
     } else if (e == cudaSuccess) {
         const int gp = h_grid(n, sms), gn = h_grid(n * (m - 1), sms);
+        // the staged per-pixel pass for trees whose columns fit the default
+        // 48 KB of shared memory (15 nodes in float, 7 in double)
+        const int k1_smem = K1Stage::bytes(m, (int)sizeof(T));
         if (dirs)
             k_norm_dirs<T><<<h_grid(n * m, sms), kThreads, 0, st>>>(A);
         for (int it = 0; it < its && e == cudaSuccess; ++it) {
             if (pseudo)
                 k_pseudo_point<T><<<gp, kThreads, 0, st>>>(A);
+            else if (k1_smem <= 48 * 1024)
+                k1_staged<T><<<gp, kThreads, k1_smem, st>>>(A);
             else
                 k1_pointwise<T><<<gp, kThreads, 0, st>>>(A);
             spatial_passes(A, gn, st, dirs);
@@ -1082,6 +1288,7 @@ asets_status run_dag(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
     A.steps = (T)steps;
     A.inv_cc = (T)(1.0 / cc);
     A.paren = 0;  // both DAG files: (p + g(k+1)) - g(k)
+    A.nedges = (int)kids.size();
     // child weights 1/(parents of the child); per node the sum of their squares
     std::vector<T> w(kids.size());
     std::vector<NodeDev<T>> nodes(m);
@@ -1172,13 +1379,19 @@ asets_status run_dag(asets_context *ctx, int dim, int d1, int d2, int d3, int m,
         set_last_error("asets_dag_full_flow: out of device memory");
     } else if (e == cudaSuccess) {
         const int gp = h_grid(n, sms), gn = h_grid(n * (m - 1), sms);
+        // the staged per-pixel pass for graphs whose columns fit the default
+        // 48 KB of shared memory (9 nodes in float, 4 in double)
+        const int dag_smem = DagStage::bytes(m, (int)kids.size(), (int)sizeof(T));
         k_dag_init<T><<<gp, kThreads, 0, st>>>(A);
         if (dirs)
             k_norm_dirs<T><<<h_grid(n * m, sms), kThreads, 0, st>>>(A);
         for (int it = 0; it < its && e == cudaSuccess; ++it) {
             k_dag_g<T><<<gn, kThreads, 0, st>>>(A);
             spatial_passes(A, gn, st, dirs);
-            k_dag_point<T><<<gp, kThreads, 0, st>>>(A);
+            if (dag_smem <= 48 * 1024)
+                k_dag_point_staged<T><<<gp, kThreads, dag_smem, st>>>(A);
+            else
+                k_dag_point<T><<<gp, kThreads, 0, st>>>(A);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess && dirs)
