@@ -734,9 +734,10 @@ __global__ void k_dag_point(const HArgs<T> A)
 // once per block.  Same operations in the same order as k_dag_point; pn, g
 // and u are stored for the nodes k_dag_point stores them for.
 struct DagStage {
-    // ints: parents, first parent, first child, child count, top-down order
-    // (5m) and the children list (E); then the weights: wdiv (m) and the
-    // child edges' (E); then the nodes' Ct pointers; then five columns
+    // ints: parent count, first parent, first child, child count, the
+    // top-down order (5m) and the children list (E); then the weights: wdiv
+    // (m) and the child edges' (E); then the nodes' Ct pointers; then the
+    // five per-thread columns of every node
     static constexpr int int_bytes(int m, int e) { return (4 * (5 * m + e) + 15) / 16 * 16; }
     static constexpr int w_bytes(int m, int e, int elem) { return (elem * (m + e) + 15) / 16 * 16; }
     static constexpr int table_bytes(int m, int e, int elem)
