@@ -448,9 +448,9 @@ def _per_iteration_s(solve, n: int) -> float:
     """Seconds per iteration of a synchronous host-array solve: the slope of
     the wall time of n-, 2n- and 4n-iteration solves (best of three each;
     copies and set-up do not depend on the iteration count).  While the
-    iterations are not at least half of the n-iteration solve's time, or the
-    slope is not positive, n grows fourfold (at most three times), so that
-    host copy noise cannot swamp the iteration time."""
+    iterations are not at least twice the fixed part of the n-iteration
+    solve's time, or the slope is not positive, n grows fourfold (at most
+    three times), so that host copy noise cannot swamp the iteration time."""
     import torch
 
     def wall(k):
@@ -468,7 +468,7 @@ def _per_iteration_s(solve, n: int) -> float:
         ks = np.array([n, 2 * n, 4 * n], float)
         ts = np.array([wall(int(k)) for k in ks])
         slope = float(np.polyfit(ks, ts, 1)[0])
-        if slope > 0 and slope * n >= 0.5 * ts[0]:
+        if slope > 0 and slope * n >= 2.0 * (ts[0] - slope * n):
             break
         n *= 4
     if slope <= 0:
@@ -498,7 +498,9 @@ def next_rows_run(ctx, stream, cpu: bool) -> list:
     device time per iteration (host-array solves: difference of two solve
     lengths; cost kernels: CUDA events on device arrays), rate against the
     algorithmic bytes, and (cpu) the numpy restatement timed on one core for
-    a few iterations of the same problem.  `stream` is the context's stream."""
+    a few iterations of the same problem, after every GPU row is timed (a
+    numpy restatement's large temporaries disturbed the next host-array
+    timing).  `stream` is the context's stream."""
     import torch
 
     from asetsmatlabmaxflow_gb300 import costs as K
@@ -510,6 +512,7 @@ def next_rows_run(ctx, stream, cpu: bool) -> list:
 
     peak, peak_kind = peaks()
     rows = []
+    pending_cpu = []
 
     def row(name, units, unit_name, bytes_per_unit, bytes_note, sec_per_it, cpu_fn=None,
             cpu_its=0, dtype="f32"):
@@ -521,13 +524,7 @@ def next_rows_run(ctx, stream, cpu: bool) -> list:
                           "frac": units * bytes_per_unit / sec_per_it / 1e9 / peak,
                           "peak_kind": peak_kind}}
         if cpu and cpu_fn is not None:
-            t = time.perf_counter()
-            cpu_fn(cpu_its)
-            s = (time.perf_counter() - t) / cpu_its
-            r["cpu_baseline"] = {"value": units / s / 1e9, "unit": f"G{unit_name}/s", "cores": 1,
-                                 "kind": "port",
-                                 "sample": f"{cpu_its} iterations incl. initialisation, numpy, "
-                                           "same problem"}
+            pending_cpu.append((r, cpu_fn, cpu_its, units, unit_name))
         rows.append(r)
 
     shape2 = (1024, 1024)
@@ -635,6 +632,14 @@ def next_rows_run(ctx, stream, cpu: bool) -> list:
             lambda: N.check(N.lib().asets_alpha_contrast(ctx.handle, N.DEVICE, img.data_ptr(),
                                                          256, 256, 256, 1, 0.1, 0.9, 10.0, 1, 1,
                                                          out.data_ptr()))))
+    for r, cpu_fn, cpu_its, units, unit_name in pending_cpu:
+        t = time.perf_counter()
+        cpu_fn(cpu_its)
+        sec = (time.perf_counter() - t) / cpu_its
+        r["cpu_baseline"] = {"value": units / sec / 1e9, "unit": f"G{unit_name}/s", "cores": 1,
+                             "kind": "port",
+                             "sample": f"{cpu_its} iterations incl. initialisation, numpy, "
+                                       "same problem"}
     return rows
 
 
