@@ -127,3 +127,48 @@ def test_geodesic_full_flow_matches_restatement(shape, dtype, kind):
         if r.lx is not None:
             for nm in names:
                 assert np.array_equal(_bits(getattr(q, nm)), _bits(getattr(r, nm))), nm
+
+
+@pytest.mark.parametrize("dtype,nodes", [(np.float64, 4), (np.float64, 5), (np.float32, 9),
+                                         (np.float32, 10)])
+def test_full_flow_on_graphs_either_side_of_the_staged_limit(dtype, nodes):
+    """The per-pixel pass keeps every node of a pixel in shared memory up to
+    9 nodes in float32 and 4 in float64, and reads them from global memory
+    beyond: both forms against the restatement, bit for bit."""
+    from asetsmatlabmaxflow_gb300.hmf import asetsDAGMF2D
+
+    shape = (19, 23)
+
+    def graph(make):
+        g = np.random.default_rng(nodes)
+        img = g.random(shape).astype(dtype)
+        if nodes <= 5:  # flat: root over nodes - 1 leaves
+            return make([make([], 0.15, np.abs(img - dtype(i / 3)).astype(dtype))
+                         for i in range(nodes - 1)], 0)
+        # root over three inner nodes sharing leaves, leaves 0 .. nodes - 5
+        L = [make([], 0.15, np.abs(img - dtype(i / 6)).astype(dtype)) for i in range(nodes - 4)]
+        a = make([L[0], L[1]], 0.2)
+        b = make([L[1], L[2]], 0.2)
+        c = make(L[2:], 0.1)
+        return make([a, b, c], 0)
+
+    ref, gpu = graph(Dg.Node), graph(asetsDAGMF2D)
+    ref.max_full_flow(15, 0.1, 0.25)
+    gpu.MaxFullFlow(15, 0.1, 0.25)
+
+    def order(root):
+        out, seen, st = [], set(), [root]
+        while st:
+            n = st.pop(0)
+            if id(n) not in seen:
+                seen.add(id(n))
+                out.append(n)
+                st.extend(n.C)
+        return out
+
+    assert len(order(gpu)) == nodes
+    for r, q in zip(order(ref), order(gpu)):
+        for name in ("u", "pt", "div", "g"):
+            assert np.array_equal(_bits(getattr(q, name)), _bits(getattr(r, name))), name
+        if len(r.P) > 1:
+            assert np.array_equal(_bits(q.pn), _bits(r.pn))

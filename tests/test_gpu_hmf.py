@@ -72,6 +72,47 @@ def test_full_flow_matches_restatement(shape, dtype, nested, alpha_array):
         assert np.isclose(q.reguCost, r.reguCost, rtol=rt, atol=1e-6)
 
 
+@pytest.mark.parametrize("dtype,nodes", [(np.float32, 15), (np.float32, 16), (np.float64, 7),
+                                         (np.float64, 8)])
+def test_full_flow_on_trees_either_side_of_the_staged_limit(dtype, nodes):
+    """The per-pixel pass keeps every node of a pixel in shared memory up to
+    15 nodes in float32 and 7 in float64, and reads them from global memory
+    beyond: both forms against the restatement, bit for bit."""
+    from asetsmatlabmaxflow_gb300.hmf import asetsHMF2D
+
+    shape = (21, 18)
+    g = np.random.default_rng(nodes)
+    img = g.random(shape).astype(dtype)
+
+    def tree(make):
+        # root -> inner nodes of two or three leaves each, then leaves
+        # under the root until `nodes` nodes
+        count, kids, lab = 1, [], 0
+        while count < nodes:
+            room = nodes - count
+            if room >= 4:
+                n = 3 if room >= 5 else 2
+                leaves = [make([], 0.15, np.sqrt(np.abs(img - dtype((lab + i) / 12))).astype(dtype))
+                          for i in range(n)]
+                lab += n
+                kids.append(make(leaves, 0.2))
+                count += 1 + n
+            else:
+                kids.append(make([], 0.1, np.abs(img - dtype(lab / 12)).astype(dtype)))
+                lab += 1
+                count += 1
+        return make(kids, 0)
+
+    ref, gpu = tree(H.Node), tree(asetsHMF2D)
+    assert len(gpu._nodes()) == nodes
+    ref.max_full_flow(15, 0.1, 0.2)
+    gpu.MaxFullFlow(15, 0.1, 0.2)
+    bits = lambda a: np.ascontiguousarray(a).view(np.uint64 if a.dtype == np.float64 else np.uint32)  # noqa: E731
+    for r, q in zip(H.preorder(ref), gpu._nodes()):
+        for name in ("u", "pt", "div", "g"):
+            assert np.array_equal(bits(getattr(q, name)), bits(getattr(r, name))), name
+
+
 def test_linear_model_denoises():
     """runTestHMFLinearModel.m: numLevels leaves with sqrt(|I - l/(L-1)|)
     costs under one root; the label-weighted reconstruction is closer to the
