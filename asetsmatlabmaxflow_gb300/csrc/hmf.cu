@@ -187,9 +187,9 @@ struct K1Stage {
     // the node table: parent, first child and child count per node and the
     // children list (4m ints), then the nodes' Ct pointers; then the three
     // per-thread columns (sink flow, divergence, label) of every node
-    static constexpr int ptr_off(int m) { return 16 * m; }
-    static constexpr int table_bytes(int m) { return 16 * m + (8 * m + 15) / 16 * 16; }
-    static constexpr int bytes(int m, int elem) { return table_bytes(m) + 3 * m * kThreads * elem; }
+    __host__ __device__ static constexpr int ptr_off(int m) { return 16 * m; }
+    __host__ __device__ static constexpr int table_bytes(int m) { return 16 * m + (8 * m + 15) / 16 * 16; }
+    __host__ __device__ static constexpr int bytes(int m, int elem) { return table_bytes(m) + 3 * m * kThreads * elem; }
 };
 
 template <class T>
@@ -738,13 +738,13 @@ struct DagStage {
     // top-down order (5m) and the children list (E); then the weights: wdiv
     // (m) and the child edges' (E); then the nodes' Ct pointers; then the
     // five per-thread columns of every node
-    static constexpr int int_bytes(int m, int e) { return (4 * (5 * m + e) + 15) / 16 * 16; }
-    static constexpr int w_bytes(int m, int e, int elem) { return (elem * (m + e) + 15) / 16 * 16; }
-    static constexpr int table_bytes(int m, int e, int elem)
+    __host__ __device__ static constexpr int int_bytes(int m, int e) { return (4 * (5 * m + e) + 15) / 16 * 16; }
+    __host__ __device__ static constexpr int w_bytes(int m, int e, int elem) { return (elem * (m + e) + 15) / 16 * 16; }
+    __host__ __device__ static constexpr int table_bytes(int m, int e, int elem)
     {
         return int_bytes(m, e) + w_bytes(m, e, elem) + (8 * m + 15) / 16 * 16;
     }
-    static constexpr int bytes(int m, int e, int elem)
+    __host__ __device__ static constexpr int bytes(int m, int e, int elem)
     {
         return table_bytes(m, e, elem) + 5 * m * kThreads * elem;
     }
@@ -857,12 +857,17 @@ __global__ void __launch_bounds__(kThreads) k_dag_point_staged(const HArgs<T> A)
 // (k5), with each pass's expression and validity tests, and stores the
 // tile's faces, divergence and factor (g) as the passes leave them.  The
 // halo's faces are recomputed by the neighbouring tiles' blocks; one read
-// and one write of each array instead of four passes over them.
+// and one write of each array instead of four passes over them.  The frame
+// is R + 4 = 32 rows high: lane q of every warp owns frame row q (y0 - 2 +
+// q) in every phase, and warp w the frame columns w, w + 8, ..., so a
+// thread's row tests are made once and a warp's loads and stores are one
+// 128-byte run of a column.
 template <class T, int R, int S>
 struct SpatialTile {
     static constexpr int FR = R + 4;   // frame cells y0-2 .. y0+R+1
     static constexpr int FC = S + 4;   // frame cells x0-2 .. x0+S+1
     static constexpr int F = FR * FC;
+    static_assert(FR == 32, "one frame row per lane");
     static constexpr int smem_bytes() { return 5 * F * (int)sizeof(T); }
 };
 
@@ -870,7 +875,7 @@ template <class T, int R, int S>
 __global__ void __launch_bounds__(kThreads) k_spatial_tile2d(const HArgs<T> A, int tiles_y)
 {
     using Q = SpatialTile<T, R, S>;
-    constexpr int FR = Q::FR, F = Q::F;
+    constexpr int FR = Q::FR, FC = Q::FC, F = Q::F, NW = kThreads / 32;
     extern __shared__ __align__(16) unsigned char hsm[];
     T *G = reinterpret_cast<T *>(hsm);   // g, at cells
     T *P1 = G + F;                        // face (y, y+1) at cell y
@@ -884,99 +889,102 @@ __global__ void __launch_bounds__(kThreads) k_spatial_tile2d(const HArgs<T> A, i
     const T *g = A.g + (long long)i * A.n;
     T *p1 = A.p1 + (long long)i * A.f1;
     T *p2 = A.p2 + (long long)i * A.f2;
-    const int tid = threadIdx.x;
-    for (int k = tid; k < F; k += kThreads) {
-        const int c = k / FR, q = k - c * FR;
-        const int y = y0 - 2 + q, x = x0 - 2 + c;
-        const bool in = (y >= 0 && y < d1 && x >= 0 && x < d2);
+    const int q = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int y = y0 - 2 + q;
+    const bool y_in = (y >= 0 && y < d1), y_up = (y + 1 < d1), y_dn = (y >= 1);
+    for (int c = w; c < FC; c += NW) {
+        const int x = x0 - 2 + c, f = c * FR + q;
+        const bool in = y_in && x >= 0 && x < d2;
         const unsigned int cell = (unsigned int)x * (unsigned int)d1 + (unsigned int)y;
-        G[k] = in ? g[cell] : (T)0;
-        P1[k] = (in && y + 1 < d1) ? p1[(unsigned int)x * (unsigned int)(d1 - 1) + (unsigned int)y] : (T)0;
-        P2[k] = (in && x + 1 < d2) ? p2[cell] : (T)0;
-        AL[k] = in ? (nd.alpha ? nd.alpha[cell] : nd.alpha_s) : (T)0;
+        G[f] = in ? g[cell] : (T)0;
+        P1[f] = (in && y_up) ? p1[(unsigned int)x * (unsigned int)(d1 - 1) + (unsigned int)y] : (T)0;
+        P2[f] = (in && x + 1 < d2) ? p2[cell] : (T)0;
+        AL[f] = in ? (nd.alpha ? nd.alpha[cell] : nd.alpha_s) : (T)0;
     }
     __syncthreads();
     // k2: 2D p + (g(k+1) - g(k)) (asetsHMF2D.m), else (p + g(k+1)) - g(k)
     auto step = [&](T pv, T gn, T gc) { return A.paren ? add(pv, sub(gn, gc)) : sub(add(pv, gn), gc); };
-    for (int k = tid; k < (R + 3) * (S + 2); k += kThreads) {   // p1: y0-2 .. y0+R, x0-1 .. x0+S
-        const int c = 1 + k / (R + 3), q = k % (R + 3);
-        const int f = c * FR + q;
-        const int y = y0 - 2 + q, x = x0 - 2 + c;
-        if (y >= 0 && y + 1 < d1 && x >= 0 && x < d2)
-            P1[f] = step(P1[f], G[f + 1], G[f]);
+    if (q <= R + 2 && y_in && y_up) {                            // p1: y0-2 .. y0+R, x0-1 .. x0+S
+        for (int c = 1 + w; c <= S + 2; c += NW) {
+            const int x = x0 - 2 + c, f = c * FR + q;
+            if (x >= 0 && x < d2)
+                P1[f] = step(P1[f], G[f + 1], G[f]);
+        }
     }
-    for (int k = tid; k < (R + 2) * (S + 3); k += kThreads) {   // p2: y0-1 .. y0+R, x0-2 .. x0+S
-        const int c = k / (R + 2), q = 1 + k % (R + 2);
-        const int f = c * FR + q;
-        const int y = y0 - 2 + q, x = x0 - 2 + c;
-        if (x >= 0 && x + 1 < d2 && y >= 0 && y < d1)
-            P2[f] = step(P2[f], G[f + FR], G[f]);
+    if (q >= 1 && q <= R + 2 && y_in) {                          // p2: y0-1 .. y0+R, x0-2 .. x0+S
+        for (int c = w; c <= S + 2; c += NW) {
+            const int x = x0 - 2 + c, f = c * FR + q;
+            if (x >= 0 && x + 1 < d2)
+                P2[f] = step(P2[f], G[f + FR], G[f]);
+        }
     }
     __syncthreads();
     // k3: the cell's faces' squares in the .m files' order, the factor
-    for (int k = tid; k < (R + 2) * (S + 2); k += kThreads) {   // y0-1 .. y0+R, x0-1 .. x0+S
-        const int c = 1 + k / (R + 2), q = 1 + k % (R + 2);
-        const int f = c * FR + q;
-        const int y = y0 - 2 + q, x = x0 - 2 + c;
-        if (y < 0 || y >= d1 || x < 0 || x >= d2)
-            continue;
-        T sq = (T)0;
-        if (y + 1 < d1)
-            sq = add(sq, mul(P1[f], P1[f]));
-        if (y >= 1)
-            sq = add(sq, mul(P1[f - 1], P1[f - 1]));
-        if (x + 1 < d2)
-            sq = add(sq, mul(P2[f], P2[f]));
-        if (x >= 1)
-            sq = add(sq, mul(P2[f - FR], P2[f - FR]));
-        const T mag = sqr(sq);
-        const T al = AL[f];
-        FS[f] = (mag <= al) ? (T)1 : dvd(al, mag);
+    if (q >= 1 && q <= R + 2 && y_in) {                          // y0-1 .. y0+R, x0-1 .. x0+S
+        for (int c = 1 + w; c <= S + 2; c += NW) {
+            const int x = x0 - 2 + c, f = c * FR + q;
+            if (x < 0 || x >= d2)
+                continue;
+            T sq = (T)0;
+            if (y_up)
+                sq = add(sq, mul(P1[f], P1[f]));
+            if (y_dn)
+                sq = add(sq, mul(P1[f - 1], P1[f - 1]));
+            if (x + 1 < d2)
+                sq = add(sq, mul(P2[f], P2[f]));
+            if (x >= 1)
+                sq = add(sq, mul(P2[f - FR], P2[f - FR]));
+            const T mag = sqr(sq);
+            const T al = AL[f];
+            FS[f] = (mag <= al) ? (T)1 : dvd(al, mag);
+        }
     }
     __syncthreads();
     // k4: p = 0.5 p (f(k+1) + f(k)); the tile's own faces are stored
-    for (int k = tid; k < (R + 1) * S; k += kThreads) {         // p1: y0-1 .. y0+R-1, tile columns
-        const int c = 2 + k / (R + 1), q = 1 + k % (R + 1);
-        const int f = c * FR + q;
-        const int y = y0 - 2 + q, x = x0 - 2 + c;
-        if (y < 0 || y + 1 >= d1 || x >= d2)
-            continue;
-        const T r = mul(mul((T)0.5, P1[f]), add(FS[f + 1], FS[f]));
-        P1[f] = r;
-        if (q >= 2)
-            p1[(unsigned int)x * (unsigned int)(d1 - 1) + (unsigned int)y] = r;
+    if (q >= 1 && q <= R + 1 && y >= 0 && y_up) {                // p1: y0-1 .. y0+R-1, tile columns
+        for (int c = 2 + w; c <= S + 1; c += NW) {
+            const int x = x0 - 2 + c, f = c * FR + q;
+            if (x >= d2)
+                break;
+            const T r = mul(mul((T)0.5, P1[f]), add(FS[f + 1], FS[f]));
+            P1[f] = r;
+            if (q >= 2)
+                p1[(unsigned int)x * (unsigned int)(d1 - 1) + (unsigned int)y] = r;
+        }
     }
-    for (int k = tid; k < R * (S + 1); k += kThreads) {         // p2: tile rows, x0-1 .. x0+S-1
-        const int c = 1 + k / R, q = 2 + k % R;
-        const int f = c * FR + q;
-        const int y = y0 - 2 + q, x = x0 - 2 + c;
-        if (x < 0 || x + 1 >= d2 || y >= d1)
-            continue;
-        const T r = mul(mul((T)0.5, P2[f]), add(FS[f + FR], FS[f]));
-        P2[f] = r;
-        if (c >= 2)
-            p2[(unsigned int)x * (unsigned int)d1 + (unsigned int)y] = r;
+    if (q >= 2 && q <= R + 1 && y < d1) {                        // p2: tile rows, x0-1 .. x0+S-1
+        for (int c = 1 + w; c <= S + 1; c += NW) {
+            const int x = x0 - 2 + c, f = c * FR + q;
+            if (x + 1 >= d2)
+                break;
+            if (x < 0)
+                continue;
+            const T r = mul(mul((T)0.5, P2[f]), add(FS[f + FR], FS[f]));
+            P2[f] = r;
+            if (c >= 2)
+                p2[(unsigned int)x * (unsigned int)d1 + (unsigned int)y] = r;
+        }
     }
     __syncthreads();
     // k5: the tile's divergence; g keeps the factor, as k3 leaves it
     T *divp = A.div + (long long)i * A.n;
     T *gw = A.g + (long long)i * A.n;
-    for (int k = tid; k < R * S; k += kThreads) {
-        const int c = 2 + k / R, q = 2 + k % R;
-        const int f = c * FR + q;
-        const int y = y0 - 2 + q, x = x0 - 2 + c;
-        if (y >= d1 || x >= d2)
-            continue;
-        T d = (y + 1 < d1) ? P1[f] : (T)0;
-        if (y >= 1)
-            d = sub(d, P1[f - 1]);
-        if (x + 1 < d2)
-            d = add(d, P2[f]);
-        if (x >= 1)
-            d = sub(d, P2[f - FR]);
-        const unsigned int cell = (unsigned int)x * (unsigned int)d1 + (unsigned int)y;
-        divp[cell] = d;
-        gw[cell] = FS[f];
+    if (q >= 2 && q <= R + 1 && y < d1) {
+        for (int c = 2 + w; c <= S + 1; c += NW) {
+            const int x = x0 - 2 + c, f = c * FR + q;
+            if (x >= d2)
+                break;
+            T d = y_up ? P1[f] : (T)0;
+            if (y_dn)
+                d = sub(d, P1[f - 1]);
+            if (x + 1 < d2)
+                d = add(d, P2[f]);
+            if (x >= 1)
+                d = sub(d, P2[f - FR]);
+            const unsigned int cell = (unsigned int)x * (unsigned int)d1 + (unsigned int)y;
+            divp[cell] = d;
+            gw[cell] = FS[f];
+        }
     }
 }
 
@@ -993,9 +1001,9 @@ template <class T>
 void spatial_passes(const HArgs<T> &A, int gn, cudaStream_t st, bool dirs)
 {
     if (A.dim == 2 && !dirs && A.m > 1) {
-        // 32 x 32 tiles in float, 16 x 32 in double: the frame stays within
-        // the default 48 KB of dynamic shared memory
-        constexpr int R = sizeof(T) == 8 ? 16 : 32, S = 32;
+        // 28 x 32 tiles: a 32-row frame (one row per lane), within the
+        // default 48 KB of dynamic shared memory in double as well
+        constexpr int R = 28, S = 32;
         using Q = SpatialTile<T, R, S>;
         static_assert(Q::smem_bytes() <= 48 * 1024, "frame above the default shared memory");
         const int ty = (A.d1 + R - 1) / R, tx = (A.d2 + S - 1) / S;
