@@ -346,6 +346,8 @@ struct Around {
             zu = cell[has_zu ? g + pl : g];
             p = f3[fp];
             q = f3[j3(A, c.y, c.x, c.z + 1)];
+        } else {
+            zl = zu = p = q = (T)0;  // no slices: unused
         }
     }
 };
