@@ -8,7 +8,8 @@
 //   K1 per pixel, all nodes: sink flows children-first (UpdateSinkFlows),
 //      then the labels (UpdateLabels), then g = steps*(div + pt - P.pt - u/cc)
 //      of every non-root node (the first line of UpdateSpatialFlows) -- all
-//      per-pixel, so one pass;
+//      per-pixel, so one pass (with the pixel's nodes staged in shared
+//      memory when they fit, k1_staged);
 //   K2 gradient step of the spatial flows, K3 flow magnitude and projection
 //   factor, K4 flow rescale, K5 divergence (the rest of UpdateSpatialFlows);
 //   in 2D without direction fields one tiled kernel runs K2-K5.
